@@ -1,0 +1,214 @@
+/*
+ * spacetime_gb300.h -- C ABI of libspacetime_gb300.so, the GB300 (sm_103a)
+ * implementation of SpaceTime.jl's per-pixel null-geodesic render path.
+ *
+ * Plain C: POD structs, pointers and sizes, integer status codes, no C++
+ * exceptions across the boundary.  A Julia `ccall`, Python `ctypes` or any
+ * C caller binds it directly.
+ *
+ * Reference interfaces replaced (paths within SpaceTime.jl):
+ *   st_context_create      MetalPreviewContext(bg, w, h; dt, nmax, disc, volume)
+ *                          src/metal.jl:129-182 (sky uploaded once, :111-121, :134)
+ *   st_context_set_disc    the disc block of MetalPreviewContext, src/metal.jl:140-154,
+ *                          and set_disc_enabled!, src/metal.jl:206-214
+ *   st_context_set_volume  the volume block of MetalPreviewContext, src/metal.jl:155-166,
+ *                          set_volume_enabled! / set_march_stride!, src/metal.jl:192-308
+ *   st_render              render(cam, bh, sky; disc, width, height, samples, relativistic)
+ *                          src/raytrace.jl:339-428 (semantics ST_SEM_RENDER), and
+ *                          render_draft_mtl(ctx, cam, st; width, height, samples, dt,
+ *                          fisheye_deg, aperture_world, focus_dist, relativistic, order)
+ *                          src/metal.jl:2040-2242 (semantics ST_SEM_DRAFT)
+ *   st_render_frames       the per-frame loop of examples/videos/*.jl over
+ *                          render_draft_mtl, batched into one persistent launch
+ *   st_render_device       _trace_preview_gpu!, src/metal.jl:1825-1881 (result left
+ *                          on the device, no download)
+ *   st_camera_tetrad       ks_camera_tetrad + camera_beta, src/preview.jl:93-198,
+ *                          src/camera.jl:19-22
+ *
+ * Output layout: linear HDR RGB float32 in the reference's column-major
+ * (3, width, height) order, i.e. out[3*(i + width*j) + c] for 0-based pixel
+ * (i, j); row j = 0 is the bottom of the frame (v < 0), as in
+ * src/metal.jl:870-872 and src/camera.jl:391-396.
+ *
+ * Threading: one context is single-threaded (one CUDA stream).  Independent
+ * contexts may be driven from different host threads.  st_render is
+ * synchronous: it returns after the device-to-host copy.
+ */
+#ifndef SPACETIME_GB300_H
+#define SPACETIME_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ST_ABI_VERSION 1
+
+typedef struct st_context st_context;
+
+/* status codes; ST_EINVAL mirrors the reference's ArgumentError (src/gr.jl:31) */
+enum {
+  ST_OK = 0,
+  ST_EINVAL = 1,        /* bad argument: |a| > M, sizes <= 0, NULL pointer, ... */
+  ST_ECUDA = 2,         /* a CUDA runtime call failed */
+  ST_EBUDGET = 3,       /* the persistent queue hit its iteration budget */
+  ST_ENOMEM = 4,        /* device or host allocation failed */
+  ST_EUNSUPPORTED = 5,  /* combination not provided (e.g. Kerr with ST_SEM_RENDER) */
+  ST_ESTATE = 6         /* context not ready (e.g. surrogate requested, none loaded) */
+};
+
+enum { ST_PROJ_PINHOLE = 0, ST_PROJ_FISHEYE = 1 };
+/* disc emitter model: the CPU renderer's Keplerian Planck-Doppler shading
+ * (src/accretion_disc.jl:19-49) or the kernel's exact Kerr-Schild emitter
+ * (src/metal.jl:396-428) */
+enum { ST_EMIT_KEPLER = 0, ST_EMIT_KS_EXACT = 1 };
+/* which reference path's rules are reproduced (they differ on purpose):
+ * RENDER = src/raytrace.jl render (horizon 2.00001, r_max, affine budget,
+ * black iff r < 2.1M); DRAFT = src/metal.jl trace_kernel_mtl! (photon-orbit
+ * and 2.95M kill tests, Bardeen launch test, black iff r < 4M). */
+enum { ST_SEM_RENDER = 0, ST_SEM_DRAFT = 1 };
+/* arithmetic of the geodesic integration */
+enum {
+  ST_PREC_FP64 = 0,          /* everything in double */
+  ST_PREC_FP32_GUARDED = 1,  /* FP32 RK4 with a compensated (float-float) state;
+                                FP64 for steps inside r_guard, for rays in the
+                                critical band, and for the null-constraint
+                                renormalisation */
+  ST_PREC_FP32 = 2           /* plain FP32, as the reference's Metal kernel */
+};
+/* launch schedule */
+enum {
+  ST_SCHED_PIXEL = 0,       /* one thread per pixel, 2-D tiles */
+  ST_SCHED_PERSISTENT = 1   /* persistent CTAs, device ray queue, per-lane refill */
+};
+
+typedef struct {
+  double pos[3];
+  double fwd[3], right[3], up[3];  /* orthonormal camera axes (world frame) */
+  double fov_factor;               /* tan(half vertical fov); Lens(f) -> 18/f */
+  double velocity[3];              /* world-frame 3-velocity in units of c */
+  int projection;                  /* ST_PROJ_* */
+  double fisheye_deg;              /* fisheye half-angle at the top edge */
+  double aperture_world;           /* thin-lens aperture diameter; 0 = pinhole */
+  double focus_dist;               /* thin-lens focus distance (world units) */
+} st_camera;
+
+typedef struct {
+  double M; /* mass */
+  double a; /* spin, |a| <= M; 0 = Schwarzschild */
+} st_spacetime;
+
+typedef struct {
+  double inner, outer;       /* annulus radii; inner <= 0 disables the disc */
+  double falloff;            /* density_falloff */
+  double wb_temperature;     /* Blackbody(wb_temperature=...) */
+  double table_min, table_max;
+  int table_size;
+  int emitter;               /* ST_EMIT_* */
+} st_disc;
+
+typedef struct {
+  const float* density;      /* (nr, nphi, nz) column-major, peak-normalised */
+  int nr, nphi, nz;
+  float log_s_in, log_s_out, z_max;
+  float emission_scale, opacity_scale;
+  int march_stride;          /* gas sampled every march_stride*dt of arc, 1..16 */
+} st_volume;
+
+typedef struct {
+  int width, height;
+  int samples;               /* samples^2 stratified passes per pixel */
+  double dt;                 /* base affine step */
+  int nmax;                  /* step budget; 0 = the reference's rule */
+  int semantics;             /* ST_SEM_* */
+  int precision;             /* ST_PREC_* */
+  int schedule;              /* ST_SCHED_* */
+  double r_escape;           /* DRAFT escape radius / RENDER r_max; 0 = rule */
+  double tspan;              /* RENDER affine budget; 0 = rule */
+  int relativistic;          /* per-ray camera/infinity shift on shading */
+  int exit_landing;          /* land exactly on r_escape before reading the sky */
+  int pixel_jitter;          /* per-pixel hashed jitter inside each stratum */
+  unsigned long long seed;   /* pass shuffles and hash seeds */
+  double r_guard;            /* FP32_GUARDED: FP64 steps inside this KS radius */
+  double crit_band;          /* FP32_GUARDED: |b - b_crit| band (Schwarzschild) */
+  int renorm_every;          /* FP32_GUARDED: FP64 null renormalisation period */
+  int surrogate;             /* 1 = gate + learned surrogate (st_surrogate_*) */
+  double surrogate_sigma;    /* gate: max predicted std-dev (rad) served */
+  int block_x, block_y;      /* ST_SCHED_PIXEL tile; 0 = tuned default */
+  int chunk_steps;           /* ST_SCHED_PERSISTENT steps per refill check */
+} st_render_params;
+
+typedef struct {
+  double total_ms;           /* wall time of the call */
+  double kernel_ms;          /* device time of the trace kernels (CUDA events) */
+  unsigned long long rays;
+  unsigned long long steps;        /* accepted integration steps */
+  unsigned long long fp64_steps;   /* of which ran in FP64 */
+  unsigned long long gas_samples;
+  unsigned long long surrogate_rays;
+  int launches;              /* trace-kernel launches issued */
+  int status;                /* ST_OK or the persistent queue's status */
+  unsigned long long h2d_bytes, d2h_bytes;
+} st_stats;
+
+/* per-ray record (st_render_diag) */
+typedef struct {
+  float dir[3];              /* unit escape direction (coordinate velocity) */
+  int flags;                 /* ST_RAY_* */
+  float r_final, alpha, r_cross, g_cross;
+  int steps, fp64_steps;
+  float lambda;
+  int pad;
+} st_ray_diag;
+
+enum {
+  ST_RAY_ESCAPED = 1, ST_RAY_CAPTURED = 2, ST_RAY_BUDGET = 4, ST_RAY_BLACK = 8,
+  ST_RAY_CROSSED = 16, ST_RAY_GRAZE = 32, ST_RAY_BCAPT = 64, ST_RAY_SURROGATE = 128,
+  ST_RAY_GUARDED = 256
+};
+
+int st_abi_version(void);
+const char* st_strerror(int code);
+
+/* Fill *p with the defaults of the given semantics (the reference's keyword
+ * defaults: dt 0.02, samples 1, rule-based nmax / r_escape / tspan). */
+void st_render_params_default(st_render_params* p, int semantics);
+
+/* Create a context on `device`; copies the (3, sky_w, sky_h) float sky to HBM. */
+int st_context_create(st_context** out, const float* sky_rgb, int sky_w, int sky_h, int device);
+/* NULL disables the thin disc. */
+int st_context_set_disc(st_context* ctx, const st_disc* disc);
+/* NULL disables the volume; the density grid is copied to HBM. */
+int st_context_set_volume(st_context* ctx, const st_volume* vol);
+void st_context_destroy(st_context* ctx);
+
+/* Render one frame into caller-owned host memory out_rgb[3*width*height]. */
+int st_render(st_context* ctx, const st_camera* cam, const st_spacetime* st,
+              const st_render_params* p, float* out_rgb, st_stats* stats);
+
+/* As st_render, also writing one st_ray_diag per pixel of the last pass. */
+int st_render_diag(st_context* ctx, const st_camera* cam, const st_spacetime* st,
+                   const st_render_params* p, float* out_rgb, st_ray_diag* diag,
+                   st_stats* stats);
+
+/* Render and leave the frame on the device: *dev_rgba receives a pointer to
+ * the context's float4 [height][width] framebuffer (valid until the next call). */
+int st_render_device(st_context* ctx, const st_camera* cam, const st_spacetime* st,
+                     const st_render_params* p, const float** dev_rgba, st_stats* stats);
+
+/* Render `nframes` camera poses (a camera track) in one persistent launch;
+ * out_rgb holds nframes frames back to back. */
+int st_render_frames(st_context* ctx, int nframes, const st_camera* cams,
+                     const st_spacetime* st, const st_render_params* p,
+                     float* out_rgb, st_stats* stats);
+
+/* The camera's orthonormal Kerr-Schild tetrad (u, Ef, Er, Eu), each a
+ * contravariant (t, x, y, z) 4-vector, boosted by the camera velocity. */
+int st_camera_tetrad(const st_camera* cam, const st_spacetime* st, double out16[16]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPACETIME_GB300_H */

@@ -1,0 +1,274 @@
+"""Python host API over the C ABI, mirroring SpaceTime.jl's render interface.
+
+    Schwarzschild(M), Kerr(M, a)                 src/gr.jl:7-34
+    Blackbody(...), AccretionDisc(...)           src/blackbody.jl:42-60, src/accretion_disc.jl:5-13
+    Lens(f), Camera                              src/raytrace.jl:22-29, src/camera.jl:36-50
+    render(cam, bh, sky; disc, width, height)    src/raytrace.jl:339-428
+    Context(sky; disc, volume)                   MetalPreviewContext, src/metal.jl:129-182
+    render_draft(ctx, cam, bh; ...)              render_draft_mtl, src/metal.jl:2040-2242
+
+Images come back as float32 arrays of shape (height, width, 3): element
+[j, i] is pixel (i, j) of the reference's Matrix{RGBf}(width, height), i.e.
+the same bytes as its column-major (3, width, height) buffer.  Row j = 0 is
+the bottom of the frame.  Every call runs the CUDA library; there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from .scene import Camera, Volume, lens_fov
+
+__all__ = [
+    "Schwarzschild", "Kerr", "Blackbody", "AccretionDisc", "Lens", "Camera", "Context",
+    "render", "render_draft", "render_frames", "camera_tetrad", "RenderResult",
+]
+
+
+@dataclass(frozen=True)
+class Schwarzschild:
+    M: float = 1.0
+
+    @property
+    def a(self) -> float:
+        return 0.0
+
+
+@dataclass(frozen=True)
+class Kerr:
+    M: float
+    a: float
+
+    def __post_init__(self):
+        if not abs(self.a) <= self.M:
+            # src/gr.jl:31: ArgumentError("|a| must be <= M")
+            raise ValueError(f"|a| must be <= M (got a={self.a}, M={self.M})")
+
+
+@dataclass(frozen=True)
+class Blackbody:
+    wb_temperature: float = 6500.0
+    table_min: float = 500.0
+    table_max: float = 30000.0
+    table_size: int = 1024
+
+
+@dataclass(frozen=True)
+class AccretionDisc:
+    inner_radius: float = 3.0
+    outer_radius: float = 20.0
+    blackbody: Blackbody = field(default_factory=Blackbody)
+    density_falloff: float = 0.0
+
+
+@dataclass(frozen=True)
+class Lens:
+    focal_length: float
+
+    @property
+    def fov_factor(self) -> float:
+        return lens_fov(self.focal_length)
+
+
+@dataclass
+class RenderResult:
+    image: np.ndarray
+    stats: dict
+    diag: np.ndarray | None = None
+
+
+def _st_camera(cam: Camera) -> _abi.StCamera:
+    c = _abi.StCamera()
+    c.pos[:] = [float(v) for v in cam.pos]
+    c.fwd[:] = [float(v) for v in cam.fwd]
+    c.right[:] = [float(v) for v in cam.right]
+    c.up[:] = [float(v) for v in cam.up_local]
+    c.fov_factor = float(cam.fov_factor)
+    c.velocity[:] = [float(v) for v in cam.velocity]
+    c.projection = int(cam.projection)
+    c.fisheye_deg = float(cam.fisheye_deg)
+    c.aperture_world = float(cam.aperture_world)
+    c.focus_dist = float(cam.focus_dist)
+    return c
+
+
+def _st_spacetime(bh) -> _abi.StSpacetime:
+    return _abi.StSpacetime(float(bh.M), float(getattr(bh, "a", 0.0)))
+
+
+def camera_tetrad(cam: Camera, bh) -> np.ndarray:
+    """(u, Ef, Er, Eu) as a 4x4 array (rows), src/preview.jl:93-198."""
+    lib = _abi.load()
+    out = (C.c_double * 16)()
+    _abi.check(lib.st_camera_tetrad(C.byref(_st_camera(cam)), C.byref(_st_spacetime(bh)), out),
+               "st_camera_tetrad")
+    return np.array(out[:]).reshape(4, 4)
+
+
+class Context:
+    """Device-resident sky, blackbody table and gas grid (MetalPreviewContext)."""
+
+    def __init__(self, sky: np.ndarray, disc: AccretionDisc | None = None, volume: Volume | None = None,
+                 emitter: int | None = None, device: int = 0):
+        self._lib = _abi.load()
+        sky = np.ascontiguousarray(sky, dtype=np.float32)
+        if sky.ndim != 3 or sky.shape[2] != 3:
+            raise ValueError("sky must be (height, width, 3) float32")
+        h, w, _ = sky.shape
+        handle = C.c_void_p()
+        _abi.check(self._lib.st_context_create(C.byref(handle), sky.ctypes.data_as(C.POINTER(C.c_float)),
+                                               w, h, device), "st_context_create")
+        self._h = handle
+        self.sky_shape = (w, h)
+        self.disc = None
+        self.volume = None
+        self.emitter = emitter
+        self.set_disc(disc, emitter)
+        self.set_volume(volume)
+
+    def set_disc(self, disc: AccretionDisc | None, emitter: int | None = None):
+        if disc is None:
+            _abi.check(self._lib.st_context_set_disc(self._h, None), "st_context_set_disc")
+            self.disc = None
+            return
+        bb = disc.blackbody
+        em = _abi.ST_EMIT_KS_EXACT if emitter is None else emitter
+        d = _abi.StDisc(disc.inner_radius, disc.outer_radius, disc.density_falloff, bb.wb_temperature,
+                        bb.table_min, bb.table_max, bb.table_size, em)
+        _abi.check(self._lib.st_context_set_disc(self._h, C.byref(d)), "st_context_set_disc")
+        self.disc = disc
+        self.emitter = em
+
+    def set_volume(self, vol: Volume | None):
+        if vol is None:
+            _abi.check(self._lib.st_context_set_volume(self._h, None), "st_context_set_volume")
+            self.volume = None
+            return
+        dens = np.ascontiguousarray(vol.density, dtype=np.float32)
+        nr, nphi, nz = vol.shape
+        v = _abi.StVolume(dens.ctypes.data_as(C.POINTER(C.c_float)), nr, nphi, nz, vol.log_s_in,
+                          vol.log_s_out, vol.z_max, vol.emission_scale, vol.opacity_scale, vol.march_stride)
+        _abi.check(self._lib.st_context_set_volume(self._h, C.byref(v)), "st_context_set_volume")
+        self.volume = vol
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.st_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- low level ------------------------------------------------------------
+    def params(self, semantics: int, **kw) -> _abi.StRenderParams:
+        p = _abi.StRenderParams()
+        self._lib.st_render_params_default(C.byref(p), semantics)
+        for k, v in kw.items():
+            if not hasattr(p, k):
+                raise TypeError(f"unknown render parameter {k!r}")
+            setattr(p, k, v)
+        return p
+
+    def render_raw(self, cam: Camera, bh, p: _abi.StRenderParams, diag: bool = False,
+                   out: np.ndarray | None = None) -> RenderResult:
+        img = out if out is not None else np.empty((p.height, p.width, 3), dtype=np.float32)
+        stats = _abi.StStats()
+        cam_c, st_c = _st_camera(cam), _st_spacetime(bh)
+        fptr = img.ctypes.data_as(C.POINTER(C.c_float))
+        if diag:
+            d = np.empty(p.height * p.width, dtype=_abi.DIAG_DTYPE)
+            rc = self._lib.st_render_diag(self._h, C.byref(cam_c), C.byref(st_c), C.byref(p), fptr,
+                                          C.c_void_p(d.ctypes.data), C.byref(stats))
+            _abi.check(rc, "st_render_diag")
+            return RenderResult(img, stats.as_dict(), d.reshape(p.height, p.width))
+        rc = self._lib.st_render(self._h, C.byref(cam_c), C.byref(st_c), C.byref(p), fptr, C.byref(stats))
+        _abi.check(rc, "st_render")
+        return RenderResult(img, stats.as_dict())
+
+    def render_device(self, cam: Camera, bh, p: _abi.StRenderParams) -> tuple[int, dict]:
+        """Render, leaving the float4 frame on the device; returns its address."""
+        stats = _abi.StStats()
+        ptr = C.c_void_p()
+        rc = self._lib.st_render_device(self._h, C.byref(_st_camera(cam)), C.byref(_st_spacetime(bh)),
+                                        C.byref(p), C.byref(ptr), C.byref(stats))
+        _abi.check(rc, "st_render_device")
+        return ptr.value, stats.as_dict()
+
+    def render_frames_raw(self, cams, bh, p: _abi.StRenderParams) -> RenderResult:
+        n = len(cams)
+        arr = (_abi.StCamera * n)(*[_st_camera(c) for c in cams])
+        img = np.empty((n, p.height, p.width, 3), dtype=np.float32)
+        stats = _abi.StStats()
+        rc = self._lib.st_render_frames(self._h, n, arr, C.byref(_st_spacetime(bh)), C.byref(p),
+                                        img.ctypes.data_as(C.POINTER(C.c_float)), C.byref(stats))
+        _abi.check(rc, "st_render_frames")
+        return RenderResult(img, stats.as_dict())
+
+
+_PREC = {"fp64": _abi.ST_PREC_FP64, "fp32": _abi.ST_PREC_FP32, "fp32g": _abi.ST_PREC_FP32_GUARDED,
+         "fp32_guarded": _abi.ST_PREC_FP32_GUARDED}
+
+
+def _prec(x):
+    return _PREC[x] if isinstance(x, str) else int(x)
+
+
+def render(cam: Camera, bh, sky: np.ndarray, *, disc: AccretionDisc | None = AccretionDisc(),
+           width: int = 400, height: int = 200, samples: int = 1, relativistic: bool = False,
+           precision="fp64", dt: float = 0.02, jittered: bool = False, seed: int = 0,
+           context: Context | None = None, **kw) -> np.ndarray:
+    """The CPU renderer's call, `render(cam, bh, sky; disc, width, height,
+    samples, relativistic)` (src/raytrace.jl:339-428), on the GPU: horizon at
+    r = 2.00001, escape at r_max = max(5|pos|, 100), affine budget
+    max(10|pos|, 500), Keplerian Planck-Doppler disc, black iff r < 2.1M.
+    `jittered=False` places samples at stratum centres (the reference's
+    `jittered=false`); jittered samples are hashed per pixel, not drawn from
+    Julia's Xoshiro stream."""
+    if not isinstance(bh, Schwarzschild) and getattr(bh, "a", 0.0) != 0.0:
+        # the reference has no render(cam, ::Kerr, ...) method
+        raise TypeError("render: the CPU-renderer semantics are Schwarzschild-only; use render_draft")
+    ctx = context or Context(sky, disc=disc, emitter=_abi.ST_EMIT_KEPLER)
+    try:
+        p = ctx.params(_abi.ST_SEM_RENDER, width=width, height=height, samples=samples,
+                       relativistic=int(relativistic), precision=_prec(precision), dt=dt,
+                       pixel_jitter=int(jittered), seed=seed, **kw)
+        return ctx.render_raw(cam, bh, p).image
+    finally:
+        if context is None:
+            ctx.close()
+
+
+def render_draft(ctx: Context, cam: Camera, bh, *, width: int = 1920, height: int = 1080, samples: int = 2,
+                 dt: float = 0.02, fisheye_deg: float = 0.0, aperture_world: float = 0.0,
+                 focus_dist: float = 1.0, relativistic: bool = False, precision="fp32",
+                 pixel_jitter: bool = True, seed: int = 0, **kw) -> np.ndarray:
+    """render_draft_mtl(ctx, cam, st; width, height, samples, dt, fisheye_deg,
+    aperture_world, focus_dist, relativistic) (src/metal.jl:2040-2242)."""
+    cam2 = Camera(cam.pos, cam.fwd, cam.right, cam.up_local, cam.fov_factor, cam.velocity,
+                  _abi.ST_PROJ_FISHEYE if fisheye_deg > 0 else _abi.ST_PROJ_PINHOLE, fisheye_deg,
+                  aperture_world, focus_dist)
+    p = ctx.params(_abi.ST_SEM_DRAFT, width=width, height=height, samples=samples, dt=dt,
+                   relativistic=int(relativistic), precision=_prec(precision),
+                   pixel_jitter=int(pixel_jitter), seed=seed, **kw)
+    return ctx.render_raw(cam2, bh, p).image
+
+
+def render_frames(ctx: Context, cams, bh, *, width: int, height: int, dt: float = 0.02, precision="fp32g",
+                  **kw) -> np.ndarray:
+    """A camera track rendered in one persistent launch (DRAFT semantics)."""
+    p = ctx.params(_abi.ST_SEM_DRAFT, width=width, height=height, samples=1, dt=dt,
+                   precision=_prec(precision), pixel_jitter=0, schedule=_abi.ST_SCHED_PERSISTENT, **kw)
+    return ctx.render_frames_raw(cams, bh, p).image

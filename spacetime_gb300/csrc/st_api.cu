@@ -1,0 +1,751 @@
+// st_api.cu -- host side of libspacetime_gb300.so: the C ABI declared in
+// include/spacetime_gb300.h.  FP64 host work (camera tetrad, blackbody LUT,
+// reference step/escape rules) plus device-memory management and launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "st_internal.h"
+
+namespace st {
+cudaError_t launch_trace_fp64(const Variant&, const TraceParams&, int, int, int, cudaStream_t);
+cudaError_t launch_trace_fp32(const Variant&, const TraceParams&, int, int, int, cudaStream_t);
+cudaError_t launch_trace_fp32_guarded(const Variant&, const TraceParams&, int, int, int, cudaStream_t);
+int variant_registers_fp64(const Variant&);
+int variant_registers_fp32(const Variant&);
+int variant_registers_fp32_guarded(const Variant&);
+
+cudaError_t launch_trace(const Variant& v, const TraceParams& p, int bx, int by, int num_sms, cudaStream_t s) {
+  switch (v.prec) {
+    case ST_PREC_FP64: return launch_trace_fp64(v, p, bx, by, num_sms, s);
+    case ST_PREC_FP32: return launch_trace_fp32(v, p, bx, by, num_sms, s);
+    default: return launch_trace_fp32_guarded(v, p, bx, by, num_sms, s);
+  }
+}
+
+int variant_registers(const Variant& v) {
+  switch (v.prec) {
+    case ST_PREC_FP64: return variant_registers_fp64(v);
+    case ST_PREC_FP32: return variant_registers_fp32(v);
+    default: return variant_registers_fp32_guarded(v);
+  }
+}
+
+__global__ void pack_rgb_kernel(const float4* __restrict__ fb, float* __restrict__ rgb, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const float4 c = fb[i];
+    rgb[3 * i + 0] = c.x;
+    rgb[3 * i + 1] = c.y;
+    rgb[3 * i + 2] = c.z;
+  }
+}
+
+cudaError_t launch_pack_rgb(const float4* fb, float* rgb, int n, cudaStream_t s) {
+  pack_rgb_kernel<<<(n + 255) / 256, 256, 0, s>>>(fb, rgb, n);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// FP64 host physics (the reference computes these on the CPU in Float64).
+// ---------------------------------------------------------------------------
+
+struct V4 { double c[4]; };
+
+static double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// ks_camera_tetrad (src/preview.jl:93-198): static / 2.5M free-faller
+// observer (a = 0) or static->ZAMO blend (a != 0), Gram-Schmidt under the KS
+// metric with forward first, then the Lorentz boost by beta.
+static void host_tetrad(const double* pos, const double* fwd, const double* right, const double* up, double M,
+                        double a, const double* beta, double* U, double* Ef, double* Er, double* Eu) {
+  double l[3], f, u[4];
+  if (a == 0.0) {
+    const double r = std::sqrt(dot3(pos, pos));
+    for (int k = 0; k < 3; ++k) l[k] = pos[k] / r;
+    f = 2.0 * M / r;
+    const double E = std::sqrt(std::max(1.0 - 2.0 / 2.5, 1.0 - f));
+    const double v = -std::sqrt(std::max(E * E - (1.0 - f), 0.0));
+    const double w = (1.0 - E * (E - v)) / (E - v);
+    const double lu = E + w;
+    u[0] = E + f * lu;
+    for (int k = 0; k < 3; ++k) u[k + 1] = (w - f * lu) * l[k];
+  } else {
+    const double x = pos[0], y = pos[1], z = pos[2], a2 = a * a;
+    const double wq = x * x + y * y + z * z - a2;
+    const double rk2 = 0.5 * (wq + std::sqrt(wq * wq + 4.0 * a2 * z * z));
+    const double rk = std::sqrt(std::max(rk2, 1e-12));
+    const double ira = 1.0 / (rk2 + a2);
+    l[0] = (rk * x + a * y) * ira;
+    l[1] = (rk * y - a * x) * ira;
+    l[2] = z / rk;
+    const double sig = rk2 * rk2 + a2 * z * z;
+    f = 2.0 * M * rk2 * rk / sig;
+    const double delta = std::max(rk2 - 2.0 * M * rk + a2, 1e-6);
+    const double kA = 2.0 * M * rk / delta;
+    const double gr[3] = {x * rk2 * rk / sig, y * rk2 * rk / sig, z * rk * (rk2 + a2) / sig};
+    const double luc = 1.0 + kA * dot3(l, gr);
+    double uz[4] = {1.0 + f * luc, 0, 0, 0};
+    for (int c = 0; c < 3; ++c) uz[c + 1] = kA * gr[c] - (f * luc) * l[c];
+    const double luz = uz[0] + l[0] * uz[1] + l[1] * uz[2] + l[2] * uz[3];
+    const double n2 = -uz[0] * uz[0] + uz[1] * uz[1] + uz[2] * uz[2] + uz[3] * uz[3] + f * luz * luz;
+    double zamo[4];
+    for (int c = 0; c < 4; ++c) zamo[c] = uz[c] / std::sqrt(-n2);
+    if (f >= 0.88) {
+      std::memcpy(u, zamo, sizeof u);
+    } else {
+      double wb = std::min(std::max((f - 0.72) / 0.16, 0.0), 1.0);
+      wb = wb * wb * (3.0 - 2.0 * wb);
+      const double us[4] = {1.0 / std::sqrt(1.0 - f), 0, 0, 0};
+      if (wb == 0.0) {
+        std::memcpy(u, us, sizeof u);
+      } else {
+        double um[4];
+        for (int c = 0; c < 4; ++c) um[c] = (1.0 - wb) * us[c] + wb * zamo[c];
+        const double lu = um[0] + l[0] * um[1] + l[1] * um[2] + l[2] * um[3];
+        const double nn = -um[0] * um[0] + um[1] * um[1] + um[2] * um[2] + um[3] * um[3] + f * lu * lu;
+        for (int c = 0; c < 4; ++c) u[c] = um[c] / std::sqrt(-nn);
+      }
+    }
+  }
+  auto ld = [&](const double* A) { return A[0] + l[0] * A[1] + l[1] * A[2] + l[2] * A[3]; };
+  auto g = [&](const double* A, const double* B) {
+    return -A[0] * B[0] + A[1] * B[1] + A[2] * B[2] + A[3] * B[3] + f * ld(A) * ld(B);
+  };
+  double ef[4] = {0, fwd[0], fwd[1], fwd[2]}, er[4] = {0, right[0], right[1], right[2]},
+         eu[4] = {0, up[0], up[1], up[2]};
+  auto axpy = [](double* y, double s, const double* x) { for (int k = 0; k < 4; ++k) y[k] += s * x[k]; };
+  auto scale = [](double* y, double s) { for (int k = 0; k < 4; ++k) y[k] /= s; };
+  axpy(ef, g(ef, u), u);
+  scale(ef, std::sqrt(g(ef, ef)));
+  axpy(er, g(er, u), u);
+  axpy(er, -g(er, ef), ef);
+  scale(er, std::sqrt(g(er, er)));
+  axpy(eu, g(eu, u), u);
+  {
+    const double c1 = g(eu, ef), c2 = g(eu, er);
+    for (int k = 0; k < 4; ++k) eu[k] -= c1 * ef[k] + c2 * er[k];
+  }
+  scale(eu, std::sqrt(g(eu, eu)));
+  const double b2raw = dot3(beta, beta);
+  if (b2raw > 1e-12) {
+    const double b2 = std::min(b2raw, 0.9801);
+    const double s = std::sqrt(b2 / b2raw);
+    const double b[3] = {beta[0] * s, beta[1] * s, beta[2] * s};
+    const double gam = 1.0 / std::sqrt(1.0 - b2);
+    double bE[4];
+    for (int k = 0; k < 4; ++k) bE[k] = b[0] * ef[k] + b[1] * er[k] + b[2] * eu[k];
+    const double kk = (gam - 1.0) / b2;
+    for (int k = 0; k < 4; ++k) {
+      const double common = kk * bE[k] + gam * u[k];
+      U[k] = gam * (u[k] + bE[k]);
+      Ef[k] = ef[k] + b[0] * common;
+      Er[k] = er[k] + b[1] * common;
+      Eu[k] = eu[k] + b[2] * common;
+    }
+    return;
+  }
+  std::memcpy(U, u, sizeof u);
+  std::memcpy(Ef, ef, sizeof ef);
+  std::memcpy(Er, er, sizeof er);
+  std::memcpy(Eu, eu, sizeof eu);
+}
+
+// CIE piecewise-Gaussian blackbody colour, src/blackbody.jl:5-35.
+static double cie_g(double lam, double mu, double s1, double s2) {
+  const double s = lam < mu ? s1 : s2;
+  const double t = (lam - mu) / s;
+  return std::exp(-0.5 * t * t);
+}
+static void host_blackbody(double T, double* rgb) {
+  double X = 0, Y = 0, Z = 0;
+  for (int i = 0; i <= 80; ++i) {
+    const double lam = 380.0 + 5.0 * i, lm = lam * 1e-9;
+    const double B = 1.0 / (std::pow(lm, 5) * (std::exp(0.014388 / (lm * T)) - 1.0));
+    X += B * (1.056 * cie_g(lam, 599.8, 37.9, 31.0) + 0.362 * cie_g(lam, 442.0, 16.0, 26.7) -
+              0.065 * cie_g(lam, 501.1, 20.4, 26.2));
+    Y += B * (0.821 * cie_g(lam, 568.8, 46.9, 40.5) + 0.286 * cie_g(lam, 530.9, 16.3, 31.1));
+    Z += B * (1.217 * cie_g(lam, 437.0, 11.8, 36.0) + 0.681 * cie_g(lam, 459.0, 26.0, 13.8));
+  }
+  const double r = std::max(3.2406 * X - 1.5372 * Y - 0.4986 * Z, 0.0);
+  const double gg = std::max(-0.9689 * X + 1.8758 * Y + 0.0415 * Z, 0.0);
+  const double b = std::max(0.0557 * X - 0.2040 * Y + 1.0570 * Z, 0.0);
+  const double m = std::max(std::max(r, gg), std::max(b, 1e-10));
+  rgb[0] = r / m; rgb[1] = gg / m; rgb[2] = b / m;
+}
+
+// ISCO (BPT 1972), as the kernel's isco_mtl (src/metal.jl:371-380) in double.
+static void host_isco(double M, double a, double* r_isco, double* E, double* L) {
+  auto cb = [](double x) { return std::exp(std::log(std::max(x, 1e-12)) / 3.0); };
+  const double q = a / M;
+  const double z1 = 1.0 + cb(1.0 - q * q) * (cb(1.0 + q) + cb(1.0 - q));
+  const double z2 = std::sqrt(3.0 * q * q + z1 * z1);
+  const double r = M * (3.0 + z2 - std::sqrt(std::max((3.0 - z1) * (3.0 + z1 + 2.0 * z2), 0.0)));
+  *r_isco = r;
+  *E = std::sqrt(1.0 - 2.0 * M / (3.0 * r));
+  *L = (2.0 * M / (3.0 * std::sqrt(3.0))) * (1.0 + 2.0 * std::sqrt(3.0 * r / M - 2.0));
+}
+
+// Prograde photon orbit, src/gr.jl:58-60.
+static double host_photon_orbit_min(double M, double a) {
+  if (a == 0.0) return 3.0 * M;
+  return 2.0 * M * (1.0 + std::cos((2.0 / 3.0) * std::acos(-a / M)));
+}
+
+// splitmix64 for the host-side pass shuffles
+struct Rng {
+  uint64_t s;
+  uint64_t next() {
+    uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+  }
+  int below(int n) { return (int)(next() % (uint64_t)n); }
+};
+static void shuffle(std::vector<int>& v, Rng& r) {
+  for (int i = (int)v.size() - 1; i > 0; --i) std::swap(v[i], v[r.below(i + 1)]);
+}
+
+}  // namespace st
+
+// ---------------------------------------------------------------------------
+// Context.
+// ---------------------------------------------------------------------------
+
+struct st_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  float4* d_sky = nullptr;
+  int sky_w = 0, sky_h = 0;
+  float4* d_lut = nullptr;
+  int lut_size = 0;
+  st_disc disc{};
+  bool disc_on = false;
+  float* d_vol = nullptr;
+  size_t vol_bytes = 0;
+  st_volume vol{};
+  bool vol_on = false;
+  float4* d_fb = nullptr;
+  size_t fb_cap = 0;
+  float* d_rgb = nullptr;
+  size_t rgb_cap = 0;
+  st_ray_diag* d_diag = nullptr;
+  size_t diag_cap = 0;
+  st::FrameCam* d_frames = nullptr;
+  size_t frames_cap = 0;
+  unsigned long long* d_counters = nullptr;
+  unsigned int* d_queue = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+using st::TraceParams;
+
+#define ST_CUDA(call)                         \
+  do {                                        \
+    cudaError_t e_ = (call);                  \
+    if (e_ != cudaSuccess) return ST_ECUDA;   \
+  } while (0)
+
+template <class T>
+int ensure(T** ptr, size_t* cap, size_t n) {
+  if (*cap >= n && *ptr) return ST_OK;
+  if (*ptr) cudaFree(*ptr);
+  *ptr = nullptr;
+  *cap = 0;
+  if (cudaMalloc((void**)ptr, n * sizeof(T)) != cudaSuccess) return ST_ENOMEM;
+  *cap = n;
+  return ST_OK;
+}
+
+double norm3(const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+
+// Fill the frame-independent part of TraceParams and the camera of `cam`.
+int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
+                TraceParams* p, st::Variant* v) {
+  if (!ctx || !cam || !stp || !rp) return ST_EINVAL;
+  const double M = stp->M, a = stp->a;
+  if (!(M > 0.0) || !(std::fabs(a) <= M)) return ST_EINVAL;
+  if (rp->width <= 0 || rp->height <= 0 || rp->samples <= 0 || !(rp->dt > 0.0)) return ST_EINVAL;
+  if ((long long)rp->width * rp->height > (1ll << 30)) return ST_EINVAL;
+  if (rp->precision < ST_PREC_FP64 || rp->precision > ST_PREC_FP32) return ST_EINVAL;
+  if (rp->semantics != ST_SEM_RENDER && rp->semantics != ST_SEM_DRAFT) return ST_EINVAL;
+  const double rpos = norm3(cam->pos);
+  if (!(rpos > 0.0) || !std::isfinite(rpos)) return ST_EINVAL;
+  if (rp->semantics == ST_SEM_RENDER) {
+    // the reference's CPU renderer has Schwarzschild methods only
+    if (a != 0.0) return ST_EUNSUPPORTED;
+    if (ctx->vol_on) return ST_EUNSUPPORTED;
+  }
+  if (rp->surrogate) return ST_ESTATE;
+  std::memset(p, 0, sizeof(*p));
+  const double beta[3] = {st::dot3(cam->velocity, cam->fwd), st::dot3(cam->velocity, cam->right),
+                          st::dot3(cam->velocity, cam->up)};
+  st::host_tetrad(cam->pos, cam->fwd, cam->right, cam->up, M, a, beta, p->U, p->Ef, p->Er, p->Eu);
+  for (int k = 0; k < 3; ++k) p->pos[k] = cam->pos[k];
+  p->fov = cam->fov_factor;
+  p->projection = cam->projection;
+  p->fisheye_rad = std::max(cam->fisheye_deg, 0.0) * 3.141592653589793 / 180.0;
+  p->focus = cam->focus_dist > 0.0 ? cam->focus_dist : 1.0;
+  p->width = rp->width;
+  p->height = rp->height;
+  p->frame_stride = rp->width * rp->height;
+  p->M = M;
+  p->a = a;
+  const double rph = st::host_photon_orbit_min(M, a);
+  {
+    // the kernel holds the kill radius in Float32 (src/metal.jl:355-356)
+    const float rk = (float)(0.995 * rph);
+    p->rkill2 = (double)(rk * rk);
+  }
+  st::host_isco(M, a, &p->r_isco, &p->E_isco, &p->L_isco);
+  p->dt = rp->dt;
+  p->hcoef = 0.16;
+  p->hcap = 8.0;
+  p->relativistic = rp->relativistic ? 1 : 0;
+  if (rp->semantics == ST_SEM_DRAFT) {
+    // src/metal.jl:2058-2062: r_escape = 2 max(|pos|, 15M) (Float32);
+    // nmax = min(max(1000, ceil((75 + 6.5 ln(r_esc/M)) M/dt)), 40000)
+    const double re = rp->r_escape > 0.0 ? rp->r_escape : (double)(float)(2.0 * std::max(rpos, 15.0 * M));
+    p->r_escape = re;
+    if (rp->nmax > 0) {
+      p->nmax = rp->nmax;
+    } else {
+      const double Mf = (double)(float)M, dtf = (double)(float)rp->dt;
+      const double lg = (double)std::log((float)((float)re / (float)M));
+      const double n = std::ceil((75.0 + 6.5 * lg) * Mf / dtf);
+      p->nmax = (int)std::min(std::max(1000.0, n), 40000.0);
+    }
+    p->tspan = 0.0;
+    p->exit_landing = rp->exit_landing ? 1 : 0;
+  } else {
+    // src/raytrace.jl:352-354, 373: r_max = max(5|pos|, 100); tspan = max(10|pos|, 500);
+    // the step budget stands in for maxiters = 50_000
+    p->r_escape = rp->r_escape > 0.0 ? rp->r_escape : std::max(5.0 * rpos, 100.0);
+    p->tspan = rp->tspan > 0.0 ? rp->tspan : std::max(10.0 * rpos, 500.0);
+    p->nmax = rp->nmax > 0 ? rp->nmax : 50000;
+    p->exit_landing = 1;
+  }
+  // FP32_GUARDED policy
+  const double rg = rp->r_guard > 0.0 ? rp->r_guard : 0.0;
+  p->r_guard2 = rg * rg;
+  p->crit_band = rp->crit_band;
+  p->b_crit = 3.0 * std::sqrt(3.0) * M;
+  p->renorm_every = rp->renorm_every;
+  // disc
+  p->disc_on = (ctx->disc_on && ctx->disc.inner > 0.0 && ctx->disc.outer > ctx->disc.inner) ? 1 : 0;
+  p->emitter = ctx->disc.emitter;
+  p->disc_inner = ctx->disc.inner;
+  p->disc_outer = ctx->disc.outer;
+  p->disc_falloff = ctx->disc.falloff;
+  p->lut = ctx->d_lut;
+  p->lut_size = ctx->lut_size;
+  p->lut_tmin = ctx->disc.table_min;
+  p->lut_tmax = ctx->disc.table_max;
+  if (p->disc_on && !ctx->d_lut) p->disc_on = 0;
+  // volume (DRAFT only), src/metal.jl:1147-1159
+  p->vol_on = (rp->semantics == ST_SEM_DRAFT && ctx->vol_on) ? 1 : 0;
+  if (p->vol_on) {
+    const st_volume& vv = ctx->vol;
+    p->vol = ctx->d_vol;
+    p->nr = vv.nr; p->nphi = vv.nphi; p->nz = vv.nz;
+    p->ls_in = vv.log_s_in; p->ls_out = vv.log_s_out; p->zmax = vv.z_max;
+    p->emis = vv.emission_scale; p->opac = vv.opacity_scale;
+    const int stride = std::min(std::max(vv.march_stride, 1), 16);
+    p->ds_gas = stride * rp->dt;
+    const double so = std::exp((double)vv.log_s_out);
+    p->vol_rb2 = so * so + (double)vv.z_max * vv.z_max;
+  } else {
+    p->vol_rb2 = -1.0;
+  }
+  p->sky = ctx->d_sky;
+  p->sky_w = ctx->sky_w;
+  p->sky_h = ctx->sky_h;
+  p->counters = ctx->d_counters;
+  p->queue = ctx->d_queue;
+  p->chunk_steps = rp->chunk_steps > 0 ? rp->chunk_steps : 32;
+  v->prec = rp->precision;
+  v->kerr = (a != 0.0) ? 1 : 0;
+  v->vol = p->vol_on;
+  v->sem = rp->semantics;
+  v->sched = rp->schedule == ST_SCHED_PERSISTENT ? ST_SCHED_PERSISTENT : ST_SCHED_PIXEL;
+  return ST_OK;
+}
+
+struct PassPlan {
+  double ju, jv, jw;
+  int jseed;
+  double lens_u0, lens_v0, lens_w;
+  int lens_seed;
+};
+
+// The samples^2 passes of render_draft_mtl (src/metal.jl:2091-2168) or of
+// render's stratified offsets (src/raytrace.jl:375-419).  Host draws use
+// splitmix64 seeded by p->seed.
+std::vector<PassPlan> plan_passes(const st_render_params* rp, const st_camera* cam) {
+  const int S = rp->samples;
+  const int n = S * S;
+  st::Rng rng{rp->seed ^ 0x5eed5eedull};
+  std::vector<int> order(n), lens(n);
+  for (int k = 0; k < n; ++k) { order[k] = k; lens[k] = k; }
+  if (rp->pixel_jitter) st::shuffle(order, rng);
+  st::shuffle(lens, rng);
+  const bool dof = cam->aperture_world > 0.0 && cam->projection == ST_PROJ_PINHOLE;
+  std::vector<PassPlan> out(n);
+  for (int k = 0; k < n; ++k) {
+    const int m = order[k];
+    const int a = m / S, b = m % S;
+    PassPlan pp{};
+    const double shift = rp->semantics == ST_SEM_RENDER ? 0.5 : 0.0;  // CPU pixel-centre convention
+    if (rp->pixel_jitter) {
+      pp.ju = (double)a / S + shift;
+      pp.jv = (double)b / S + shift;
+      pp.jw = 1.0 / S;
+    } else {
+      pp.ju = (a + 0.5) / S + shift;
+      pp.jv = (b + 0.5) / S + shift;
+      pp.jw = 0.0;
+    }
+    pp.jseed = 15485863 + (k + 1);
+    if (dof) {
+      const int lm = lens[k];
+      pp.lens_u0 = (double)(lm / S) / S;
+      pp.lens_v0 = (double)(lm % S) / S;
+      pp.lens_w = 1.0 / S;
+      pp.lens_seed = k + 1;
+    }
+    out[k] = pp;
+  }
+  return out;
+}
+
+int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
+              float* host_rgb, st_ray_diag* host_diag, const float** dev_rgba, st_stats* stats) {
+  const auto t0 = std::chrono::steady_clock::now();
+  TraceParams p;
+  st::Variant v;
+  int rc = fill_params(ctx, cam, stp, rp, &p, &v);
+  if (rc != ST_OK) return rc;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
+  const size_t npix = (size_t)rp->width * rp->height;
+  if ((rc = ensure(&ctx->d_fb, &ctx->fb_cap, npix)) != ST_OK) return rc;
+  if (host_rgb && (rc = ensure(&ctx->d_rgb, &ctx->rgb_cap, 3 * npix)) != ST_OK) return rc;
+  if (host_diag && (rc = ensure(&ctx->d_diag, &ctx->diag_cap, npix)) != ST_OK) return rc;
+  p.out = ctx->d_fb;
+  p.diag = host_diag ? ctx->d_diag : nullptr;
+  p.ap_r = cam->aperture_world > 0.0 ? cam->aperture_world / 2.0 : 0.0;
+  cudaStream_t s = ctx->stream;
+  ST_CUDA(cudaMemsetAsync(ctx->d_counters, 0, st::CNT_N * sizeof(unsigned long long), s));
+  const std::vector<PassPlan> passes = plan_passes(rp, cam);
+  p.weight = (float)(1.0 / passes.size());
+  ST_CUDA(cudaEventRecord(ctx->ev0, s));
+  int launches = 0;
+  for (size_t k = 0; k < passes.size(); ++k) {
+    const PassPlan& pp = passes[k];
+    p.ju = pp.ju; p.jv = pp.jv; p.jw = pp.jw; p.jseed = pp.jseed;
+    p.lens_u0 = pp.lens_u0; p.lens_v0 = pp.lens_v0; p.lens_w = pp.lens_w; p.lens_seed = pp.lens_seed;
+    p.first_pass = (k == 0) ? 1 : 0;
+    if (v.sched == ST_SCHED_PERSISTENT) {
+      ST_CUDA(cudaMemsetAsync(ctx->d_queue, 0, sizeof(unsigned int), s));
+      const long long tiles = (long long)((rp->width + 7) / 8) * ((rp->height + 3) / 4);
+      p.n_rays = (int)(tiles * 32);
+      p.budget_iters = ((long long)p.n_rays + 32) * ((long long)p.nmax / std::max(p.chunk_steps, 1) + 2);
+    }
+    ST_CUDA(st::launch_trace(v, p, rp->block_x, rp->block_y, ctx->num_sms, s));
+    ++launches;
+  }
+  ST_CUDA(cudaEventRecord(ctx->ev1, s));
+  unsigned long long cnt[st::CNT_N];
+  ST_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
+  unsigned long long d2h = 0;
+  if (host_rgb) {
+    ST_CUDA(st::launch_pack_rgb(ctx->d_fb, ctx->d_rgb, (int)npix, s));
+    ST_CUDA(cudaMemcpyAsync(host_rgb, ctx->d_rgb, 3 * npix * sizeof(float), cudaMemcpyDeviceToHost, s));
+    d2h += 3 * npix * sizeof(float);
+  }
+  if (host_diag) {
+    ST_CUDA(cudaMemcpyAsync(host_diag, ctx->d_diag, npix * sizeof(st_ray_diag), cudaMemcpyDeviceToHost, s));
+    d2h += npix * sizeof(st_ray_diag);
+  }
+  ST_CUDA(cudaStreamSynchronize(s));
+  if (dev_rgba) *dev_rgba = reinterpret_cast<const float*>(ctx->d_fb);
+  const int status = cnt[st::CNT_STATUS] ? (int)cnt[st::CNT_STATUS] : ST_OK;
+  if (stats) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    std::memset(stats, 0, sizeof(*stats));
+    stats->kernel_ms = ms;
+    stats->rays = cnt[st::CNT_RAYS];
+    stats->steps = cnt[st::CNT_STEPS];
+    stats->fp64_steps = cnt[st::CNT_FP64];
+    stats->gas_samples = cnt[st::CNT_GAS];
+    stats->surrogate_rays = cnt[st::CNT_SURR];
+    stats->launches = launches;
+    stats->status = status;
+    stats->h2d_bytes = sizeof(TraceParams) * launches;
+    stats->d2h_bytes = d2h + sizeof cnt;
+    stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return status;
+}
+
+}  // namespace
+
+extern "C" {
+
+int st_abi_version(void) { return ST_ABI_VERSION; }
+
+const char* st_strerror(int code) {
+  switch (code) {
+    case ST_OK: return "ok";
+    case ST_EINVAL: return "invalid argument";
+    case ST_ECUDA: return "CUDA runtime error";
+    case ST_EBUDGET: return "persistent queue iteration budget exhausted";
+    case ST_ENOMEM: return "out of memory";
+    case ST_EUNSUPPORTED: return "unsupported combination";
+    case ST_ESTATE: return "context not ready for this request";
+    default: return "unknown status";
+  }
+}
+
+void st_render_params_default(st_render_params* p, int semantics) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->samples = 1;
+  p->dt = 0.02;
+  p->semantics = semantics;
+  p->schedule = ST_SCHED_PIXEL;
+  p->seed = 0;
+  p->r_guard = 3.0;
+  p->crit_band = 0.05;
+  p->renorm_every = 64;
+  p->surrogate_sigma = 1e-4;
+  p->chunk_steps = 32;
+  if (semantics == ST_SEM_RENDER) {
+    // render(...; width=400, height=200, samples=1): FP64 like the CPU path
+    p->width = 400; p->height = 200;
+    p->precision = ST_PREC_FP64;
+    p->exit_landing = 1;
+    p->pixel_jitter = 0;
+  } else {
+    // render_draft_mtl(...; width=1920, height=1080, samples=2, dt=0.02): Float32
+    p->width = 1920; p->height = 1080; p->samples = 2;
+    p->precision = ST_PREC_FP32;
+    p->exit_landing = 0;
+    p->pixel_jitter = 1;
+  }
+}
+
+int st_context_create(st_context** out, const float* sky_rgb, int sky_w, int sky_h, int device) {
+  if (!out || !sky_rgb || sky_w < 2 || sky_h < 2) return ST_EINVAL;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return ST_ECUDA;
+  if (device < 0 || device >= ndev) return ST_EINVAL;
+  st_context* c = new (std::nothrow) st_context();
+  if (!c) return ST_ENOMEM;
+  c->device = device;
+  auto fail = [&](int code) { st_context_destroy(c); return code; };
+  if (cudaSetDevice(device) != cudaSuccess) return fail(ST_ECUDA);
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(ST_ECUDA);
+  if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return fail(ST_ECUDA);
+  // sky: (3, W, H) column-major RGB -> float4 [H][W]
+  const size_t n = (size_t)sky_w * sky_h;
+  std::vector<float4> host(n);
+  for (size_t i = 0; i < n; ++i) host[i] = make_float4(sky_rgb[3 * i], sky_rgb[3 * i + 1], sky_rgb[3 * i + 2], 0.f);
+  if (cudaMalloc(&c->d_sky, n * sizeof(float4)) != cudaSuccess) return fail(ST_ENOMEM);
+  if (cudaMemcpy(c->d_sky, host.data(), n * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(ST_ECUDA);
+  c->sky_w = sky_w;
+  c->sky_h = sky_h;
+  if (cudaMalloc(&c->d_counters, st::CNT_N * sizeof(unsigned long long)) != cudaSuccess) return fail(ST_ENOMEM);
+  if (cudaMalloc(&c->d_queue, sizeof(unsigned int)) != cudaSuccess) return fail(ST_ENOMEM);
+  *out = c;
+  return ST_OK;
+}
+
+int st_context_set_disc(st_context* ctx, const st_disc* d) {
+  if (!ctx) return ST_EINVAL;
+  if (!d) { ctx->disc_on = false; return ST_OK; }
+  const int n = d->table_size > 0 ? d->table_size : 1024;
+  const double tmin = d->table_size > 0 ? d->table_min : 500.0;
+  const double tmax = d->table_size > 0 ? d->table_max : 30000.0;
+  if (!(tmax > tmin) || n < 2 || n > (1 << 20)) return ST_EINVAL;
+  if (d->emitter != ST_EMIT_KEPLER && d->emitter != ST_EMIT_KS_EXACT) return ST_EINVAL;
+  // Blackbody(wb_temperature, table_min, table_max, table_size), src/blackbody.jl:51-60
+  double ref[3];
+  st::host_blackbody(d->wb_temperature > 0.0 ? d->wb_temperature : 6500.0, ref);
+  std::vector<float4> lut(n);
+  for (int i = 0; i < n; ++i) {
+    const double T = tmin + (tmax - tmin) * i / (n - 1);
+    double c[3];
+    st::host_blackbody(std::max(T, 1.0), c);
+    lut[i] = make_float4((float)(c[0] / ref[0]), (float)(c[1] / ref[1]), (float)(c[2] / ref[2]), 0.f);
+  }
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
+  if (ctx->d_lut && ctx->lut_size != n) { cudaFree(ctx->d_lut); ctx->d_lut = nullptr; }
+  if (!ctx->d_lut && cudaMalloc(&ctx->d_lut, n * sizeof(float4)) != cudaSuccess) return ST_ENOMEM;
+  if (cudaMemcpy(ctx->d_lut, lut.data(), n * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess)
+    return ST_ECUDA;
+  ctx->lut_size = n;
+  ctx->disc = *d;
+  ctx->disc.table_min = tmin;
+  ctx->disc.table_max = tmax;
+  ctx->disc.table_size = n;
+  ctx->disc_on = true;
+  return ST_OK;
+}
+
+int st_context_set_volume(st_context* ctx, const st_volume* v) {
+  if (!ctx) return ST_EINVAL;
+  if (!v) { ctx->vol_on = false; return ST_OK; }
+  if (!v->density || v->nr < 2 || v->nphi < 1 || v->nz < 2) return ST_EINVAL;
+  if (!(v->log_s_out > v->log_s_in) || !(v->z_max > 0.0f)) return ST_EINVAL;
+  const size_t n = (size_t)v->nr * v->nphi * v->nz;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
+  if (ctx->d_vol && ctx->vol_bytes != n * sizeof(float)) { cudaFree(ctx->d_vol); ctx->d_vol = nullptr; }
+  if (!ctx->d_vol && cudaMalloc(&ctx->d_vol, n * sizeof(float)) != cudaSuccess) return ST_ENOMEM;
+  if (cudaMemcpy(ctx->d_vol, v->density, n * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+    return ST_ECUDA;
+  ctx->vol_bytes = n * sizeof(float);
+  ctx->vol = *v;
+  ctx->vol.density = nullptr;
+  ctx->vol_on = true;
+  return ST_OK;
+}
+
+void st_context_destroy(st_context* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  cudaFree(ctx->d_sky);
+  cudaFree(ctx->d_lut);
+  cudaFree(ctx->d_vol);
+  cudaFree(ctx->d_fb);
+  cudaFree(ctx->d_rgb);
+  cudaFree(ctx->d_diag);
+  cudaFree(ctx->d_frames);
+  cudaFree(ctx->d_counters);
+  cudaFree(ctx->d_queue);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+int st_render(st_context* ctx, const st_camera* cam, const st_spacetime* st, const st_render_params* p,
+              float* out_rgb, st_stats* stats) {
+  if (!out_rgb) return ST_EINVAL;
+  return do_render(ctx, cam, st, p, out_rgb, nullptr, nullptr, stats);
+}
+
+int st_render_diag(st_context* ctx, const st_camera* cam, const st_spacetime* st, const st_render_params* p,
+                   float* out_rgb, st_ray_diag* diag, st_stats* stats) {
+  if (!out_rgb || !diag) return ST_EINVAL;
+  return do_render(ctx, cam, st, p, out_rgb, diag, nullptr, stats);
+}
+
+int st_render_device(st_context* ctx, const st_camera* cam, const st_spacetime* st, const st_render_params* p,
+                     const float** dev_rgba, st_stats* stats) {
+  if (!dev_rgba) return ST_EINVAL;
+  return do_render(ctx, cam, st, p, nullptr, nullptr, dev_rgba, stats);
+}
+
+int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const st_spacetime* stp,
+                     const st_render_params* rp, float* out_rgb, st_stats* stats) {
+  if (!ctx || nframes <= 0 || !cams || !stp || !rp || !out_rgb) return ST_EINVAL;
+  if (rp->semantics != ST_SEM_DRAFT || rp->samples != 1) return ST_EUNSUPPORTED;
+  const auto t0 = std::chrono::steady_clock::now();
+  TraceParams p;
+  st::Variant v;
+  int rc = fill_params(ctx, &cams[0], stp, rp, &p, &v);
+  if (rc != ST_OK) return rc;
+  const size_t npix = (size_t)rp->width * rp->height;
+  if (npix * (size_t)nframes > (size_t)1 << 31) return ST_EINVAL;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
+  std::vector<st::FrameCam> fc(nframes);
+  int nmax_max = 0;
+  for (int f = 0; f < nframes; ++f) {
+    TraceParams q;
+    st::Variant w;
+    rc = fill_params(ctx, &cams[f], stp, rp, &q, &w);
+    if (rc != ST_OK) return rc;
+    std::memcpy(fc[f].pos, q.pos, sizeof q.pos);
+    std::memcpy(fc[f].Ef, q.Ef, sizeof q.Ef);
+    std::memcpy(fc[f].Er, q.Er, sizeof q.Er);
+    std::memcpy(fc[f].Eu, q.Eu, sizeof q.Eu);
+    std::memcpy(fc[f].U, q.U, sizeof q.U);
+    fc[f].r_escape = q.r_escape;
+    fc[f].nmax = q.nmax;
+    nmax_max = std::max(nmax_max, q.nmax);
+  }
+  if ((rc = ensure(&ctx->d_frames, &ctx->frames_cap, (size_t)nframes)) != ST_OK) return rc;
+  if ((rc = ensure(&ctx->d_fb, &ctx->fb_cap, npix * nframes)) != ST_OK) return rc;
+  if ((rc = ensure(&ctx->d_rgb, &ctx->rgb_cap, 3 * npix * nframes)) != ST_OK) return rc;
+  cudaStream_t s = ctx->stream;
+  ST_CUDA(cudaMemcpyAsync(ctx->d_frames, fc.data(), nframes * sizeof(st::FrameCam), cudaMemcpyHostToDevice, s));
+  ST_CUDA(cudaMemsetAsync(ctx->d_counters, 0, st::CNT_N * sizeof(unsigned long long), s));
+  ST_CUDA(cudaMemsetAsync(ctx->d_queue, 0, sizeof(unsigned int), s));
+  const std::vector<PassPlan> passes = plan_passes(rp, &cams[0]);
+  const PassPlan& pp = passes[0];
+  p.ju = pp.ju; p.jv = pp.jv; p.jw = pp.jw; p.jseed = pp.jseed;
+  p.weight = 1.0f;
+  p.first_pass = 1;
+  p.out = ctx->d_fb;
+  p.frames = ctx->d_frames;
+  p.frame_stride = (int)npix;
+  const long long tiles = (long long)((rp->width + 7) / 8) * ((rp->height + 3) / 4);
+  p.n_rays = (int)(tiles * 32 * nframes);
+  p.chunk_steps = rp->chunk_steps > 0 ? rp->chunk_steps : 32;
+  p.budget_iters = ((long long)p.n_rays + 32) * ((long long)nmax_max / p.chunk_steps + 2);
+  p.nmax = nmax_max;
+  v.sched = ST_SCHED_PERSISTENT;
+  ST_CUDA(cudaEventRecord(ctx->ev0, s));
+  ST_CUDA(st::launch_trace(v, p, 0, 0, ctx->num_sms, s));
+  ST_CUDA(cudaEventRecord(ctx->ev1, s));
+  unsigned long long cnt[st::CNT_N];
+  ST_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
+  ST_CUDA(st::launch_pack_rgb(ctx->d_fb, ctx->d_rgb, (int)(npix * nframes), s));
+  ST_CUDA(cudaMemcpyAsync(out_rgb, ctx->d_rgb, 3 * npix * nframes * sizeof(float), cudaMemcpyDeviceToHost, s));
+  ST_CUDA(cudaStreamSynchronize(s));
+  const int status = cnt[st::CNT_STATUS] ? (int)cnt[st::CNT_STATUS] : ST_OK;
+  if (stats) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    std::memset(stats, 0, sizeof(*stats));
+    stats->kernel_ms = ms;
+    stats->rays = cnt[st::CNT_RAYS];
+    stats->steps = cnt[st::CNT_STEPS];
+    stats->fp64_steps = cnt[st::CNT_FP64];
+    stats->gas_samples = cnt[st::CNT_GAS];
+    stats->launches = 1;
+    stats->status = status;
+    stats->h2d_bytes = sizeof(TraceParams) + nframes * sizeof(st::FrameCam);
+    stats->d2h_bytes = 3 * npix * nframes * sizeof(float) + sizeof cnt;
+    stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return status;
+}
+
+int st_camera_tetrad(const st_camera* cam, const st_spacetime* stp, double out16[16]) {
+  if (!cam || !stp || !out16) return ST_EINVAL;
+  if (!(stp->M > 0.0) || !(std::fabs(stp->a) <= stp->M)) return ST_EINVAL;
+  const double beta[3] = {st::dot3(cam->velocity, cam->fwd), st::dot3(cam->velocity, cam->right),
+                          st::dot3(cam->velocity, cam->up)};
+  st::host_tetrad(cam->pos, cam->fwd, cam->right, cam->up, stp->M, stp->a, beta, out16, out16 + 4, out16 + 8,
+                  out16 + 12);
+  return ST_OK;
+}
+
+}  // extern "C"

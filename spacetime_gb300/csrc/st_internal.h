@@ -1,0 +1,100 @@
+// st_internal.h -- device-side parameter block and launch entry points shared
+// by the host API (st_api.cu) and the trace kernels (st_trace.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/spacetime_gb300.h"
+
+namespace st {
+
+// Counters written by the trace kernels (one slot each, 64-bit).
+enum { CNT_STEPS = 0, CNT_FP64 = 1, CNT_GAS = 2, CNT_RAYS = 3, CNT_SURR = 4, CNT_QUEUE = 5,
+       CNT_STATUS = 6, CNT_N = 8 };
+
+// Per-frame camera of a batched track (st_render_frames).
+struct FrameCam {
+  double pos[3];
+  double Ef[4], Er[4], Eu[4], U[4];
+  double r_escape;
+  int nmax;
+  int pad;
+};
+
+// Everything a trace launch needs, passed by value as a __grid_constant__
+// kernel parameter (well under the 4 KB limit).
+struct TraceParams {
+  // camera tetrad (FP64 host computation, src/preview.jl:93-198)
+  double pos[3];
+  double Ef[4], Er[4], Eu[4], U[4];
+  double fov;
+  int projection;
+  double fisheye_rad;
+  double ap_r, focus;
+  int lens_seed;
+  double lens_u0, lens_v0, lens_w;
+  // frame / pass
+  int width, height;
+  int frame_stride;          // pixels per frame in the output (batched frames)
+  double ju, jv, jw;
+  int jseed;
+  float weight;
+  int first_pass;            // 1: assign instead of accumulate
+  // spacetime and integration
+  double M, a, rkill2;
+  double r_escape, tspan;
+  double hcoef, hcap, dt;
+  int nmax;
+  double r_isco, E_isco, L_isco;
+  int relativistic, exit_landing;
+  // FP32_GUARDED policy
+  double r_guard2, crit_band, b_crit;
+  int renorm_every;
+  // thin disc
+  int disc_on, emitter;
+  double disc_inner, disc_outer, disc_falloff;
+  const float4* lut;         // [lut_size] RGB_
+  int lut_size;
+  double lut_tmin, lut_tmax;
+  // volume
+  int vol_on;
+  const float* vol;
+  int nr, nphi, nz;
+  double ls_in, ls_out, zmax, emis, opac, ds_gas, vol_rb2;
+  // sky
+  const float4* sky;         // [sky_h][sky_w] RGB_
+  int sky_w, sky_h;
+  // outputs
+  float4* out;               // [height][width] (x frames)
+  st_ray_diag* diag;         // optional
+  unsigned long long* counters;  // CNT_N slots
+  // persistent schedule
+  const FrameCam* frames;    // optional per-frame cameras (device)
+  int n_rays;                // rays in the queue (frames x pixels)
+  int chunk_steps;
+  unsigned int* queue;       // queue head (device)
+  long long budget_iters;    // per-warp loop bound of the persistent kernel
+};
+
+// Variant key of the compiled kernels (the reference's Val{...} switches,
+// src/metal.jl:759-763, plus precision and schedule).
+struct Variant {
+  int prec;       // ST_PREC_*
+  int kerr;       // a != 0
+  int vol;        // volume on (DRAFT only)
+  int sem;        // ST_SEM_*
+  int sched;      // ST_SCHED_*
+};
+
+// Launch one trace pass; returns a cudaError_t.
+cudaError_t launch_trace(const Variant& v, const TraceParams& p, int block_x, int block_y,
+                         int num_sms, cudaStream_t stream);
+
+// Pack the float4 framebuffer into RGB float32 (3, W, H) for download.
+cudaError_t launch_pack_rgb(const float4* fb, float* rgb, int n, cudaStream_t stream);
+
+// Number of registers the pixel kernel of a variant uses (for reporting).
+int variant_registers(const Variant& v);
+
+}  // namespace st

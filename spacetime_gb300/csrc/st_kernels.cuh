@@ -1,0 +1,155 @@
+// st_kernels.cuh -- the trace kernels (per-pixel and persistent schedules)
+// and their launchers, instantiated per precision in st_trace_*.cu.
+#pragma once
+
+#include "st_trace.cuh"
+
+namespace st {
+
+__device__ __forceinline__ void flush_counters(const TraceParams& p, unsigned long long steps,
+                                               unsigned long long f64, unsigned long long gas,
+                                               unsigned long long rays) {
+  // warp-aggregated atomics on the launch counters
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    steps += __shfl_down_sync(0xffffffffu, steps, o);
+    f64 += __shfl_down_sync(0xffffffffu, f64, o);
+    gas += __shfl_down_sync(0xffffffffu, gas, o);
+    rays += __shfl_down_sync(0xffffffffu, rays, o);
+  }
+  if ((threadIdx.x & 31) == 0 && p.counters) {
+    if (steps) atomicAdd(p.counters + CNT_STEPS, steps);
+    if (f64) atomicAdd(p.counters + CNT_FP64, f64);
+    if (gas) atomicAdd(p.counters + CNT_GAS, gas);
+    if (rays) atomicAdd(p.counters + CNT_RAYS, rays);
+  }
+}
+
+// One thread per pixel over a 2-D grid of tiles (blockDim.x * blockDim.y a
+// multiple of 32; threads are linearised so a warp covers a compact tile).
+template <int PREC, int KERR, int VOL, int SEM>
+__global__ void __launch_bounds__(128) trace_pixel_kernel(const __grid_constant__ TraceParams p) {
+  using R = typename RealOf<PREC>::T;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  unsigned long long steps = 0, f64 = 0, gas = 0, rays = 0;
+  if (i < p.width && j < p.height) {
+    RayState<R> st;
+    const CamView cam{p.pos, p.Ef, p.Er, p.Eu, p.U, p.r_escape, p.nmax};
+    init_ray<PREC, KERR, SEM>(p, cam, i, j, st);
+    st.pix = j * p.width + i;
+    while (!step_ray<PREC, KERR, VOL, SEM>(p, st)) {
+    }
+    finish_ray<PREC, KERR, SEM>(p, st, st.pix, st.pix);
+    steps = st.steps; f64 = st.fp64_steps; gas = st.gas; rays = 1;
+  }
+  flush_counters(p, steps, f64, gas, rays);
+}
+
+// Persistent schedule: each warp pulls rays from a device queue; a lane whose
+// ray retires is refilled at the next chunk boundary (warp-ballot refill), so
+// short escaping rays do not idle lanes while photon-ring rays run on.  Queue
+// indices are ordered in 8x4 pixel tiles so a warp's first rays are coherent.
+// The outer loop is bounded by budget_iters; on exhaustion the kernel records
+// ST_EBUDGET in the status counter and returns.
+template <int PREC, int KERR, int VOL, int SEM>
+__global__ void __launch_bounds__(128) trace_persistent_kernel(const __grid_constant__ TraceParams p) {
+  using R = typename RealOf<PREC>::T;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int tiles_x = (p.width + 7) >> 3;
+  const int tiles_y = (p.height + 3) >> 2;
+  const int per_frame = tiles_x * tiles_y * 32;
+  RayState<R> st;
+  bool active = false, exhausted = false, done = false;
+  int out_idx = 0;
+  unsigned long long steps = 0, f64 = 0, gas = 0, rays = 0;
+  for (long long it = 0; it < p.budget_iters; ++it) {
+    const unsigned idle = __ballot_sync(FULL, !active);
+    if (idle && !exhausted) {
+      unsigned base = 0;
+      if (lane == 0) base = atomicAdd(p.queue, (unsigned)__popc(idle));
+      base = __shfl_sync(FULL, base, 0);
+      if (base >= (unsigned)p.n_rays) exhausted = true;
+      if (!active) {
+        const unsigned rank = __popc(idle & ((1u << lane) - 1u));
+        const unsigned idx = base + rank;
+        if (idx < (unsigned)p.n_rays) {
+          const int frame = (int)idx / per_frame;
+          const int w = (int)idx - frame * per_frame;
+          const int tile = w >> 5, within = w & 31;
+          const int ti = tile % tiles_x, tj = tile / tiles_x;
+          const int i = ti * 8 + (within & 7), j = tj * 4 + (within >> 3);
+          if (i < p.width && j < p.height) {
+            CamView cam{p.pos, p.Ef, p.Er, p.Eu, p.U, p.r_escape, p.nmax};
+            if (p.frames) {
+              const FrameCam& fc = p.frames[frame];
+              cam = CamView{fc.pos, fc.Ef, fc.Er, fc.Eu, fc.U, fc.r_escape, fc.nmax};
+            }
+            init_ray<PREC, KERR, SEM>(p, cam, i, j, st);
+            out_idx = frame * p.frame_stride + j * p.width + i;
+            st.pix = out_idx;
+            active = true;
+          }
+        }
+      }
+    }
+    if (!__any_sync(FULL, active)) { done = true; break; }
+    if (active) {
+      bool fin = false;
+      for (int s = 0; s < p.chunk_steps && !fin; ++s) fin = step_ray<PREC, KERR, VOL, SEM>(p, st);
+      if (fin) {
+        finish_ray<PREC, KERR, SEM>(p, st, out_idx, out_idx);
+        steps += st.steps; f64 += st.fp64_steps; gas += st.gas; rays += 1;
+        active = false;
+      }
+    }
+  }
+  flush_counters(p, steps, f64, gas, rays);
+  if (!done && lane == 0 && p.counters) atomicMax(p.counters + CNT_STATUS, (unsigned long long)ST_EBUDGET);
+}
+
+template <int PREC, int KERR, int VOL, int SEM>
+cudaError_t launch_variant(const TraceParams& p, int sched, int bx, int by, int num_sms, cudaStream_t s) {
+  if (sched == ST_SCHED_PERSISTENT) {
+    auto k = trace_persistent_kernel<PREC, KERR, VOL, SEM>;
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    k<<<num_sms * per_sm, 128, 0, s>>>(p);
+  } else {
+    if (bx <= 0 || by <= 0 || bx * by != 128) { bx = 16; by = 8; }
+    dim3 block(bx, by);
+    dim3 grid((p.width + bx - 1) / bx, (p.height + by - 1) / by);
+    trace_pixel_kernel<PREC, KERR, VOL, SEM><<<grid, block, 0, s>>>(p);
+  }
+  return cudaGetLastError();
+}
+
+template <int PREC>
+int variant_regs_impl(int kerr, int vol, int sem) {
+  cudaFuncAttributes a{};
+  cudaError_t e;
+  if (sem == ST_SEM_RENDER) e = cudaFuncGetAttributes(&a, trace_pixel_kernel<PREC, 0, 0, ST_SEM_RENDER>);
+  else if (kerr && vol) e = cudaFuncGetAttributes(&a, trace_pixel_kernel<PREC, 1, 1, ST_SEM_DRAFT>);
+  else if (kerr) e = cudaFuncGetAttributes(&a, trace_pixel_kernel<PREC, 1, 0, ST_SEM_DRAFT>);
+  else if (vol) e = cudaFuncGetAttributes(&a, trace_pixel_kernel<PREC, 0, 1, ST_SEM_DRAFT>);
+  else e = cudaFuncGetAttributes(&a, trace_pixel_kernel<PREC, 0, 0, ST_SEM_DRAFT>);
+  return e == cudaSuccess ? a.numRegs : -1;
+}
+
+// Per-precision dispatch over the remaining switches.  RENDER semantics is
+// Schwarzschild-only and has no volume (as the reference's CPU renderer).
+template <int PREC>
+cudaError_t launch_prec(const Variant& v, const TraceParams& p, int bx, int by, int num_sms, cudaStream_t s) {
+  if (v.sem == ST_SEM_RENDER) return launch_variant<PREC, 0, 0, ST_SEM_RENDER>(p, v.sched, bx, by, num_sms, s);
+  if (v.kerr) {
+    if (v.vol) return launch_variant<PREC, 1, 1, ST_SEM_DRAFT>(p, v.sched, bx, by, num_sms, s);
+    return launch_variant<PREC, 1, 0, ST_SEM_DRAFT>(p, v.sched, bx, by, num_sms, s);
+  }
+  if (v.vol) return launch_variant<PREC, 0, 1, ST_SEM_DRAFT>(p, v.sched, bx, by, num_sms, s);
+  return launch_variant<PREC, 0, 0, ST_SEM_DRAFT>(p, v.sched, bx, by, num_sms, s);
+}
+
+}  // namespace st

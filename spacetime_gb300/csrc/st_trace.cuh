@@ -1,0 +1,910 @@
+// st_trace.cuh -- device code of the null-geodesic trace (sm_103a).
+//
+// One ray = one pixel sample, traced backward from the camera in Cartesian
+// Kerr-Schild coordinates: tetrad ray generation, radius-adaptive RK4 with
+// horizon / escape termination, thin-disc or volumetric-gas shading, and the
+// equirectangular sky.  The rules follow SpaceTime.jl's two renderers:
+//   SEM = ST_SEM_DRAFT   trace_kernel_mtl!  (src/metal.jl:750-1707)
+//   SEM = ST_SEM_RENDER  render / _trace_color (src/raytrace.jl:225-428,
+//                        src/callbacks.jl:7-105, src/accretion_disc.jl:19-49)
+// Precision:
+//   ST_PREC_FP64          all double
+//   ST_PREC_FP32          all float (the reference kernel's arithmetic)
+//   ST_PREC_FP32_GUARDED  float RHS, float-float (TwoSum) state, FP64 steps
+//                         for guarded rays/regions, FP64 null renormalisation
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+#include "st_internal.h"
+
+namespace st {
+
+// ---------------------------------------------------------------------------
+// Scalar helpers: the double forms follow the oracle's arithmetic exactly;
+// the float forms use the MUFU reciprocal / reciprocal-sqrt.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+__device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+__device__ __forceinline__ float rcp_(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp_(double x) { return 1.0 / x; }
+__device__ __forceinline__ float exp_(float x) { return expf(x); }
+__device__ __forceinline__ double exp_(double x) { return exp(x); }
+__device__ __forceinline__ float log_(float x) { return logf(x); }
+__device__ __forceinline__ double log_(double x) { return log(x); }
+__device__ __forceinline__ float atan2_(float y, float x) { return atan2f(y, x); }
+__device__ __forceinline__ double atan2_(double y, double x) { return atan2(y, x); }
+__device__ __forceinline__ float acos_(float x) { return acosf(x); }
+__device__ __forceinline__ double acos_(double x) { return acos(x); }
+__device__ __forceinline__ float cos_(float x) { return cosf(x); }
+__device__ __forceinline__ double cos_(double x) { return cos(x); }
+__device__ __forceinline__ float sin_(float x) { return sinf(x); }
+__device__ __forceinline__ double sin_(double x) { return sin(x); }
+__device__ __forceinline__ float fabs_(float x) { return fabsf(x); }
+__device__ __forceinline__ double fabs_(double x) { return fabs(x); }
+__device__ __forceinline__ float floor_(float x) { return floorf(x); }
+__device__ __forceinline__ double floor_(double x) { return floor(x); }
+template <typename R> __device__ __forceinline__ R min_(R a, R b) { return a < b ? a : b; }
+template <typename R> __device__ __forceinline__ R max_(R a, R b) { return a > b ? a : b; }
+template <typename R> __device__ __forceinline__ R clamp_(R x, R lo, R hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+// r and 1/r from r^2
+__device__ __forceinline__ void r_and_inv(float r2, float& r, float& ir) { ir = rsqrtf(r2); r = r2 * ir; }
+__device__ __forceinline__ void r_and_inv(double r2, double& r, double& ir) { r = sqrt(r2); ir = 1.0 / r; }
+
+template <typename R> struct IsD { static constexpr bool v = std::is_same<R, double>::value; };
+
+// Integer hash -> [0,1): src/disc_sim.jl:83-91 (bit-exact).
+__device__ __forceinline__ float sim_hash(int x, int y, int z) {
+  uint32_t h = (uint32_t)x * 0x8da6b343u ^ (uint32_t)y * 0xd8163841u ^ (uint32_t)z * 0xcb1ab31fu;
+  h ^= h >> 13;
+  h *= 0x9e3779b9u;
+  h ^= h >> 16;
+  return (float)(h & 0x00ffffffu) * 5.9604645e-8f;
+}
+
+// ---------------------------------------------------------------------------
+// Geodesic RHS in Cartesian Kerr-Schild coordinates.
+// ---------------------------------------------------------------------------
+
+// Schwarzschild, src/gr.jl:85-109 / src/metal.jl:324-340.
+template <typename R>
+__device__ __forceinline__ void rhs_schw(const R* s, R pt, R M, R* d) {
+  const R x = s[0], y = s[1], z = s[2], px = s[3], py = s[4], pz = s[5];
+  const R r2 = x * x + y * y + z * z;
+  R inv_r;
+  if constexpr (IsD<R>::v) inv_r = 1.0 / sqrt(r2); else inv_r = rsqrtf(r2);
+  const R f = R(2) * M * inv_r;
+  const R kap = (x * px + y * py + z * pz) * inv_r;
+  const R ell = -pt + kap;
+  const R c1 = f * ell * inv_r;
+  const R c2 = f * ell * (R(0.5) * ell + kap) * inv_r * inv_r;
+  d[0] = px - c1 * x;
+  d[1] = py - c1 * y;
+  d[2] = pz - c1 * z;
+  d[3] = c1 * px - c2 * x;
+  d[4] = c1 * py - c2 * y;
+  d[5] = c1 * pz - c2 * z;
+}
+
+template <typename R>
+__device__ __forceinline__ R ks_r2(R x, R y, R z, R a) {
+  const R a2 = a * a;
+  const R w = x * x + y * y + z * z - a2;
+  return R(0.5) * (w + sqrt_(w * w + R(4) * a2 * z * z));
+}
+
+// Kerr, src/metal.jl:466-508 (implicit-quartic r, four derivative terms).
+template <typename R>
+__device__ __forceinline__ void rhs_kerr(const R* s, R pt, R M, R a, R* d) {
+  const R x = s[0], y = s[1], z = s[2], px = s[3], py = s[4], pz = s[5];
+  const R a2 = a * a, z2 = z * z;
+  R r2 = ks_r2(x, y, z, a);
+  r2 = max_(r2, R(1e-12));
+  R r, inv_r;
+  r_and_inv(r2, r, inv_r);
+  const R r3 = r2 * r;
+  const R inv_sig = rcp_(r2 * r2 + a2 * z2);
+  const R r2a = r2 + a2;
+  const R ira = rcp_(r2a);
+  const R Lx = (r * x + a * y) * ira;
+  const R Ly = (r * y - a * x) * ira;
+  const R Lz = z * inv_r;
+  const R ell = -pt + Lx * px + Ly * py + Lz * pz;
+  const R f = R(2) * M * r3 * inv_sig;
+  const R fl = f * ell;
+  const R drx = x * r3 * inv_sig;
+  const R dry = y * r3 * inv_sig;
+  const R drz = z * r * r2a * inv_sig;
+  const R dfdr = R(2) * M * r2 * (R(3) * a2 * z2 - r2 * r2) * inv_sig * inv_sig;
+  const R dfz0 = R(-4) * M * r3 * a2 * z * inv_sig * inv_sig;
+  const R dlx0 = (r * px - a * py) * ira;
+  const R dly0 = (a * px + r * py) * ira;
+  const R dlz0 = pz * inv_r;
+  const R dldr = (px * (x * r2a - R(2) * r * (r * x + a * y)) + py * (y * r2a - R(2) * r * (r * y - a * x))) *
+                     ira * ira -
+                 z * pz * inv_r * inv_r;
+  const R hl2 = R(0.5) * ell * ell;
+  d[0] = px - fl * Lx;
+  d[1] = py - fl * Ly;
+  d[2] = pz - fl * Lz;
+  d[3] = hl2 * (dfdr * drx) + fl * (dldr * drx + dlx0);
+  d[4] = hl2 * (dfdr * dry) + fl * (dldr * dry + dly0);
+  d[5] = hl2 * (dfdr * drz + dfz0) + fl * (dldr * drz + dlz0);
+}
+
+template <int KERR, typename R>
+__device__ __forceinline__ void rhs(const R* s, R pt, R M, R a, R* d) {
+  if constexpr (KERR) rhs_kerr(s, pt, M, a, d); else rhs_schw(s, pt, M, d);
+}
+
+// Classical RK4 increment (src/metal.jl:1382-1401); k1 is the slope at y.
+template <int KERR, typename R>
+__device__ __forceinline__ void rk4_inc(const R* y, R pt, R M, R a, R h, const R* k1, R* inc) {
+  R t[6], k[6], sum[6];
+  const R hh = R(0.5) * h;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) { t[i] = y[i] + hh * k1[i]; sum[i] = k1[i]; }
+  rhs<KERR>(t, pt, M, a, k);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) { sum[i] = sum[i] + R(2) * k[i]; t[i] = y[i] + hh * k[i]; }
+  rhs<KERR>(t, pt, M, a, k);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) { sum[i] = sum[i] + R(2) * k[i]; t[i] = y[i] + h * k[i]; }
+  rhs<KERR>(t, pt, M, a, k);
+  const R h6 = h / R(6);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) inc[i] = h6 * (sum[i] + k[i]);
+}
+
+// (hi + lo) += d with Knuth's TwoSum; hi keeps the rounded sum.
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float d) {
+  const float s = __fadd_rn(hi, d);
+  const float bb = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(d, bb));
+  const float l2 = __fadd_rn(lo, e);
+  const float t = __fadd_rn(s, l2);
+  lo = __fsub_rn(l2, __fsub_rn(t, s));
+  hi = t;
+}
+
+// ---------------------------------------------------------------------------
+// Emission models (see the oracle for the reference line numbers).
+// ---------------------------------------------------------------------------
+
+// Exact emitter shift 1+z = -p.u/E, src/metal.jl:396-428.
+template <typename R>
+__device__ __forceinline__ R emitter_opz(R sx, R sy, R psx, R psy, R E, R M, R a, R r_isco, R E_isco, R L_isco) {
+  const R a2 = a * a;
+  const R s2 = sx * sx + sy * sy;
+  const R r = sqrt_(max_(s2 - a2, R(1e-6)));
+  const R sqM = sqrt_(M), sqr = sqrt_(r), r32 = r * sqr;
+  const R delta = r * r - R(2) * M * r + a2;
+  R ut, uphi, ur = R(0);
+  if (r >= r_isco) {
+    const R den = r32 - R(3) * M * sqr + R(2) * a * sqM;
+    ut = (r32 + a * sqM) / (sqrt_(r32) * sqrt_(max_(den, R(1e-2))));
+    uphi = sqM / (r32 + a * sqM) * ut;
+  } else {
+    const R inv_d = R(1) / max_(delta, R(1e-3));
+    ut = ((r * r + a2 + R(2) * M * a2 / r) * E_isco - R(2) * M * a * L_isco / r) * inv_d;
+    uphi = (R(2) * M * a * E_isco / r + (R(1) - R(2) * M / r) * L_isco) * inv_d;
+    const R t1 = E_isco * (r * r + a2) - a * L_isco;
+    const R t2 = L_isco - a * E_isco;
+    const R Rr = t1 * t1 - delta * (r * r + t2 * t2);
+    ur = -sqrt_(max_(Rr, R(0))) / (r * r);
+    ut += R(2) * M * r * inv_d * ur;
+    uphi += a * inv_d * ur;
+  }
+  const R inv_s2 = R(1) / max_(s2, R(1e-6));
+  const R cphi = (r * sx + a * sy) * inv_s2;
+  const R sphi = (r * sy - a * sx) * inv_s2;
+  const R ux = ur * cphi - sy * uphi;
+  const R uy = ur * sphi + sx * uphi;
+  const R Es = fabs_(E) > R(1e-6) ? E : R(1e-6);
+  return clamp_(ut - (psx * ux + psy * uy) / Es, R(0.1), R(20));
+}
+
+// LUT colour; RENDER rounds half to even (Julia round), DRAFT truncates x+0.5.
+template <typename R>
+__device__ __forceinline__ float4 lut_color(const TraceParams& p, R T, bool render_rule) {
+  const R tmin = R(p.lut_tmin), tmax = R(p.lut_tmax);
+  const R fr = (clamp_(T, tmin, tmax) - tmin) / (tmax - tmin);
+  int idx;
+  if (render_rule) idx = (int)rint(fr * R(p.lut_size - 1));
+  else idx = (int)(fr * (R(p.lut_size) - R(1)) + R(0.5));
+  idx = min(max(idx, 0), p.lut_size - 1);
+  return __ldg(p.lut + idx);
+}
+
+// Trilinear gas density, src/metal.jl:569-610.
+template <typename R>
+__device__ __forceinline__ R sample_volume(const TraceParams& p, R sc, R phi, R z) {
+  const R zmax = R(p.zmax);
+  if (sc <= R(0) || fabs_(z) >= zmax) return R(0);
+  const R ls = log_(sc);
+  const R lin = R(p.ls_in), lout = R(p.ls_out);
+  if (ls <= lin || ls >= lout) return R(0);
+  const int nr = p.nr, nphi = p.nphi, nz = p.nz;
+  const R two_pi = R(6.283185307179586);
+  const R fr = (ls - lin) / (lout - lin) * R(nr - 1);
+  R pm = IsD<R>::v ? (R)fmod((double)phi, 6.283185307179586) : (R)fmodf((float)phi, 6.2831855f);
+  if (pm < R(0)) pm += two_pi;
+  const R fp = pm / two_pi * R(nphi);
+  const R fz = (z + zmax) / (R(2) * zmax) * R(nz - 1);
+  const int i0 = min(max((int)floor_(fr), 0), nr - 2);
+  const R tr = fr - R(i0);
+  const int j0 = (int)floor_(fp);
+  const R tp = fp - R(j0);
+  const int k0 = min(max((int)floor_(fz), 0), nz - 2);
+  const R tz = fz - R(k0);
+  const int ja = ((j0 % nphi) + nphi) % nphi;
+  const int jb = (((j0 + 1) % nphi) + nphi) % nphi;
+  const float* v = p.vol;
+  const size_t sj = (size_t)nr, sk = (size_t)nr * nphi;
+  const size_t b00 = (size_t)i0 + sj * ja + sk * k0, b10 = (size_t)i0 + sj * jb + sk * k0;
+  const size_t b01 = b00 + sk, b11 = b10 + sk;
+  const R d000 = __ldg(v + b00), d100 = __ldg(v + b00 + 1);
+  const R d010 = __ldg(v + b10), d110 = __ldg(v + b10 + 1);
+  const R d001 = __ldg(v + b01), d101 = __ldg(v + b01 + 1);
+  const R d011 = __ldg(v + b11), d111 = __ldg(v + b11 + 1);
+  const R c00 = d000 + tr * (d100 - d000);
+  const R c10 = d010 + tr * (d110 - d010);
+  const R c01 = d001 + tr * (d101 - d001);
+  const R c11 = d011 + tr * (d111 - d011);
+  const R c0 = c00 + tp * (c10 - c00);
+  const R c1 = c01 + tp * (c11 - c01);
+  return c0 + tz * (c1 - c0);
+}
+
+// Bilinear equirectangular sky, src/metal.jl:523-561 / src/raytrace.jl:154-177.
+template <typename R>
+__device__ __forceinline__ void sample_sky(const TraceParams& p, R theta, R phi, R* rgb) {
+  const int W = p.sky_w, H = p.sky_h;
+  const R pi = R(3.141592653589793), two_pi = R(6.283185307179586);
+  const R v = clamp_(theta / pi, R(0), R(1));
+  R pm = IsD<R>::v ? (R)fmod((double)phi, 6.283185307179586) : (R)fmodf((float)phi, 6.2831855f);
+  if (pm < R(0)) pm += two_pi;
+  const R u = clamp_(pm / two_pi, R(0), R(1));
+  const R xf = u * R(W - 1), yf = v * R(H - 1);
+  const int x0 = min(max((int)floor_(xf), 0), W - 1);
+  const int x1 = min(x0 + 1, W - 1);
+  const int y0 = min(max((int)floor_(yf), 0), H - 1);
+  const int y1 = min(y0 + 1, H - 1);
+  const R fx = xf - R(x0), fy = yf - R(y0);
+  const float4 c00 = __ldg(p.sky + (size_t)y0 * W + x0), c10 = __ldg(p.sky + (size_t)y0 * W + x1);
+  const float4 c01 = __ldg(p.sky + (size_t)y1 * W + x0), c11 = __ldg(p.sky + (size_t)y1 * W + x1);
+  const R w00 = (R(1) - fx) * (R(1) - fy), w10 = fx * (R(1) - fy), w01 = (R(1) - fx) * fy, w11 = fx * fy;
+  rgb[0] = R(c00.x) * w00 + R(c10.x) * w10 + R(c01.x) * w01 + R(c11.x) * w11;
+  rgb[1] = R(c00.y) * w00 + R(c10.y) * w10 + R(c01.y) * w01 + R(c11.y) * w11;
+  rgb[2] = R(c00.z) * w00 + R(c10.z) * w10 + R(c01.z) * w01 + R(c11.z) * w11;
+}
+
+// ---------------------------------------------------------------------------
+// Ray state machine.
+// ---------------------------------------------------------------------------
+
+template <int PREC>
+struct RealOf { using T = float; };
+template <>
+struct RealOf<ST_PREC_FP64> { using T = double; };
+
+template <typename R>
+struct RayState {
+  R y[6];        // (x, y, z, p_x, p_y, p_z); hi parts under FP32_GUARDED
+  float lo[6];   // FP32_GUARDED low parts
+  R pt;          // conserved p_t
+  R scam;        // camera shift applied to shading (1 if not relativistic)
+  R acc[3];
+  R alpha;
+  R r_prev;      // DRAFT Schwarzschild inward test
+  R r_floor;
+  R march_acc;   // arc length since the last gas sample
+  R lambda;      // affine parameter (RENDER budget)
+  int steps, fp64_steps, gas;
+  int flags;     // ST_RAY_* bits in progress
+  int pix;       // global ray index
+  float r_cross, g_cross;
+  R r_esc;       // escape radius of this ray's frame
+  int nmax;      // step budget of this ray's frame
+  bool inside0;  // RENDER: camera inside r = 2.00001
+  bool guard_ray;
+};
+
+// Camera tetrad for the current ray; per-frame data lives in TraceParams for
+// single frames and in FrameCam for batched tracks (st_render_frames).
+struct CamView {
+  const double* pos;
+  const double* Ef;
+  const double* Er;
+  const double* Eu;
+  const double* U;
+  double r_escape;
+  int nmax;
+};
+
+template <int KERR, typename D>
+__device__ __forceinline__ void lower_photon(const D* x, const D* q, D M, D a, D* s, D* pt) {
+  D l[3], f;
+  if constexpr (KERR) {
+    const D a2 = a * a;
+    const D rk2 = ks_r2(x[0], x[1], x[2], a);
+    const D rk = sqrt_(max_(rk2, D(1e-12)));
+    const D ira = D(1) / (rk2 + a2);
+    l[0] = (rk * x[0] + a * x[1]) * ira;
+    l[1] = (rk * x[1] - a * x[0]) * ira;
+    l[2] = x[2] / rk;
+    f = D(2) * M * rk2 * rk / (rk2 * rk2 + a2 * x[2] * x[2]);
+  } else {
+    const D r = sqrt_(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+    l[0] = x[0] / r; l[1] = x[1] / r; l[2] = x[2] / r;
+    f = D(2) * M / r;
+  }
+  const D lq = q[0] + l[0] * q[1] + l[1] * q[2] + l[2] * q[3];
+  *pt = -q[0] + f * lq;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) { s[k] = x[k]; s[k + 3] = q[k + 1] + f * lq * l[k]; }
+}
+
+// Bardeen launch-time capture test (Kerr), src/metal.jl:1026-1094.
+template <typename D>
+__device__ void bardeen(const D* y, D pt, D M, D a, bool* captured0, bool* graze0) {
+  *captured0 = false;
+  *graze0 = false;
+  const D E0 = -pt;
+  if (!(fabs_(E0) > D(1e-6))) return;
+  const D x = y[0], yy = y[1], z = y[2], px = y[3], py = y[4], pz = y[5];
+  const D a2 = a * a;
+  const D rk2 = ks_r2(x, yy, z, a);
+  const D rk = sqrt_(max_(rk2, D(1e-12)));
+  const D cth = z / rk;
+  const D s2 = max_(D(1) - cth * cth, D(1e-8));
+  const D sth = sqrt_(s2);
+  const D Lz0 = x * py - yy * px;
+  const D pth = (cth / sth) * (x * px + yy * py) - rk * sth * pz;
+  const D Q0 = pth * pth + cth * cth * (Lz0 * Lz0 / s2 - a2 * E0 * E0);
+  const D lam = Lz0 / E0, eta = Q0 / (E0 * E0);
+  const D c2 = a2 - lam * lam - eta;
+  const D c1 = D(2) * M * (eta + (lam - a) * (lam - a));
+  const D c0 = -a2 * eta;
+  const D rplus = M + sqrt_(max_(M * M - a2, D(0)));
+  D v[6];
+  rhs_kerr(y, pt, M, a, v);
+  const D rdot = rk2 * (x * v[0] + yy * v[1]) + (rk2 + a2) * z * v[2];
+  if (!(rdot < D(0))) return;
+  const D pb = D(0.5) * c2, qb = D(0.25) * c1;
+  const D Db = D(0.25) * qb * qb + pb * pb * pb / D(27);
+  bool cap = true;
+  if (Db >= D(0)) {
+    const D sD = sqrt_(Db);
+    const D u1 = D(-0.5) * qb + sD, u2 = D(-0.5) * qb - sD;
+    const D s1 = u1 > D(0) ? D(1) : (u1 < D(0) ? D(-1) : D(0));
+    const D s2b = u2 > D(0) ? D(1) : (u2 < D(0) ? D(-1) : D(0));
+    const D rc = s1 * exp_(log_(max_(fabs_(u1), D(1e-30))) / D(3)) + s2b * exp_(log_(max_(fabs_(u2), D(1e-30))) / D(3));
+    if (rc > rplus && rc < rk) {
+      const D Rv = ((rc * rc + c2) * rc + c1) * rc + c0;
+      cap = Rv > D(0);
+      if (fabs_(Rv) < D(0.08) * max_(rc * rc * rc * rc, D(1))) *graze0 = true;
+    }
+  } else {
+    const D mb = D(2) * sqrt_(-pb / D(3));
+    const D ac = clamp_(D(3) * qb / (pb * mb), D(-1), D(1));
+    const D tb = acos_(ac) / D(3);
+#pragma unroll
+    for (int kk = 0; kk < 3; ++kk) {
+      const D rc = mb * cos_(tb - D(2.0943951023931953) * D(kk));
+      if (rc > rplus && rc < rk) {
+        const D Rv = ((rc * rc + c2) * rc + c1) * rc + c0;
+        if (Rv <= D(0)) cap = false;
+        if (fabs_(Rv) < D(0.08) * max_(rc * rc * rc * rc, D(1))) *graze0 = true;
+      }
+    }
+  }
+  *captured0 = cap;
+}
+
+// Build the ray of pixel (i0, j0) (0-based, frame-local).  Ray generation and
+// index lowering run in D (double for FP64 and FP32_GUARDED, float for FP32).
+template <int PREC, int KERR, int SEM>
+__device__ void init_ray(const TraceParams& p, const CamView& cam, int i0, int j0, RayState<typename RealOf<PREC>::T>& st) {
+  using R = typename RealOf<PREC>::T;
+  using D = typename std::conditional<PREC == ST_PREC_FP32, float, double>::type;
+  const int i1 = i0 + 1, j1 = j0 + 1;
+  D ju = D(p.ju), jv = D(p.jv);
+  if (p.jw > 0.0) {
+    ju += D(sim_hash(i1, j1, p.jseed)) * D(p.jw);
+    jv += D(sim_hash(i1, j1, p.jseed + 271)) * D(p.jw);
+  }
+  const D half_h = D(p.height) / D(2);
+  const D u = (D(i1) - D(1) + ju - D(p.width) / D(2)) / half_h;
+  const D v = (D(j1) - D(1) + jv - D(p.height) / D(2)) / half_h;
+  D offr = D(0), offu = D(0);
+  if (p.lens_w > 0.0 && p.ap_r > 0.0) {
+    const D u01 = D(p.lens_u0) + D(sim_hash(i1, j1, p.lens_seed)) * D(p.lens_w);
+    const D v01 = D(p.lens_v0) + D(sim_hash(i1, j1, p.lens_seed + 7919)) * D(p.lens_w);
+    const D ox = D(2) * u01 - D(1), oy = D(2) * v01 - D(1);
+    if (ox != D(0) || oy != D(0)) {
+      D rr, th;
+      const D qpi = D(0.7853981633974483);
+      if (fabs_(ox) > fabs_(oy)) { rr = ox; th = qpi * (oy / ox); }
+      else { rr = oy; th = D(2) * qpi - qpi * (ox / oy); }
+      offr = D(p.ap_r) * rr * cos_(th);
+      offu = D(p.ap_r) * rr * sin_(th);
+    }
+  }
+  D cf, cr, cu;
+  if (p.projection == ST_PROJ_FISHEYE) {
+    const D rho = sqrt_(u * u + v * v);
+    const D tp = rho * D(p.fisheye_rad);
+    const D s = sin_(tp);
+    const D ir = rho > D(1e-8) ? D(1) / rho : D(0);
+    cr = s * u * ir; cu = s * v * ir; cf = cos_(tp);
+  } else {
+    D dxl = u * D(p.fov), dyl = v * D(p.fov);
+    D nu = sqrt_(dxl * dxl + dyl * dyl + D(1));
+    if (offr != D(0) || offu != D(0)) {
+      const D k = nu / D(p.focus);
+      dxl -= offr * k; dyl -= offu * k;
+      nu = sqrt_(dxl * dxl + dyl * dyl + D(1));
+    }
+    cr = dxl / nu; cu = dyl / nu; cf = D(1) / nu;
+  }
+  D x[3], q[4];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) x[k] = D(cam.pos[k]) + offr * D(cam.Er[k + 1]) + offu * D(cam.Eu[k + 1]);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) q[k] = cf * D(cam.Ef[k]) + cr * D(cam.Er[k]) + cu * D(cam.Eu[k]) - D(cam.U[k]);
+  D s[6], pt;
+  lower_photon<KERR>(x, q, D(p.M), D(p.a), s, &pt);
+
+  st.flags = 0;
+  st.guard_ray = false;
+  if constexpr (KERR && SEM == ST_SEM_DRAFT) {
+    bool c0 = false, g0 = false;
+    bardeen(s, pt, D(p.M), D(p.a), &c0, &g0);
+    if (c0) st.flags |= ST_RAY_BCAPT;
+    if (g0) st.flags |= ST_RAY_GRAZE;
+    st.guard_ray = g0;
+  }
+  if constexpr (!KERR && PREC == ST_PREC_FP32_GUARDED) {
+    // critical impact-parameter band: b = |x cross p| / E, b_crit = 3 sqrt(3) M
+    const D Lx = s[1] * s[5] - s[2] * s[4], Ly = s[2] * s[3] - s[0] * s[5], Lz = s[0] * s[4] - s[1] * s[3];
+    const D b = sqrt_(Lx * Lx + Ly * Ly + Lz * Lz) / fabs_(pt);
+    st.guard_ray = fabs_(b - D(p.b_crit)) < D(p.crit_band);
+  }
+  if constexpr (PREC == ST_PREC_FP32_GUARDED) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const float h = (float)s[k];
+      st.y[k] = h;
+      st.lo[k] = (float)(s[k] - (D)h);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) { st.y[k] = R(s[k]); st.lo[k] = 0.f; }
+  }
+  st.pt = R(pt);
+  const D g = D(1) / clamp_(fabs_(pt), D(0.05), D(20));
+  st.scam = p.relativistic ? R(g) : R(1);
+  st.acc[0] = st.acc[1] = st.acc[2] = R(0);
+  st.alpha = R(1);
+  st.r_prev = R(-1);
+  const D r0 = sqrt_(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+  st.r_floor = r0 > D(2.05) * D(p.M) ? R(2) * R(p.M) : R(0.3) * R(p.M);
+  st.inside0 = r0 < D(2.00001);
+  st.march_acc = R(0);
+  st.lambda = R(0);
+  st.r_esc = R(cam.r_escape);
+  st.nmax = cam.nmax;
+  st.steps = st.fp64_steps = st.gas = 0;
+  st.r_cross = -1.f;
+  st.g_cross = 0.f;
+}
+
+// ---- shading pieces applied at interpolated points --------------------------
+
+template <typename R>
+__device__ __forceinline__ R disc_kepler(const TraceParams& p, R X0, R X1, const R* Pm, R pt, R gcam, R* acc, R* alpha) {
+  const R M = R(p.M);
+  const R r = sqrt_(X0 * X0 + X1 * X1);
+  if (!(R(p.disc_inner) < r && r < R(p.disc_outer))) return R(0);
+  const R f = R(2) * M / r;
+  const R kap = (X0 * Pm[0] + X1 * Pm[1]) / r;
+  const R c1 = f * (-pt + kap) / r;
+  const R pc0 = Pm[0] - c1 * X0, pc1 = Pm[1] - c1 * X1, pc2 = Pm[2];
+  const R R_ = r / (R(2) * M);
+  const R T_emit = exp_(R(10.034259) - R(0.375) * log_(R_ * R_));
+  R vmag = R(0.70710678) / sqrt_(max_(R_ - R(1), R(0.1)));
+  vmag = clamp_(vmag, R(0), R(0.999));
+  const R n0 = X0 / r, n1 = X1 / r;
+  const R dv0 = -vmag * n1, dv1 = vmag * n0;
+  const R vsq = clamp_(dv0 * dv0 + dv1 * dv1, R(0), R(0.99));
+  const R gam = R(1) / sqrt_(R(1) - vsq);
+  const R pn = sqrt_(pc0 * pc0 + pc1 * pc1 + pc2 * pc2);
+  const R opz_d = gam * (R(1) + (dv0 * pc0 + dv1 * pc1) / pn);
+  const R opz_g = R(1) / sqrt_(max_(R(1) - R(1) / max_(R_, R(1)), R(0.01)));
+  const R T_obs = T_emit * gcam / max_(opz_d * opz_g, R(0.1));
+  const R inten = R(100) / (exp_(R(29622.4) / max_(T_obs, R(1))) - R(1));
+  const float4 col = lut_color(p, T_obs, true);
+  const R R_in = R(p.disc_inner) / (R(2) * M), R_out = R(p.disc_outer) / (R(2) * M);
+  const R iscotaper = clamp_((R_ * R_ - R_in * R_in) * R(0.3), R(0), R(1));
+  const R outertaper = clamp_(T_emit / R(1000), R(0), R(1));
+  const R dens = clamp_((R_out - R_) / (R_out - R_in), R(0), R(1));
+  const R fall = R(p.disc_falloff);
+  const R dpow = (fall == R(0)) ? R(1) : (dens <= R(0) ? R(0) : exp_(fall * log_(dens)));
+  const R op = iscotaper * outertaper * dpow;
+  const R w = inten * (*alpha * op);
+  acc[0] += w * R(col.x); acc[1] += w * R(col.y); acc[2] += w * R(col.z);
+  *alpha *= (R(1) - op);
+  return T_obs / T_emit;
+}
+
+template <typename R>
+__device__ __forceinline__ R disc_exact(const TraceParams& p, R xh, R yh, R pxh, R pyh, R pt, R scam, R* acc, R* alpha) {
+  const R M = R(p.M);
+  const R sc = sqrt_(xh * xh + yh * yh);
+  if (!(R(p.disc_inner) < sc && sc < R(p.disc_outer))) return R(0);
+  const R r_isco = R(p.r_isco);
+  const R R_ = sc / (R(2) * M);
+  const R RT = max_(sc, r_isco) / (R(2) * M);
+  const R T_emit = exp_(R(10.034259) - R(0.375) * log_(RT * RT));
+  const R t3 = sc / r_isco;
+  const R plunge = sc < r_isco ? t3 * t3 * t3 : R(1);
+  const R opz = emitter_opz(xh, yh, pxh, pyh, -pt, M, R(p.a), r_isco, R(p.E_isco), R(p.L_isco));
+  const R T_obs = T_emit * scam / opz;
+  const R inten = R(100) / (exp_(R(29622.4) / max_(T_obs, R(1))) - R(1));
+  const float4 col = lut_color(p, T_obs, false);
+  const R R_in = R(p.disc_inner) / (R(2) * M), R_out = R(p.disc_outer) / (R(2) * M);
+  const R iscotaper = clamp_((R_ * R_ - R_in * R_in) * R(0.3), R(0), R(1));
+  const R outertaper = clamp_(T_emit / R(1000), R(0), R(1));
+  const R dens = clamp_((R_out - R_) / (R_out - R_in), R(0), R(1));
+  const R fall = R(p.disc_falloff);
+  const R dpow = dens <= R(1e-6) ? (fall > R(0) ? R(0) : R(1)) : exp_(fall * log_(dens));
+  const R op = iscotaper * outertaper * dpow * plunge;
+  const R w = *alpha * op * inten;
+  acc[0] += w * R(col.x); acc[1] += w * R(col.y); acc[2] += w * R(col.z);
+  *alpha *= (R(1) - op);
+  return T_obs / T_emit;
+}
+
+// Gas march along one accepted step, src/metal.jl:1429-1513.  Returns true
+// when the transmittance is exhausted.
+template <typename R>
+__device__ __forceinline__ bool march_gas(const TraceParams& p, const R* yp, const R* yn, R r2p, R h_used, R vlen,
+                                          RayState<R>& st) {
+  const R r2n = yn[0] * yn[0] + yn[1] * yn[1] + yn[2] * yn[2];
+  if (!(st.alpha > R(0.003) && min_(r2p, r2n) < R(p.vol_rb2))) return false;
+  const R ds = R(p.ds_gas);
+  const R seg = h_used * vlen;
+  R t_s = ds - st.march_acc;
+  if (t_s > seg) { st.march_acc += seg; return false; }
+  const R zmax = R(p.zmax);
+  const R r_isco = R(p.r_isco), M = R(p.M);
+  const R inv_seg = R(1) / seg;
+  while (t_s <= seg && st.alpha > R(0.003)) {
+    const R fs = IsD<R>::v ? t_s / seg : t_s * inv_seg;
+    const R sx = yp[0] + fs * (yn[0] - yp[0]);
+    const R sy = yp[1] + fs * (yn[1] - yp[1]);
+    const R sz = yp[2] + fs * (yn[2] - yp[2]);
+    if (fabs_(sz) < zmax) {
+      const R scyl = sqrt_(sx * sx + sy * sy);
+      if (scyl > R(1e-6)) {
+        const R phi = atan2_(sy, sx);
+        R rho = sample_volume(p, scyl, phi, sz);
+        ++st.gas;
+        if (rho > R(1e-4)) {
+          const R Rr = max_(scyl, r_isco) / (R(2) * M);
+          const R T_emit = exp_(R(10.034259) - R(0.375) * log_(max_(Rr * Rr, R(1e-6))));
+          if (scyl < r_isco) { const R t3 = scyl / r_isco; rho *= t3 * t3 * t3; }
+          const R psx = yp[3] + fs * (yn[3] - yp[3]);
+          const R psy = yp[4] + fs * (yn[4] - yp[4]);
+          const R opz = emitter_opz(sx, sy, psx, psy, -st.pt, M, R(p.a), r_isco, R(p.E_isco), R(p.L_isco));
+          const R T_obs = T_emit * st.scam / opz;
+          const R inten = R(100) / (exp_(R(29622.4) / max_(T_obs, R(1))) - R(1));
+          const float4 col = lut_color(p, T_obs, false);
+          const R tau = R(p.opac) * rho * ds;
+          const R aa = R(1) - exp_(-tau);
+          const R w = st.alpha * aa * inten * R(p.emis);
+          st.acc[0] += w * R(col.x); st.acc[1] += w * R(col.y); st.acc[2] += w * R(col.z);
+          st.alpha *= (R(1) - aa);
+        }
+      }
+    }
+    t_s += ds;
+  }
+  st.march_acc = seg - (t_s - ds);
+  return st.alpha < R(0.003);
+}
+
+// Null-constraint renormalisation in FP64: rescale the spatial momentum so
+// that H = 1/2(-p_t^2 + |p|^2 - f l^2) = 0 at fixed p_t.
+template <int KERR>
+__device__ __forceinline__ void null_renorm(double* y, double pt, double M, double a) {
+  double f, L[3];
+  if constexpr (KERR) {
+    const double a2 = a * a;
+    const double r2 = fmax(ks_r2(y[0], y[1], y[2], a), 1e-12);
+    const double r = sqrt(r2);
+    const double ira = 1.0 / (r2 + a2);
+    L[0] = (r * y[0] + a * y[1]) * ira;
+    L[1] = (r * y[1] - a * y[0]) * ira;
+    L[2] = y[2] / r;
+    f = 2.0 * M * r2 * r / (r2 * r2 + a2 * y[2] * y[2]);
+  } else {
+    const double r = sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+    L[0] = y[0] / r; L[1] = y[1] / r; L[2] = y[2] / r;
+    f = 2.0 * M / r;
+  }
+  const double kap = L[0] * y[3] + L[1] * y[4] + L[2] * y[5];
+  const double pp = y[3] * y[3] + y[4] * y[4] + y[5] * y[5];
+  const double A = pp - f * kap * kap;
+  const double B = 2.0 * f * pt * kap;
+  const double C = -(1.0 + f) * pt * pt;
+  const double disc = B * B - 4.0 * A * C;
+  if (!(A > 0.0) || !(disc >= 0.0)) return;
+  const double lam = (-B + sqrt(disc)) / (2.0 * A);
+  if (lam > 0.9 && lam < 1.1) { y[3] *= lam; y[4] *= lam; y[5] *= lam; }
+}
+
+// One integration step for the variant; returns true when the ray is done.
+// Mirrors the step loop of src/metal.jl:1201-1572 (DRAFT) and the callback
+// structure of src/raytrace.jl:339-373 (RENDER).
+template <int PREC, int KERR, int VOL, int SEM>
+__device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename RealOf<PREC>::T>& st) {
+  using R = typename RealOf<PREC>::T;
+  const R M = R(p.M), a = R(p.a);
+  R* y = st.y;
+  const R r2 = y[0] * y[0] + y[1] * y[1] + y[2] * y[2];
+  const R r = sqrt_(r2);
+  R rk2 = r2;
+  if (st.steps >= st.nmax) { st.flags |= ST_RAY_BUDGET; return true; }
+  if constexpr (SEM == ST_SEM_DRAFT) {
+    if constexpr (KERR) {
+      rk2 = ks_r2(y[0], y[1], y[2], a);
+      if (rk2 < R(p.rkill2)) { st.flags |= ST_RAY_CAPTURED; return true; }
+    } else {
+      if (r < R(3.2) * M) {
+        if (r < st.r_floor || (r < R(2.95) * M && st.r_prev > R(0) && r < st.r_prev - R(1e-4) * M)) {
+          st.flags |= ST_RAY_CAPTURED;
+          return true;
+        }
+        st.r_prev = r;
+      }
+    }
+    if (r > st.r_esc) { st.flags |= ST_RAY_ESCAPED; return true; }
+  } else {
+    if (r >= st.r_esc) { st.flags |= ST_RAY_ESCAPED; return true; }
+    if (st.lambda >= R(p.tspan)) { st.flags |= ST_RAY_BUDGET; return true; }
+    // A ray moving inward below 2.95M never escapes (escaping rays have
+    // periapsis > 3M).  In ingoing KS coordinates the backward ray reaches the
+    // past horizon only asymptotically, which a fixed step cannot follow, so
+    // it ends here as horizon-bound (the reference's adaptive integrator
+    // follows it down to its r = 2.00001 callback; the colour is the same).
+    if (r < R(2.95) * M && st.r_prev > R(0) && r < st.r_prev - R(1e-4) * M) {
+      st.flags |= ST_RAY_CAPTURED;
+      return true;
+    }
+    st.r_prev = r;
+  }
+  // radius-adaptive step, src/metal.jl:1250-1260
+  const R cap = (VOL && r2 < R(p.vol_rb2)) ? R(2) : R(p.hcap);
+  R h = R(p.dt) * min_(max_(R(p.hcoef) * r / M, R(1)), cap);
+  if constexpr (KERR) {
+    const R rk = R(p.rkill2);
+    const R fr = clamp_((rk2 - rk) / max_(rk, R(1e-6)), R(0), R(1));
+    h *= R(0.12) + R(0.88) * fr;
+  }
+  if constexpr (SEM == ST_SEM_RENDER) h = min_(h, R(p.tspan) - st.lambda);
+
+  R yp[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) yp[k] = y[k];
+  R k1[6];
+  rhs<KERR>(y, st.pt, M, a, k1);
+
+  bool fp64_step = false;
+  if constexpr (PREC == ST_PREC_FP32_GUARDED) {
+    fp64_step = st.guard_ray || (!(st.flags & ST_RAY_BCAPT) && rk2 < R(p.r_guard2));
+  }
+  if (fp64_step) {
+    if constexpr (PREC == ST_PREC_FP32_GUARDED) {
+      double yd[6], k1d[6], inc[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) yd[k] = (double)y[k] + (double)st.lo[k];
+      const double ptd = (double)st.pt;
+      rhs<KERR>(yd, ptd, p.M, p.a, k1d);
+      rk4_inc<KERR>(yd, ptd, p.M, p.a, (double)h, k1d, inc);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const double v = yd[k] + inc[k];
+        const float hi = (float)v;
+        y[k] = hi;
+        st.lo[k] = (float)(v - (double)hi);
+      }
+      ++st.fp64_steps;
+    }
+  } else {
+    R inc[6];
+    rk4_inc<KERR>(y, st.pt, M, a, h, k1, inc);
+    if constexpr (PREC == ST_PREC_FP32_GUARDED) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) ff_add(y[k], st.lo[k], inc[k]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) y[k] = y[k] + inc[k];
+    }
+  }
+  ++st.steps;
+  if constexpr (PREC == ST_PREC_FP32_GUARDED) {
+    if (p.renorm_every > 0 && (st.steps % p.renorm_every) == 0) {
+      double yd[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) yd[k] = (double)y[k] + (double)st.lo[k];
+      null_renorm<KERR>(yd, (double)st.pt, p.M, p.a);
+#pragma unroll
+      for (int k = 3; k < 6; ++k) {
+        const float hi = (float)yd[k];
+        y[k] = hi;
+        st.lo[k] = (float)(yd[k] - (double)hi);
+      }
+    }
+  }
+  if (!(y[0] == y[0]) || !(y[2] == y[2]) || !(y[3] == y[3])) { st.flags |= ST_RAY_CAPTURED; return true; }
+
+  if constexpr (SEM == ST_SEM_DRAFT) {
+    const R vlen = max_(sqrt_(k1[0] * k1[0] + k1[1] * k1[1] + k1[2] * k1[2]), R(1e-20));
+    if constexpr (VOL) {
+      if (march_gas(p, yp, y, r2, h, vlen, st)) return true;
+    } else {
+      if (p.disc_on && st.alpha > R(0.001) && yp[2] * y[2] < R(0)) {
+        const R cfz = yp[2] / (yp[2] - y[2]);
+        const R xh = yp[0] + cfz * (y[0] - yp[0]);
+        const R yh = yp[1] + cfz * (y[1] - yp[1]);
+        const R pxh = yp[3] + cfz * (y[3] - yp[3]);
+        const R pyh = yp[4] + cfz * (y[4] - yp[4]);
+        R g;
+        if (p.emitter == ST_EMIT_KEPLER) {
+          const R pzh = yp[5] + cfz * (y[5] - yp[5]);
+          const R Pm[3] = {pxh, pyh, pzh};
+          g = disc_kepler(p, xh, yh, Pm, st.pt, st.scam, st.acc, &st.alpha);
+        } else {
+          g = disc_exact(p, xh, yh, pxh, pyh, st.pt, st.scam, st.acc, &st.alpha);
+        }
+        if (g > R(0) && st.r_cross < 0.f) {
+          st.r_cross = (float)sqrt_(xh * xh + yh * yh);
+          st.g_cross = (float)g;
+          st.flags |= ST_RAY_CROSSED;
+        }
+      }
+    }
+    if (p.exit_landing) {
+      const R rn = sqrt_(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+      if (rn > st.r_esc) {
+        // two secant iterations on the step size from the saved state
+        const R re = st.r_esc;
+        R ha = h, ra = rn;
+        R hb = h * (re - r) / (rn - r);
+        R inc[6], yt[6];
+#pragma unroll 1
+        for (int it = 0; it < 2; ++it) {
+          rk4_inc<KERR>(yp, st.pt, M, a, hb, k1, inc);
+#pragma unroll
+          for (int k = 0; k < 6; ++k) yt[k] = yp[k] + inc[k];
+          const R rb = sqrt_(yt[0] * yt[0] + yt[1] * yt[1] + yt[2] * yt[2]);
+          if (it == 1 || rb == ra) break;
+          const R hn = hb + (re - rb) * (hb - ha) / (rb - ra);
+          ha = hb; ra = rb; hb = hn;
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) { y[k] = yt[k]; st.lo[k] = 0.f; }
+        st.flags |= ST_RAY_ESCAPED;
+        return true;
+      }
+    }
+  } else {
+    // RENDER: z = 0 disc events (shading only), then the terminating boundary
+    if (p.disc_on && yp[2] * y[2] < R(0)) {
+      const R cfz = yp[2] / (yp[2] - y[2]);
+      const R xh = yp[0] + cfz * (y[0] - yp[0]);
+      const R yh = yp[1] + cfz * (y[1] - yp[1]);
+      const R Pm[3] = {yp[3] + cfz * (y[3] - yp[3]), yp[4] + cfz * (y[4] - yp[4]), yp[5] + cfz * (y[5] - yp[5])};
+      R g;
+      if (p.emitter == ST_EMIT_KEPLER) g = disc_kepler(p, xh, yh, Pm, st.pt, st.scam, st.acc, &st.alpha);
+      else g = disc_exact(p, xh, yh, Pm[0], Pm[1], st.pt, st.scam, st.acc, &st.alpha);
+      if (g > R(0) && st.r_cross < 0.f) {
+        st.r_cross = (float)sqrt_(xh * xh + yh * yh);
+        st.g_cross = (float)g;
+        st.flags |= ST_RAY_CROSSED;
+      }
+    }
+    st.lambda += h;
+    const R rn = sqrt_(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+    R rb = R(-1);
+    if (st.inside0) { if (rn >= R(2.00001)) rb = R(2.00001); }
+    else if (rn <= R(2.00001)) rb = R(2.00001);
+    else if (rn >= st.r_esc) rb = st.r_esc;
+    if (rb > R(0)) {
+      R ha = h, ra = rn;
+      R hb = h * (rb - r) / (rn - r);
+      R inc[6], yt[6];
+#pragma unroll 1
+      for (int it = 0; it < 2; ++it) {
+        rk4_inc<KERR>(yp, st.pt, M, a, hb, k1, inc);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) yt[k] = yp[k] + inc[k];
+        const R rr = sqrt_(yt[0] * yt[0] + yt[1] * yt[1] + yt[2] * yt[2]);
+        if (it == 1 || rr == ra) break;
+        const R hn = hb + (rb - rr) * (hb - ha) / (rr - ra);
+        ha = hb; ra = rr; hb = hn;
+      }
+#pragma unroll
+      for (int k = 0; k < 6; ++k) { y[k] = yt[k]; st.lo[k] = 0.f; }
+      st.flags |= (rb == st.r_esc) ? ST_RAY_ESCAPED : ST_RAY_CAPTURED;
+      return true;
+    }
+  }
+  return false;
+}
+
+// Classification, sky and output (src/metal.jl:1629-1704, src/raytrace.jl:267-298).
+template <int PREC, int KERR, int SEM>
+__device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typename RealOf<PREC>::T>& st, int out_index,
+                                           int diag_index) {
+  using R = typename RealOf<PREC>::T;
+  const R M = R(p.M), a = R(p.a);
+  R yv[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) yv[k] = st.y[k];
+  const R rf = max_(sqrt_(yv[0] * yv[0] + yv[1] * yv[1] + yv[2] * yv[2]), R(1e-6));
+  R vel[6];
+  rhs<KERR>(yv, st.pt, M, a, vel);
+  const R vl = max_(sqrt_(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]), R(1e-20));
+  const R d0 = vel[0] / vl, d1 = vel[1] / vl, d2 = vel[2] / vl;
+  bool black;
+  if constexpr (SEM == ST_SEM_DRAFT) black = (st.flags & (ST_RAY_CAPTURED | ST_RAY_BCAPT)) || rf < R(4) * M;
+  else black = (st.flags & ST_RAY_CAPTURED) || rf < R(2.1) * M;
+  R rgb[3] = {st.acc[0], st.acc[1], st.acc[2]};
+  if (!black) {
+    const R th = acos_(clamp_(d2, R(-1), R(1)));
+    const R ph = atan2_(d1, d0);
+    R sky[3];
+    sample_sky(p, th, ph, sky);
+    const R g = st.scam;
+    if (g != R(1)) {
+      sky[0] *= R(57.4) / (exp_(R(4.067) / g) - R(1));
+      sky[1] *= R(90.2) / (exp_(R(4.513) / g) - R(1));
+      sky[2] *= R(206.5) / (exp_(R(5.335) / g) - R(1));
+    }
+    rgb[0] += st.alpha * sky[0];
+    rgb[1] += st.alpha * sky[1];
+    rgb[2] += st.alpha * sky[2];
+  } else {
+    st.flags |= ST_RAY_BLACK;
+  }
+  const float w = p.weight;
+  float4 o = make_float4(w * (float)rgb[0], w * (float)rgb[1], w * (float)rgb[2], (float)st.alpha);
+  if (!p.first_pass) {
+    const float4 prev = p.out[out_index];
+    o.x += prev.x; o.y += prev.y; o.z += prev.z;
+  }
+  p.out[out_index] = o;
+  if (p.diag) {
+    st_ray_diag d;
+    d.dir[0] = (float)d0; d.dir[1] = (float)d1; d.dir[2] = (float)d2;
+    d.flags = st.flags | (st.guard_ray ? ST_RAY_GUARDED : 0);
+    d.r_final = (float)rf;
+    d.alpha = (float)st.alpha;
+    d.r_cross = st.r_cross;
+    d.g_cross = st.g_cross;
+    d.steps = st.steps;
+    d.fp64_steps = st.fp64_steps;
+    d.lambda = (float)st.lambda;
+    d.pad = 0;
+    p.diag[diag_index] = d;
+  }
+}
+
+}  // namespace st
