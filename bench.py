@@ -1,0 +1,315 @@
+"""Benchmark of the render path: Mrays/s on the 1080p Kerr a=0.9 frame.
+
+Workload (one "step" = one full frame): Kerr a=0.9 M=1, static camera at KS
+r=15 M, inclination 80 deg, Lens(24), 1920x1080 float32 HDR, volumetric gas
+256x64x32 from the ISCO (2.32 M) to 25 M (scale height 0.05 r), 2048x1024
+synthetic sky, kernel (render_draft_mtl) rules, samples=1 at pixel centres,
+exit landing on r_escape.  All inputs are seeded synthetic data.
+
+    value     Mrays/s with inputs resident in HBM: CUDA-event time of the trace
+              launch on the library's stream, L2 flushed (256 MiB write)
+              between timed steps.
+    e2e       the same metric through st_render with a host output buffer
+              (device->host copy of the frame inside the timed region).
+    roofline  FP32 compute roof of the trace kernel (algorithmic flops per
+              step counted from the source, x accepted steps, / launch time).
+    cpu_baseline  the FP64 oracle (Tsit5, rtol 1e-10) on a bounded crop.
+
+`--impl reference` times the reference's CPU path as restated by the oracle
+(the reference itself is Julia + Metal and cannot run here).
+Multi-GPU: replicas only (each rank renders its own frames; no collective on
+the data path); value = rays of all ranks / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s 1080p Kerr a=0.9: surrogate+FP32 vs plain RK4, same GB300, ≤1e-4 rad"
+UNIT = "Mrays/s"
+
+# Algorithmic flops, counted from spacetime_gb300/csrc/st_trace.cuh (every
+# add, mul, div, sqrt, rsqrt, rcp, exp, log, atan2 counted as one).
+FLOPS_RHS_KERR = 126
+FLOPS_RHS_SCHW = 34
+FLOPS_RK4_UPDATE = 74
+FLOPS_GAS_SAMPLE = 150
+
+
+def flops_per_step(kerr: bool) -> int:
+    return 4 * (FLOPS_RHS_KERR if kerr else FLOPS_RHS_SCHW) + FLOPS_RK4_UPDATE
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int, path: str | None = None):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.path = path
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        if self.path:
+            with open(self.path, "w") as f:
+                f.write(self.FIELDS + "\n")
+                for r in self.rows:
+                    f.write(",".join(r) + "\n")
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        load = [s for s in sm if s > 0.5 * max(sm)] if sm else []
+        return {"sm_mhz": statistics.median(load) if load else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_baseline(seconds_target: float = 15.0, threads: int | None = None) -> dict:
+    """The FP64 oracle (Tsit5 rtol 1e-10, kernel rules) on a crop of the
+    workload, sized for ~10-30 s of host work."""
+    from oracle import oracle as O
+    from spacetime_gb300 import workloads
+    w = workloads.config1()
+    threads = threads or os.cpu_count() or 1
+    # probe a small crop, then size the measured crop
+    cw, ch = 48, 27
+    sc = O.scene_for(w, workloads.sky(), O.INT_TSIT5, rect=(936, cw, 526, ch))
+    t0 = time.perf_counter()
+    sc.render(nthreads=threads, records=False)
+    dt = time.perf_counter() - t0
+    rate = cw * ch / max(dt, 1e-6)
+    n = int(min(max(rate * seconds_target, 2000), 200000))
+    cw = int(min(1920, max(48, round(math.sqrt(n * 16 / 9)))))
+    ch = int(min(1080, max(27, round(cw * 9 / 16))))
+    c0, r0 = (1920 - cw) // 2, (1080 - ch) // 2
+    sc = O.scene_for(w, workloads.sky(), O.INT_TSIT5, rect=(c0, cw, r0, ch))
+    t0 = time.perf_counter()
+    sc.render(nthreads=threads, records=False)
+    dt = time.perf_counter() - t0
+    return {"value": cw * ch / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"central {cw}x{ch} crop of the 1920x1080 frame, FP64 Tsit5 rtol 1e-10, "
+                      f"{dt:.1f} s on {threads} threads"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    per_step = []
+    base = None
+    for k in range(args.warmup + args.steps):
+        b = cpu_baseline(seconds_target=args.ref_seconds, threads=threads)
+        if k >= args.warmup:
+            per_step.append(b["value"])
+            base = b
+    value = statistics.median(per_step)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "config1: Kerr a=0.9 r=15 i=80 1920x1080, gas 256x64x32, kernel rules",
+                   "sample": base["sample"]},
+        "cpu_baseline": {**base, "value": value},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp32g", choices=["fp64", "fp32", "fp32g"])
+    ap.add_argument("--schedule", default="pixel", choices=["pixel", "persistent"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--clocks-csv", default=None)
+    args = ap.parse_args(argv)
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from spacetime_gb300 import _abi, workloads
+    from spacetime_gb300.api import Context
+
+    w = workloads.config1()
+    prec = {"fp64": _abi.ST_PREC_FP64, "fp32": _abi.ST_PREC_FP32, "fp32g": _abi.ST_PREC_FP32_GUARDED}[args.precision]
+    sched = _abi.ST_SCHED_PERSISTENT if args.schedule == "persistent" else _abi.ST_SCHED_PIXEL
+    ctx = Context(workloads.sky(), disc=w.disc, volume=w.vol, emitter=w.emitter, device=local)
+    p = ctx.params(w.semantics, width=w.width, height=w.height, precision=prec, schedule=sched,
+                   r_guard=3.0, crit_band=0.05, renorm_every=64, **w.params)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        ctx.render_device(w.cam, w.bh, p)
+    barrier()
+    clocks = ClockSampler(local, args.clocks_csv)
+    clocks.start()
+    kernel_ms, stats_last = [], None
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        _, st = ctx.render_device(w.cam, w.bh, p)
+        kernel_ms.append(st["kernel_ms"])
+        stats_last = st
+    barrier()
+    wall = time.perf_counter() - t_wall0
+    # e2e: through st_render into pinned host memory
+    host = torch.empty((w.height, w.width, 3), dtype=torch.float32, pin_memory=True)
+    host_np = host.numpy()
+    e2e_ms = []
+    barrier()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = ctx.render_raw(w.cam, w.bh, p, out=host_np)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        e2e_stats = r.stats
+    barrier()
+    clk = clocks.stop()
+
+    rays = w.width * w.height
+    ms_step = float(np.mean(kernel_ms))
+    e2e_step = float(np.mean(e2e_ms))
+    if world > 1:
+        t = torch.tensor([ms_step, e2e_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step, e2e_step = float(t[0]), float(t[1])
+    value = world * rays / (ms_step * 1e-3) / 1e6
+    e2e_value = world * rays / (e2e_step * 1e-3) / 1e6
+
+    steps = stats_last["steps"]
+    gas = stats_last["gas_samples"]
+    flops = steps * flops_per_step(True) + gas * FLOPS_GAS_SAMPLE
+    achieved = flops / (ms_step * 1e-3) / 1e12
+    props = torch.cuda.get_device_properties(local)
+    sms = props.multi_processor_count
+    peaks = measured_peaks()
+    sm_max = peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = sms * 128 * 2 * sm_max * 1e6 / 1e12
+    if rank != 0:
+        return 0
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        try:
+            cpu = cpu_baseline()
+        except Exception as e:  # report, do not fail the bench
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if args.precision != "fp64" else "f64", "data": "synthetic",
+        "config": {
+            "workload": "config1: Kerr a=0.9 M=1, static camera r=15 M i=80 deg, Lens(24), 1920x1080, "
+                        "gas 256x64x32 ISCO-25M h=0.05r, sky 2048x1024, kernel rules, samples=1",
+            "precision": {"fp64": "FP64", "fp32": "FP32", "fp32g": "FP32 bulk + FP64 guards"}[args.precision],
+            "surrogate": False,
+            "schedule": args.schedule,
+            "parallelism": f"replicas{world}",
+            "l2": "flushed between timed steps (256 MiB write)",
+            "steps_per_frame": steps, "fp64_steps_per_frame": stats_last["fp64_steps"],
+            "gas_samples_per_frame": gas,
+            "geodesic_steps_per_s": steps / (ms_step * 1e-3),
+            "wall_s": wall,
+        },
+        "roofline": {
+            "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": achieved / fp32_peak, "traffic": None,
+            "peak_note": f"nominal FP32 FMA rate: {sms} SMs x 128 lanes x 2 x {sm_max:.0f} MHz "
+                         "(MEASURED_PEAKS.json has no FP32 figure)",
+            "flops_per_step": flops_per_step(True), "flops_per_gas_sample": FLOPS_GAS_SAMPLE,
+        },
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(e2e_stats["h2d_bytes"]),
+                "d2h_bytes_per_step": int(rays * 3 * 4), "ms_per_step": e2e_step},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -155,12 +155,12 @@ typedef struct {
 
 /* per-ray record (st_render_diag) */
 typedef struct {
-  float dir[3];              /* unit escape direction (coordinate velocity) */
-  int flags;                 /* ST_RAY_* */
+  double dir[3];             /* unit escape direction (coordinate velocity) */
   float r_final, alpha, r_cross, g_cross;
+  float lambda;              /* affine parameter travelled (RENDER) */
+  int flags;                 /* ST_RAY_* */
   int steps, fp64_steps;
-  float lambda;
-  int pad;
+  int pad[2];
 } st_ray_diag;
 
 enum {
@@ -178,7 +178,9 @@ void st_render_params_default(st_render_params* p, int semantics);
 
 /* Create a context on `device`; copies the (3, sky_w, sky_h) float sky to HBM. */
 int st_context_create(st_context** out, const float* sky_rgb, int sky_w, int sky_h, int device);
-/* NULL disables the thin disc. */
+/* NULL disables the thin disc (the gas keeps the last blackbody table; a new
+ * context starts with Blackbody() defaults: 6500 K white point, 500-30000 K,
+ * 1024 entries). */
 int st_context_set_disc(st_context* ctx, const st_disc* disc);
 /* NULL disables the volume; the density grid is copied to HBM. */
 int st_context_set_volume(st_context* ctx, const st_volume* vol);

@@ -262,3 +262,18 @@ class Scene:
         if rc != 0:
             raise RuntimeError(f"orc_render failed ({rc})")
         return out, rays
+
+
+def scene_for(w, sky, integrator, width=None, height=None, rect=None, **kw) -> Scene:
+    """Oracle scene of a benchmark workload (duck-typed: bh, cam, disc, vol,
+    semantics, emitter, params); semantics/emitter codes match the C ABI."""
+    disc = None
+    if w.disc is not None:
+        disc = dict(inner=w.disc.inner_radius, outer=w.disc.outer_radius, falloff=w.disc.density_falloff,
+                    wb=w.disc.blackbody.wb_temperature)
+    args = dict(cam=w.cam, M=w.bh.M, a=getattr(w.bh, "a", 0.0), sky=sky, width=width or w.width,
+                height=height or w.height, semantics=SEM_RENDER if w.semantics == 0 else SEM_DRAFT,
+                integrator=integrator, disc=disc, emitter=EMIT_KEPLER if w.emitter == 0 else EMIT_KS_EXACT,
+                volume=w.vol, exit_landing=w.params.get("exit_landing"), rect=rect, nmax=w.params.get("nmax", 0))
+    args.update(kw)
+    return Scene(**args)

@@ -536,9 +536,10 @@ bool march_gas(const Scene& S, const double* yp, const double* yn, double pt, do
   const double r2n = yn[0] * yn[0] + yn[1] * yn[1] + yn[2] * yn[2];
   if (!(*alpha > 0.003 && std::min(r2p, r2n) < S.vol_rb2)) return false;
   const double seg = h_used * vlen;
+  if (!(seg < 64.0)) return false;
   double t_s = S.ds_gas - *march_acc;
   if (t_s > seg) { *march_acc += seg; return false; }
-  while (t_s <= seg && *alpha > 0.003) {
+  for (int guard = 0; guard < 8192 && t_s <= seg && *alpha > 0.003; ++guard) {
     const double fs = t_s / seg;
     const double sx = yp[0] + fs * (yn[0] - yp[0]);
     const double sy = yp[1] + fs * (yn[1] - yp[1]);

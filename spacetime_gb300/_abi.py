@@ -90,17 +90,16 @@ class StStats(C.Structure):
 
 class StRayDiag(C.Structure):
     _fields_ = [
-        ("dir", C.c_float * 3), ("flags", C.c_int),
-        ("r_final", C.c_float), ("alpha", C.c_float), ("r_cross", C.c_float), ("g_cross", C.c_float),
-        ("steps", C.c_int), ("fp64_steps", C.c_int), ("lambda_", C.c_float), ("pad", C.c_int),
+        ("dir", C.c_double * 3), ("r_final", C.c_float), ("alpha", C.c_float), ("r_cross", C.c_float),
+        ("g_cross", C.c_float), ("lambda_", C.c_float), ("flags", C.c_int), ("steps", C.c_int),
+        ("fp64_steps", C.c_int), ("pad", C.c_int * 2),
     ]
 
 
 # numpy view of st_ray_diag records
 DIAG_DTYPE = [
-    ("dir", "<f4", (3,)), ("flags", "<i4"), ("r_final", "<f4"), ("alpha", "<f4"),
-    ("r_cross", "<f4"), ("g_cross", "<f4"), ("steps", "<i4"), ("fp64_steps", "<i4"),
-    ("lambda_", "<f4"), ("pad", "<i4"),
+    ("dir", "<f8", (3,)), ("r_final", "<f4"), ("alpha", "<f4"), ("r_cross", "<f4"), ("g_cross", "<f4"),
+    ("lambda_", "<f4"), ("flags", "<i4"), ("steps", "<i4"), ("fp64_steps", "<i4"), ("pad", "<i4", (2,)),
 ]
 
 # Every symbol include/spacetime_gb300.h declares.

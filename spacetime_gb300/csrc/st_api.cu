@@ -228,6 +228,7 @@ struct st_context {
   int sky_w = 0, sky_h = 0;
   float4* d_lut = nullptr;
   int lut_size = 0;
+  double lut_tmin = 500.0, lut_tmax = 30000.0;
   st_disc disc{};
   bool disc_on = false;
   float* d_vol = nullptr;
@@ -350,9 +351,9 @@ int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, 
   p->disc_falloff = ctx->disc.falloff;
   p->lut = ctx->d_lut;
   p->lut_size = ctx->lut_size;
-  p->lut_tmin = ctx->disc.table_min;
-  p->lut_tmax = ctx->disc.table_max;
-  if (p->disc_on && !ctx->d_lut) p->disc_on = 0;
+  p->lut_tmin = ctx->lut_tmin;
+  p->lut_tmax = ctx->lut_tmax;
+  if (!ctx->d_lut || ctx->lut_size < 1) return ST_ESTATE;
   // volume (DRAFT only), src/metal.jl:1147-1159
   p->vol_on = (rp->semantics == ST_SEM_DRAFT && ctx->vol_on) ? 1 : 0;
   if (p->vol_on) {
@@ -501,6 +502,31 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
 
 }  // namespace
 
+// Blackbody(wb_temperature, table_min, table_max, table_size), src/blackbody.jl:51-60,
+// uploaded as float4 entries.
+static int upload_lut(st_context* ctx, double wb, double tmin, double tmax, int n) {
+  if (!(tmax > tmin) || n < 2 || n > (1 << 20)) return ST_EINVAL;
+  double ref[3];
+  st::host_blackbody(wb > 0.0 ? wb : 6500.0, ref);
+  std::vector<float4> lut(n);
+  for (int i = 0; i < n; ++i) {
+    const double T = tmin + (tmax - tmin) * i / (n - 1);
+    double c[3];
+    st::host_blackbody(std::max(T, 1.0), c);
+    lut[i] = make_float4((float)(c[0] / ref[0]), (float)(c[1] / ref[1]), (float)(c[2] / ref[2]), 0.f);
+  }
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
+  if (ctx->d_lut && ctx->lut_size != n) { cudaFree(ctx->d_lut); ctx->d_lut = nullptr; ctx->lut_size = 0; }
+  if (!ctx->d_lut && cudaMalloc(&ctx->d_lut, n * sizeof(float4)) != cudaSuccess) return ST_ENOMEM;
+  if (cudaMemcpy(ctx->d_lut, lut.data(), n * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess)
+    return ST_ECUDA;
+  ctx->lut_size = n;
+  ctx->lut_tmin = tmin;
+  ctx->lut_tmax = tmax;
+  return ST_OK;
+}
+
+
 extern "C" {
 
 int st_abi_version(void) { return ST_ABI_VERSION; }
@@ -569,6 +595,10 @@ int st_context_create(st_context** out, const float* sky_rgb, int sky_w, int sky
     return fail(ST_ECUDA);
   c->sky_w = sky_w;
   c->sky_h = sky_h;
+  {
+    const int rc = upload_lut(c, 6500.0, 500.0, 30000.0, 1024);  // Blackbody() defaults
+    if (rc != ST_OK) return fail(rc);
+  }
   if (cudaMalloc(&c->d_counters, st::CNT_N * sizeof(unsigned long long)) != cudaSuccess) return fail(ST_ENOMEM);
   if (cudaMalloc(&c->d_queue, sizeof(unsigned int)) != cudaSuccess) return fail(ST_ENOMEM);
   *out = c;
@@ -581,24 +611,9 @@ int st_context_set_disc(st_context* ctx, const st_disc* d) {
   const int n = d->table_size > 0 ? d->table_size : 1024;
   const double tmin = d->table_size > 0 ? d->table_min : 500.0;
   const double tmax = d->table_size > 0 ? d->table_max : 30000.0;
-  if (!(tmax > tmin) || n < 2 || n > (1 << 20)) return ST_EINVAL;
   if (d->emitter != ST_EMIT_KEPLER && d->emitter != ST_EMIT_KS_EXACT) return ST_EINVAL;
-  // Blackbody(wb_temperature, table_min, table_max, table_size), src/blackbody.jl:51-60
-  double ref[3];
-  st::host_blackbody(d->wb_temperature > 0.0 ? d->wb_temperature : 6500.0, ref);
-  std::vector<float4> lut(n);
-  for (int i = 0; i < n; ++i) {
-    const double T = tmin + (tmax - tmin) * i / (n - 1);
-    double c[3];
-    st::host_blackbody(std::max(T, 1.0), c);
-    lut[i] = make_float4((float)(c[0] / ref[0]), (float)(c[1] / ref[1]), (float)(c[2] / ref[2]), 0.f);
-  }
-  if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
-  if (ctx->d_lut && ctx->lut_size != n) { cudaFree(ctx->d_lut); ctx->d_lut = nullptr; }
-  if (!ctx->d_lut && cudaMalloc(&ctx->d_lut, n * sizeof(float4)) != cudaSuccess) return ST_ENOMEM;
-  if (cudaMemcpy(ctx->d_lut, lut.data(), n * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess)
-    return ST_ECUDA;
-  ctx->lut_size = n;
+  const int rc = upload_lut(ctx, d->wb_temperature, tmin, tmax, n);
+  if (rc != ST_OK) return rc;
   ctx->disc = *d;
   ctx->disc.table_min = tmin;
   ctx->disc.table_max = tmax;

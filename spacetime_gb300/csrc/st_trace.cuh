@@ -579,12 +579,15 @@ __device__ __forceinline__ bool march_gas(const TraceParams& p, const R* yp, con
   if (!(st.alpha > R(0.003) && min_(r2p, r2n) < R(p.vol_rb2))) return false;
   const R ds = R(p.ds_gas);
   const R seg = h_used * vlen;
+  // a step spans at most a few M of arc; anything else (overflow, NaN) is not marched
+  if (!(seg < R(64))) return false;
   R t_s = ds - st.march_acc;
   if (t_s > seg) { st.march_acc += seg; return false; }
   const R zmax = R(p.zmax);
   const R r_isco = R(p.r_isco), M = R(p.M);
   const R inv_seg = R(1) / seg;
-  while (t_s <= seg && st.alpha > R(0.003)) {
+  // bounded: seg < 64 and ds >= dt, so at most 64/dt + 1 samples (capped at 8192)
+  for (int guard = 0; guard < 8192 && t_s <= seg && st.alpha > R(0.003); ++guard) {
     const R fs = IsD<R>::v ? t_s / seg : t_s * inv_seg;
     const R sx = yp[0] + fs * (yn[0] - yp[0]);
     const R sy = yp[1] + fs * (yn[1] - yp[1]);
@@ -786,7 +789,7 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
         // two secant iterations on the step size from the saved state
         const R re = st.r_esc;
         R ha = h, ra = rn;
-        R hb = h * (re - r) / (rn - r);
+        R hb = (rn > r) ? h * (re - r) / (rn - r) : h;
         R inc[6], yt[6];
 #pragma unroll 1
         for (int it = 0; it < 2; ++it) {
@@ -828,7 +831,7 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
     else if (rn >= st.r_esc) rb = st.r_esc;
     if (rb > R(0)) {
       R ha = h, ra = rn;
-      R hb = h * (rb - r) / (rn - r);
+      R hb = (rn != r) ? h * (rb - r) / (rn - r) : h;
       R inc[6], yt[6];
 #pragma unroll 1
       for (int it = 0; it < 2; ++it) {
@@ -893,7 +896,7 @@ __device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typena
   p.out[out_index] = o;
   if (p.diag) {
     st_ray_diag d;
-    d.dir[0] = (float)d0; d.dir[1] = (float)d1; d.dir[2] = (float)d2;
+    d.dir[0] = (double)d0; d.dir[1] = (double)d1; d.dir[2] = (double)d2;
     d.flags = st.flags | (st.guard_ray ? ST_RAY_GUARDED : 0);
     d.r_final = (float)rf;
     d.alpha = (float)st.alpha;
@@ -902,7 +905,7 @@ __device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typena
     d.steps = st.steps;
     d.fp64_steps = st.fp64_steps;
     d.lambda = (float)st.lambda;
-    d.pad = 0;
+    d.pad[0] = d.pad[1] = 0;
     p.diag[diag_index] = d;
   }
 }

@@ -1,0 +1,95 @@
+"""CUDA path vs the FP64 oracle on identical seeded inputs (through the C ABI).
+
+Tolerances:
+  FP64 vs the oracle's fixed-step twin (same step rule, same kill tests):
+    escape direction median <= 1e-9 rad, radiance rel. p99 <= 1e-5
+    (the two differ only in rounding: the GPU fuses multiply-adds);
+  FP64 vs the oracle's Tsit5 (rtol 1e-10): direction median <= 1e-8 rad;
+  FP32_GUARDED vs Tsit5: direction median <= 1e-4 rad, p99 <= 1e-3 rad,
+    radiance median <= 1e-3 (the target of the mixed-precision path).
+Rays whose classification differs (grazing the shadow edge / photon ring,
+chaotic under any rounding) are counted and bounded separately.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from spacetime_gb300 import _abi, workloads
+
+from .helpers import compare, gpu_render, oracle_scene
+
+pytestmark = pytest.mark.gpu
+
+FP64, FP32, FP32G = _abi.ST_PREC_FP64, _abi.ST_PREC_FP32, _abi.ST_PREC_FP32_GUARDED
+
+
+@pytest.fixture(scope="module")
+def sky():
+    return workloads.sky()
+
+
+def _check_twin(c, n, mismatch_frac=2e-3):
+    assert c["class_mismatch"] <= max(2, mismatch_frac * n), c
+    assert c["dir_median"] <= 1e-9, c
+    assert c["rad_p99"] <= 1e-5, c
+
+
+def test_config0_render_fp64_vs_twin_and_tsit5(built_lib, sky):
+    w = workloads.config0()
+    g = gpu_render(w, sky, FP64)
+    assert np.isfinite(g.image).all()
+    twin, twin_rays = oracle_scene(w, sky, O.INT_RK4).render()
+    c = compare(g.image, g.diag, twin, twin_rays)
+    _check_twin(c, c["n"])
+    ts, ts_rays = oracle_scene(w, sky, O.INT_TSIT5).render()
+    c2 = compare(g.image, g.diag, ts, ts_rays)
+    assert c2["dir_median"] <= 1e-8 and c2["rad_median"] <= 1e-6, c2
+    assert c2["class_mismatch"] <= 0.002 * c2["n"], c2
+
+
+def test_config0_draft_fp64_vs_twin(built_lib, sky):
+    w = workloads.config0()
+    w.semantics = _abi.ST_SEM_DRAFT
+    w.emitter = _abi.ST_EMIT_KS_EXACT
+    w.params = dict(samples=1, pixel_jitter=0, exit_landing=0)
+    g = gpu_render(w, sky, FP64)
+    ref, rays = oracle_scene(w, sky, O.INT_RK4).render()
+    _check_twin(compare(g.image, g.diag, ref, rays), w.width * w.height)
+
+
+def test_kerr_thin_disc_fp64_vs_twin(built_lib, sky):
+    w = workloads.config1_thin().scaled(240, 135)
+    w.params = dict(samples=1, pixel_jitter=0, exit_landing=0)
+    g = gpu_render(w, sky, FP64)
+    ref, rays = oracle_scene(w, sky, O.INT_RK4).render()
+    _check_twin(compare(g.image, g.diag, ref, rays), w.width * w.height)
+
+
+def test_kerr_volume_fp64_vs_twin(built_lib, sky):
+    w = workloads.config1().scaled(160, 90)
+    g = gpu_render(w, sky, FP64)
+    assert g.stats["gas_samples"] > 0
+    ref, rays = oracle_scene(w, sky, O.INT_RK4).render()
+    _check_twin(compare(g.image, g.diag, ref, rays), w.width * w.height)
+
+
+@pytest.mark.parametrize("prec", [FP32G, FP32])
+def test_kerr_volume_fp32_vs_tsit5(built_lib, sky, prec):
+    w = workloads.config1().scaled(192, 108)
+    g = gpu_render(w, sky, prec, r_guard=3.0, crit_band=0.05, renorm_every=64)
+    ref, rays = oracle_scene(w, sky, O.INT_TSIT5).render()
+    c = compare(g.image, g.diag, ref, rays)
+    print(_abi.ST_PREC_FP32_GUARDED == prec and "FP32G" or "FP32", c, g.stats)
+    if prec == FP32G:
+        assert c["dir_median"] <= 1e-4 and c["dir_p99"] <= 1e-3, c
+        assert c["rad_median"] <= 1e-3, c
+    assert c["class_mismatch"] <= 0.01 * c["n"], c
+
+
+def test_persistent_schedule_matches_pixel(built_lib, sky):
+    w = workloads.config1().scaled(200, 120)
+    a = gpu_render(w, sky, FP32G, schedule=_abi.ST_SCHED_PIXEL)
+    b = gpu_render(w, sky, FP32G, schedule=_abi.ST_SCHED_PERSISTENT, chunk_steps=16)
+    assert b.stats["status"] == _abi.ST_OK
+    assert a.stats["steps"] == b.stats["steps"]
+    np.testing.assert_array_equal(a.image, b.image)
