@@ -1,0 +1,152 @@
+# SpaceTimeGB300.jl -- Julia bindings of libspacetime_gb300.so (include/spacetime_gb300.h).
+#
+# Drop-in methods for SpaceTime.jl's GPU entry points:
+#   render(cam, bh, sky; disc, width, height, samples, relativistic)   (src/raytrace.jl:339)
+#   GB300Context(sky, w, h; disc, volume)                             (MetalPreviewContext, src/metal.jl:129)
+#   render_draft_mtl(ctx, cam, st; width, height, samples, dt, ...)   (src/metal.jl:2040)
+# Images come back as Matrix{RGBf}(width, height), the reference's layout.
+# This file is not exercised in this repository's CI (no Julia toolchain);
+# the same ABI is tested through Python ctypes (tests/test_abi.py and the GPU tests).
+module SpaceTimeGB300
+
+using SpaceTime
+using SpaceTime: AbstractCamera, Camera, Schwarzschild, Kerr, AccretionDisc, DiscVolume, spin
+using Colors: RGB
+using StaticArrays
+
+const RGBf = RGB{Float32}
+const libst = get(ENV, "SPACETIME_GB300_LIB", joinpath(@__DIR__, "..", "spacetime_gb300", "libspacetime_gb300.so"))
+
+const ST_OK = 0
+const ST_SEM_RENDER = 0
+const ST_SEM_DRAFT = 1
+const ST_EMIT_KEPLER = 0
+const ST_EMIT_KS_EXACT = 1
+const ST_PREC_FP64 = 0
+const ST_PREC_FP32_GUARDED = 1
+const ST_PREC_FP32 = 2
+
+struct StCamera
+    pos::NTuple{3,Float64}; fwd::NTuple{3,Float64}; right::NTuple{3,Float64}; up::NTuple{3,Float64}
+    fov_factor::Float64; velocity::NTuple{3,Float64}
+    projection::Cint; fisheye_deg::Float64; aperture_world::Float64; focus_dist::Float64
+end
+struct StSpacetime; M::Float64; a::Float64; end
+struct StDisc
+    inner::Float64; outer::Float64; falloff::Float64; wb_temperature::Float64
+    table_min::Float64; table_max::Float64; table_size::Cint; emitter::Cint
+end
+struct StVolume
+    density::Ptr{Float32}; nr::Cint; nphi::Cint; nz::Cint
+    log_s_in::Float32; log_s_out::Float32; z_max::Float32
+    emission_scale::Float32; opacity_scale::Float32; march_stride::Cint
+end
+mutable struct StRenderParams
+    width::Cint; height::Cint; samples::Cint; dt::Float64; nmax::Cint
+    semantics::Cint; precision::Cint; schedule::Cint
+    r_escape::Float64; tspan::Float64
+    relativistic::Cint; exit_landing::Cint; pixel_jitter::Cint; seed::UInt64
+    r_guard::Float64; crit_band::Float64; renorm_every::Cint
+    surrogate::Cint; surrogate_sigma::Float64
+    block_x::Cint; block_y::Cint; chunk_steps::Cint
+    StRenderParams() = new()
+end
+
+check(rc, where) = rc == ST_OK ||
+    error("$where: " * unsafe_string(ccall((:st_strerror, libst), Cstring, (Cint,), rc)))
+
+st_camera(cam::Camera; fisheye_deg=0.0, aperture_world=0.0, focus_dist=1.0) =
+    StCamera(Tuple(cam.pos), Tuple(cam.fwd), Tuple(cam.right), Tuple(cam.up_local), cam.fov_factor,
+             Tuple(cam.velocity), fisheye_deg > 0 ? 1 : 0, fisheye_deg, aperture_world, focus_dist)
+
+st_disc(d::AccretionDisc, emitter) =
+    StDisc(d.inner_radius, d.outer_radius, d.density_falloff, d.blackbody.wb_temperature,
+           d.blackbody.table_min, d.blackbody.table_max, d.blackbody.table_size, emitter)
+
+function sky_buffer(bg)
+    W, H = size(bg)
+    buf = Array{Float32,3}(undef, 3, W, H)   # the reference's (3, W, H) layout
+    for j in 1:H, i in 1:W
+        c = bg[i, j]
+        buf[1, i, j] = c.r; buf[2, i, j] = c.g; buf[3, i, j] = c.b
+    end
+    buf
+end
+
+"""GB300 counterpart of MetalPreviewContext: sky, blackbody table and gas on the device."""
+mutable struct GB300Context
+    handle::Ptr{Cvoid}
+    width::Int
+    height::Int
+    dt::Float64
+    vol::Union{Nothing,Array{Float32,3}}
+end
+
+function GB300Context(background, width::Int, height::Int; dt::Real=0.1, nmax::Int=1000,
+                      disc::Union{AccretionDisc,Nothing}=nothing,
+                      volume::Union{DiscVolume,Nothing}=nothing, device::Int=0,
+                      emitter::Int=ST_EMIT_KS_EXACT)
+    sky = sky_buffer(background)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:st_context_create, libst), Cint, (Ptr{Ptr{Cvoid}}, Ptr{Float32}, Cint, Cint, Cint),
+                h, sky, size(sky, 2), size(sky, 3), device), "st_context_create")
+    ctx = GB300Context(h[], width, height, dt, nothing)
+    finalizer(c -> ccall((:st_context_destroy, libst), Cvoid, (Ptr{Cvoid},), c.handle), ctx)
+    if disc !== nothing
+        d = Ref(st_disc(disc, emitter))
+        check(ccall((:st_context_set_disc, libst), Cint, (Ptr{Cvoid}, Ref{StDisc}), ctx.handle, d),
+              "st_context_set_disc")
+    end
+    if volume !== nothing
+        dens = volume.density
+        nr, nphi, nz = size(dens)
+        v = Ref(StVolume(pointer(dens), nr, nphi, nz, volume.log_s_in, volume.log_s_out, volume.z_max,
+                         volume.emission_scale, volume.opacity_scale, 2))
+        GC.@preserve dens check(ccall((:st_context_set_volume, libst), Cint, (Ptr{Cvoid}, Ref{StVolume}),
+                                      ctx.handle, v), "st_context_set_volume")
+    end
+    ctx
+end
+
+function default_params(semantics)
+    p = StRenderParams()
+    ccall((:st_render_params_default, libst), Cvoid, (Ref{StRenderParams}, Cint), p, semantics)
+    p
+end
+
+function st_render!(ctx::GB300Context, cam::StCamera, bh, p::StRenderParams)
+    out = Array{Float32,3}(undef, 3, p.width, p.height)
+    st = Ref(StSpacetime(bh.M, spin(bh)))
+    check(ccall((:st_render, libst), Cint,
+                (Ptr{Cvoid}, Ref{StCamera}, Ref{StSpacetime}, Ref{StRenderParams}, Ptr{Float32}, Ptr{Cvoid}),
+                ctx.handle, Ref(cam), st, p, out, C_NULL), "st_render")
+    img = Matrix{RGBf}(undef, p.width, p.height)
+    @inbounds for j in 1:p.height, i in 1:p.width
+        img[i, j] = RGBf(out[1, i, j], out[2, i, j], out[3, i, j])
+    end
+    img
+end
+
+"""`render(cam, bh, sky; disc, width, height, samples, relativistic)` on the GPU with the CPU
+renderer's rules (Keplerian disc, horizon at 2.00001, r_max = max(5|pos|, 100))."""
+function render_gb300(cam::Camera, bh::Schwarzschild, sky; disc=AccretionDisc(), width::Int=400,
+                      height::Int=200, samples::Int=1, relativistic::Bool=false, precision::Int=ST_PREC_FP64)
+    ctx = GB300Context(sky, width, height; disc=disc, emitter=ST_EMIT_KEPLER)
+    p = default_params(ST_SEM_RENDER)
+    p.width = width; p.height = height; p.samples = samples
+    p.relativistic = relativistic; p.precision = precision
+    st_render!(ctx, st_camera(cam), bh, p)
+end
+
+"""`render_draft_mtl(ctx, cam, st; ...)` on the GPU with the Metal kernel's rules."""
+function render_draft_gb300(ctx::GB300Context, cam::Camera, bh; width::Int=1920, height::Int=1080,
+                            samples::Int=2, dt::Real=0.02, fisheye_deg::Real=0.0, aperture_world::Real=0.0,
+                            focus_dist::Real=1.0, relativistic::Bool=false, precision::Int=ST_PREC_FP32,
+                            pixel_jitter::Bool=true)
+    p = default_params(ST_SEM_DRAFT)
+    p.width = width; p.height = height; p.samples = samples; p.dt = dt
+    p.relativistic = relativistic; p.precision = precision; p.pixel_jitter = pixel_jitter
+    st_render!(ctx, st_camera(cam; fisheye_deg, aperture_world, focus_dist), bh, p)
+end
+
+end # module

@@ -94,7 +94,12 @@ __global__ void __launch_bounds__(128) trace_persistent_kernel(const __grid_cons
         }
       }
     }
-    if (!__any_sync(FULL, active)) { done = true; break; }
+    // leave only when the queue is drained and no lane holds a ray (a refill
+    // that drew only off-frame slots loops back for more)
+    if (!__any_sync(FULL, active)) {
+      if (exhausted) { done = true; break; }
+      continue;
+    }
     if (active) {
       bool fin = false;
       for (int s = 0; s < p.chunk_steps && !fin; ++s) fin = step_ray<PREC, KERR, VOL, SEM>(p, st);
