@@ -185,6 +185,12 @@ def main(argv=None):
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp32g", choices=["fp64", "fp32", "fp32g"])
     ap.add_argument("--schedule", default="pixel", choices=["pixel", "persistent"])
+    ap.add_argument("--size", default="1920x1080", help="frame WxH (profiling uses a smaller case)")
+    ap.add_argument("--r-guard", type=float, default=3.0)
+    ap.add_argument("--crit-band", type=float, default=0.05)
+    ap.add_argument("--renorm", type=int, default=64)
+    ap.add_argument("--chunk", type=int, default=32)
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--clocks-csv", default=None)
@@ -205,11 +211,14 @@ def main(argv=None):
     from spacetime_gb300.api import Context
 
     w = workloads.config1()
+    W, H = (int(x) for x in args.size.lower().split("x"))
+    w = w.scaled(W, H)
     prec = {"fp64": _abi.ST_PREC_FP64, "fp32": _abi.ST_PREC_FP32, "fp32g": _abi.ST_PREC_FP32_GUARDED}[args.precision]
     sched = _abi.ST_SCHED_PERSISTENT if args.schedule == "persistent" else _abi.ST_SCHED_PIXEL
     ctx = Context(workloads.sky(), disc=w.disc, volume=w.vol, emitter=w.emitter, device=local)
     p = ctx.params(w.semantics, width=w.width, height=w.height, precision=prec, schedule=sched,
-                   r_guard=3.0, crit_band=0.05, renorm_every=64, **w.params)
+                   r_guard=args.r_guard, crit_band=args.crit_band, renorm_every=args.renorm,
+                   chunk_steps=args.chunk, **w.params)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def barrier():
@@ -236,8 +245,9 @@ def main(argv=None):
     host = torch.empty((w.height, w.width, 3), dtype=torch.float32, pin_memory=True)
     host_np = host.numpy()
     e2e_ms = []
+    e2e_stats = {"h2d_bytes": 0}
     barrier()
-    for _ in range(args.steps):
+    for _ in range(0 if args.no_e2e else args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -249,7 +259,7 @@ def main(argv=None):
 
     rays = w.width * w.height
     ms_step = float(np.mean(kernel_ms))
-    e2e_step = float(np.mean(e2e_ms))
+    e2e_step = float(np.mean(e2e_ms)) if e2e_ms else float("nan")
     if world > 1:
         t = torch.tensor([ms_step, e2e_step], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -279,9 +289,10 @@ def main(argv=None):
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if args.precision != "fp64" else "f64", "data": "synthetic",
         "config": {
-            "workload": "config1: Kerr a=0.9 M=1, static camera r=15 M i=80 deg, Lens(24), 1920x1080, "
+            "workload": f"config1: Kerr a=0.9 M=1, static camera r=15 M i=80 deg, Lens(24), {W}x{H}, "
                         "gas 256x64x32 ISCO-25M h=0.05r, sky 2048x1024, kernel rules, samples=1",
             "precision": {"fp64": "FP64", "fp32": "FP32", "fp32g": "FP32 bulk + FP64 guards"}[args.precision],
+            "guards": {"r_guard": args.r_guard, "crit_band": args.crit_band, "renorm_every": args.renorm},
             "surrogate": False,
             "schedule": args.schedule,
             "parallelism": f"replicas{world}",

@@ -17,7 +17,8 @@ __device__ __forceinline__ void flush_counters(const TraceParams& p, unsigned lo
     gas += __shfl_down_sync(0xffffffffu, gas, o);
     rays += __shfl_down_sync(0xffffffffu, rays, o);
   }
-  if ((threadIdx.x & 31) == 0 && p.counters) {
+  const unsigned lin = threadIdx.y * blockDim.x + threadIdx.x;  // lane = linear index mod 32
+  if ((lin & 31) == 0 && p.counters) {
     if (steps) atomicAdd(p.counters + CNT_STEPS, steps);
     if (f64) atomicAdd(p.counters + CNT_FP64, f64);
     if (gas) atomicAdd(p.counters + CNT_GAS, gas);
@@ -56,7 +57,7 @@ template <int PREC, int KERR, int VOL, int SEM>
 __global__ void __launch_bounds__(128) trace_persistent_kernel(const __grid_constant__ TraceParams p) {
   using R = typename RealOf<PREC>::T;
   const unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
+  const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
   const int tiles_x = (p.width + 7) >> 3;
   const int tiles_y = (p.height + 3) >> 2;
   const int per_frame = tiles_x * tiles_y * 32;
