@@ -131,9 +131,13 @@ typedef struct {
   int exit_landing;          /* land exactly on r_escape before reading the sky */
   int pixel_jitter;          /* per-pixel hashed jitter inside each stratum */
   unsigned long long seed;   /* pass shuffles and hash seeds */
-  double r_guard;            /* FP32_GUARDED: FP64 steps inside this KS radius */
-  double crit_band;          /* FP32_GUARDED: |b - b_crit| band (Schwarzschild) */
-  int renorm_every;          /* FP32_GUARDED: FP64 null renormalisation period */
+  double r_guard;            /* FP32_GUARDED: FP64 steps inside this KS radius
+                                (rays not already proven captured); 0 = off */
+  double crit_band;          /* FP32_GUARDED: critical-band rays get FP64 steps:
+                                |b - b_crit| < crit_band (Schwarzschild) or the
+                                Bardeen graze flag (Kerr); <= 0 = off */
+  double crit_r;             /* ...but only inside this KS radius; 0 = whole ray */
+  int renorm_every;          /* FP32_GUARDED: FP64 null renormalisation period; 0 = off */
   int surrogate;             /* 1 = gate + learned surrogate (st_surrogate_*) */
   double surrogate_sigma;    /* gate: max predicted std-dev (rad) served */
   int block_x, block_y;      /* ST_SCHED_PIXEL tile; 0 = tuned default */

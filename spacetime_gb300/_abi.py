@@ -10,7 +10,7 @@ import ctypes as C
 import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libspacetime_gb300.so")
+LIB_PATH = os.environ.get("SPACETIME_GB300_LIB", os.path.join(_HERE, "libspacetime_gb300.so"))
 
 ST_OK, ST_EINVAL, ST_ECUDA, ST_EBUDGET, ST_ENOMEM, ST_EUNSUPPORTED, ST_ESTATE = range(7)
 ST_PROJ_PINHOLE, ST_PROJ_FISHEYE = 0, 1
@@ -69,7 +69,7 @@ class StRenderParams(C.Structure):
         ("r_escape", C.c_double), ("tspan", C.c_double),
         ("relativistic", C.c_int), ("exit_landing", C.c_int), ("pixel_jitter", C.c_int),
         ("seed", C.c_ulonglong),
-        ("r_guard", C.c_double), ("crit_band", C.c_double), ("renorm_every", C.c_int),
+        ("r_guard", C.c_double), ("crit_band", C.c_double), ("crit_r", C.c_double), ("renorm_every", C.c_int),
         ("surrogate", C.c_int), ("surrogate_sigma", C.c_double),
         ("block_x", C.c_int), ("block_y", C.c_int), ("chunk_steps", C.c_int),
     ]

@@ -13,8 +13,17 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-OBJ = os.path.join(ROOT, "_build", "obj")
-LIB = os.path.join(HERE, "libspacetime_gb300.so")
+OBJ = os.environ.get("ST_OBJ_DIR", os.path.join(ROOT, "_build", "obj"))
+LIB = os.environ.get("SPACETIME_GB300_LIB", os.path.join(HERE, "libspacetime_gb300.so"))
+# per-unit flags: the FP32 trace units use the MUFU forms of sqrt, division,
+# exp and log (their double arithmetic is unaffected) and ask ptxas for enough
+# resident blocks per SM to keep FP32 latency hidden
+FAST = os.environ.get("ST_FASTMATH", "1") == "1"
+MINB_FP32 = os.environ.get("ST_MINB_FP32", "1")
+UNIT_FLAGS = {
+    "st_trace_fp32.cu": (["--use_fast_math"] if FAST else []) + [f"-DST_MINB={MINB_FP32}"],
+    "st_trace_fp32_guarded.cu": (["--use_fast_math"] if FAST else []) + [f"-DST_MINB={MINB_FP32}"],
+}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["st_trace_fp64.cu", "st_trace_fp32.cu", "st_trace_fp32_guarded.cu", "st_api.cu"]
 
@@ -45,13 +54,19 @@ def build(verbose: bool = False, force: bool = False) -> str:
     def one(src: str) -> str:
         s = os.path.join(CSRC, src)
         o = os.path.join(OBJ, src.replace(".cu", ".o"))
-        if not force and _newer(o, [s] + headers):
+        stamp = o + ".flags"
+        want = " ".join(flags + UNIT_FLAGS.get(src, []))
+        same = os.path.exists(stamp) and open(stamp).read() == want
+        if not force and same and _newer(o, [s] + headers):
             return o
-        r = subprocess.run([exe] + flags + ["-c", s, "-o", o], capture_output=True, text=True)
+        r = subprocess.run([exe] + flags + UNIT_FLAGS.get(src, []) + ["-c", s, "-o", o], capture_output=True,
+                           text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
         if verbose:
             print(r.stderr)
+        with open(stamp, "w") as f:
+            f.write(want)
         return o
 
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:

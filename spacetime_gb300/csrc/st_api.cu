@@ -341,6 +341,7 @@ int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, 
   const double rg = rp->r_guard > 0.0 ? rp->r_guard : 0.0;
   p->r_guard2 = rg * rg;
   p->crit_band = rp->crit_band;
+  p->crit_r2 = rp->crit_r > 0.0 ? rp->crit_r * rp->crit_r : 0.0;
   p->b_crit = 3.0 * std::sqrt(3.0) * M;
   p->renorm_every = rp->renorm_every;
   // disc
@@ -554,6 +555,7 @@ void st_render_params_default(st_render_params* p, int semantics) {
   p->seed = 0;
   p->r_guard = 3.0;
   p->crit_band = 0.05;
+  p->crit_r = 0.0;
   p->renorm_every = 64;
   p->surrogate_sigma = 1e-4;
   p->chunk_steps = 32;

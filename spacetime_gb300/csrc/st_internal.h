@@ -49,7 +49,7 @@ struct TraceParams {
   double r_isco, E_isco, L_isco;
   int relativistic, exit_landing;
   // FP32_GUARDED policy
-  double r_guard2, crit_band, b_crit;
+  double r_guard2, crit_band, b_crit, crit_r2;
   int renorm_every;
   // thin disc
   int disc_on, emitter;

@@ -4,6 +4,12 @@
 
 #include "st_trace.cuh"
 
+// Minimum resident blocks per SM requested from ptxas (register budget);
+// set per translation unit by the build.
+#ifndef ST_MINB
+#define ST_MINB 1
+#endif
+
 namespace st {
 
 __device__ __forceinline__ void flush_counters(const TraceParams& p, unsigned long long steps,
@@ -29,7 +35,7 @@ __device__ __forceinline__ void flush_counters(const TraceParams& p, unsigned lo
 // One thread per pixel over a 2-D grid of tiles (blockDim.x * blockDim.y a
 // multiple of 32; threads are linearised so a warp covers a compact tile).
 template <int PREC, int KERR, int VOL, int SEM>
-__global__ void __launch_bounds__(128) trace_pixel_kernel(const __grid_constant__ TraceParams p) {
+__global__ void __launch_bounds__(128, ST_MINB) trace_pixel_kernel(const __grid_constant__ TraceParams p) {
   using R = typename RealOf<PREC>::T;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -54,7 +60,7 @@ __global__ void __launch_bounds__(128) trace_pixel_kernel(const __grid_constant_
 // The outer loop is bounded by budget_iters; on exhaustion the kernel records
 // ST_EBUDGET in the status counter and returns.
 template <int PREC, int KERR, int VOL, int SEM>
-__global__ void __launch_bounds__(128) trace_persistent_kernel(const __grid_constant__ TraceParams p) {
+__global__ void __launch_bounds__(128, ST_MINB) trace_persistent_kernel(const __grid_constant__ TraceParams p) {
   using R = typename RealOf<PREC>::T;
   const unsigned FULL = 0xffffffffu;
   const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;

@@ -467,13 +467,13 @@ __device__ void init_ray(const TraceParams& p, const CamView& cam, int i0, int j
     bardeen(s, pt, D(p.M), D(p.a), &c0, &g0);
     if (c0) st.flags |= ST_RAY_BCAPT;
     if (g0) st.flags |= ST_RAY_GRAZE;
-    st.guard_ray = g0;
+    st.guard_ray = g0 && p.crit_band > 0.0;
   }
   if constexpr (!KERR && PREC == ST_PREC_FP32_GUARDED) {
     // critical impact-parameter band: b = |x cross p| / E, b_crit = 3 sqrt(3) M
     const D Lx = s[1] * s[5] - s[2] * s[4], Ly = s[2] * s[3] - s[0] * s[5], Lz = s[0] * s[4] - s[1] * s[3];
     const D b = sqrt_(Lx * Lx + Ly * Ly + Lz * Lz) / fabs_(pt);
-    st.guard_ray = fabs_(b - D(p.b_crit)) < D(p.crit_band);
+    st.guard_ray = p.crit_band > 0.0 && fabs_(b - D(p.b_crit)) < D(p.crit_band);
   }
   if constexpr (PREC == ST_PREC_FP32_GUARDED) {
 #pragma unroll
@@ -710,7 +710,8 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
 
   bool fp64_step = false;
   if constexpr (PREC == ST_PREC_FP32_GUARDED) {
-    fp64_step = st.guard_ray || (!(st.flags & ST_RAY_BCAPT) && rk2 < R(p.r_guard2));
+    fp64_step = (st.guard_ray && (p.crit_r2 <= 0.0 || rk2 < R(p.crit_r2))) ||
+                (!(st.flags & ST_RAY_BCAPT) && rk2 < R(p.r_guard2));
   }
   if (fp64_step) {
     if constexpr (PREC == ST_PREC_FP32_GUARDED) {
