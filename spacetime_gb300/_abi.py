@@ -107,6 +107,9 @@ EXPORTS = [
     "st_abi_version", "st_strerror", "st_render_params_default",
     "st_context_create", "st_context_set_disc", "st_context_set_volume", "st_context_destroy",
     "st_render", "st_render_diag", "st_render_device", "st_render_frames", "st_camera_tetrad",
+    "st_surrogate_create", "st_surrogate_destroy", "st_surrogate_num_params", "st_surrogate_get_params",
+    "st_surrogate_set_params", "st_surrogate_forward", "st_surrogate_loss_grad", "st_surrogate_generate",
+    "st_surrogate_train",
 ]
 
 _lib = None
@@ -149,8 +152,22 @@ def load(path: str | None = None) -> C.CDLL:
     lib.st_render_frames.argtypes = [C.c_void_p, C.c_int, P(StCamera), P(StSpacetime),
                                      P(StRenderParams), P(C.c_float), P(StStats)]
     lib.st_camera_tetrad.argtypes = [P(StCamera), P(StSpacetime), P(C.c_double)]
+    FP, LL = P(C.c_float), C.c_longlong
+    lib.st_surrogate_create.argtypes = [P(C.c_void_p), C.c_int, C.c_ulonglong]
+    lib.st_surrogate_destroy.argtypes = [C.c_void_p]
+    lib.st_surrogate_destroy.restype = None
+    lib.st_surrogate_num_params.argtypes = []
+    lib.st_surrogate_get_params.argtypes = [C.c_void_p, FP]
+    lib.st_surrogate_set_params.argtypes = [C.c_void_p, FP]
+    lib.st_surrogate_forward.argtypes = [C.c_void_p, FP, C.c_int, FP]
+    lib.st_surrogate_loss_grad.argtypes = [C.c_void_p, FP, FP, C.c_int, FP, FP]
+    lib.st_surrogate_generate.argtypes = [C.c_void_p, LL, LL, C.c_double, FP, FP, FP]
+    lib.st_surrogate_train.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, FP]
     for name in ("st_context_create", "st_context_set_disc", "st_context_set_volume", "st_render",
-                 "st_render_diag", "st_render_device", "st_render_frames", "st_camera_tetrad"):
+                 "st_render_diag", "st_render_device", "st_render_frames", "st_camera_tetrad",
+                 "st_surrogate_create", "st_surrogate_num_params", "st_surrogate_get_params",
+                 "st_surrogate_set_params", "st_surrogate_forward", "st_surrogate_loss_grad",
+                 "st_surrogate_generate", "st_surrogate_train"):
         getattr(lib, name).restype = C.c_int
     if path is None:
         _lib = lib

@@ -19,13 +19,14 @@ LIB = os.environ.get("SPACETIME_GB300_LIB", os.path.join(HERE, "libspacetime_gb3
 # exp and log (their double arithmetic is unaffected) and ask ptxas for enough
 # resident blocks per SM to keep FP32 latency hidden
 FAST = os.environ.get("ST_FASTMATH", "1") == "1"
-MINB_FP32 = os.environ.get("ST_MINB_FP32", "1")
+MINB_FP32 = os.environ.get("ST_MINB_FP32", "5")
+MINB_FP32G = os.environ.get("ST_MINB_FP32G", "4")
 UNIT_FLAGS = {
     "st_trace_fp32.cu": (["--use_fast_math"] if FAST else []) + [f"-DST_MINB={MINB_FP32}"],
-    "st_trace_fp32_guarded.cu": (["--use_fast_math"] if FAST else []) + [f"-DST_MINB={MINB_FP32}"],
+    "st_trace_fp32_guarded.cu": (["--use_fast_math"] if FAST else []) + [f"-DST_MINB={MINB_FP32G}"],
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["st_trace_fp64.cu", "st_trace_fp32.cu", "st_trace_fp32_guarded.cu", "st_api.cu"]
+SOURCES = ["st_trace_fp64.cu", "st_trace_fp32.cu", "st_trace_fp32_guarded.cu", "st_api.cu", "st_surrogate.cu"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,746 @@
+// st_surrogate.cu -- the learned exit-direction surrogate.
+//
+// MLP 6 -> 256 -> 256 -> 256 -> 256 -> 6 (SiLU), 200,710 parameters.
+//   inputs  : camera KS radius r in [4, 50] M, inclination theta in [0, 90] deg,
+//             spin a in [0, 0.99], unit ray direction n in the static observer's
+//             frame (radial, polar, azimuthal axes), normalised to O(1)
+//   outputs : exit-direction residual (3) over the ray's initial coordinate
+//             direction, first equatorial-crossing radius (scaled), redshift
+//             g - 1 there, and the log-variance of the direction error.
+// The three 256x256 layers run on the tensor cores in BF16 with FP32
+// accumulation (st_mlp.cuh); the 6->256 and 256->6 layers, the loss and AdamW
+// run in FP32.  Master weights and optimiser state are FP32.
+//
+// Training labels come from the FP64 integrator on the GPU (label_kernel):
+// Sobol-sampled inputs, the kernel's step rule and kill tests
+// (src/metal.jl:1201-1572) with the spin per sample, exit direction on the
+// escape radius 2 max(|pos|, 15M) (src/metal.jl:2058-2059).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "st_internal.h"
+#include "st_mlp.cuh"
+#include "st_trace.cuh"
+
+namespace st {
+namespace sur {
+
+using mlp::EpiAccum;
+using mlp::EpiBackDX;
+using mlp::EpiHidden;
+
+constexpr int NIN = 6, NH = 256, NOUT = 6, NT = 8;  // NT: target floats per row
+// parameter offsets (floats)
+constexpr size_t OW0 = 0, OB0 = OW0 + NH * NIN, OW1 = OB0 + NH, OB1 = OW1 + NH * NH, OW2 = OB1 + NH,
+                 OB2 = OW2 + NH * NH, OW3 = OB2 + NH, OB3 = OW3 + NH * NH, OW4 = OB3 + NH, OB4 = OW4 + NOUT * NH,
+                 NPARAM = OB4 + NOUT;
+static_assert(NPARAM == 200710, "parameter count");
+constexpr size_t OWH[3] = {OW1, OW2, OW3};
+constexpr size_t OBH[3] = {OB1, OB2, OB3};
+
+// ---------------------------------------------------------------------------
+// small FP32 layers, loss, reductions, AdamW
+// ---------------------------------------------------------------------------
+
+__global__ void l0_fwd(const float* __restrict__ X, const float* __restrict__ P, float* Z0, __nv_bfloat16* H0, int B) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= B * NH) return;
+  const int b = idx / NH, n = idx - b * NH;
+  float z = P[OB0 + n];
+#pragma unroll
+  for (int i = 0; i < NIN; ++i) z += X[b * NIN + i] * P[OW0 + n * NIN + i];
+  if (Z0) Z0[idx] = z;
+  H0[idx] = __float2bfloat16_rn(mlp::silu(z));
+}
+
+// one warp per row: out[b][j] = H3[b] . W4[j] + b4[j]
+__global__ void l4_fwd(const __nv_bfloat16* __restrict__ H3, const float* __restrict__ P, float* out, int B) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= B) return;
+  float acc[NOUT] = {0, 0, 0, 0, 0, 0};
+  for (int k = lane; k < NH; k += 32) {
+    const float h = __bfloat162float(H3[(size_t)warp * NH + k]);
+#pragma unroll
+    for (int j = 0; j < NOUT; ++j) acc[j] += h * P[OW4 + j * NH + k];
+  }
+#pragma unroll
+  for (int j = 0; j < NOUT; ++j) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+  }
+  if (lane < NOUT) {
+    float v = acc[0];
+#pragma unroll
+    for (int j = 1; j < NOUT; ++j) if (lane == j) v = acc[j];
+    out[(size_t)warp * NOUT + lane] = v + P[OB4 + lane];
+  }
+}
+
+// Loss per row (targets: t0..t2 direction residual, t3 crossing radius,
+// t4 g - 1, t5 direction mask, t6 crossing mask):
+//   0.5 |o - t|^2 exp(-s) + 1.5 s   (direction, heteroscedastic, s = o5)
+//   + WR (o3 - t3)^2 + WG m (o4 - t4)^2
+// loss_acc[0..3] += (total, direction MSE, radius MSE, g MSE) / B
+constexpr float WR = 1.0f, WG = 1.0f;
+__global__ void loss_grad(const float* __restrict__ out, const float* __restrict__ T, float* dout, float* loss_acc,
+                          int B, float inv_batch) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  float l_tot = 0.f, l_dir = 0.f, l_r = 0.f, l_g = 0.f;
+  if (b < B) {
+    const float* o = out + (size_t)b * NOUT;
+    const float* t = T + (size_t)b * NT;
+    const float md = t[5], mc = t[6];
+    const float s = fminf(fmaxf(o[5], -30.f), 12.f);
+    const float es = __expf(-s);
+    float e2 = 0.f, g[NOUT];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float e = o[k] - t[k];
+      e2 += e * e;
+      g[k] = md * e * es;
+    }
+    g[5] = (o[5] > -30.f && o[5] < 12.f) ? md * (-0.5f * e2 * es + 1.5f) : 0.f;
+    const float er = o[3] - t[3], eg = o[4] - t[4];
+    g[3] = 2.f * WR * er;
+    g[4] = 2.f * WG * mc * eg;
+#pragma unroll
+    for (int k = 0; k < NOUT; ++k) dout[(size_t)b * NOUT + k] = g[k] * inv_batch;
+    l_dir = md * e2;
+    l_r = er * er;
+    l_g = mc * eg * eg;
+    l_tot = md * (0.5f * e2 * es + 1.5f * s) + WR * l_r + WG * l_g;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    l_tot += __shfl_xor_sync(0xffffffffu, l_tot, o);
+    l_dir += __shfl_xor_sync(0xffffffffu, l_dir, o);
+    l_r += __shfl_xor_sync(0xffffffffu, l_r, o);
+    l_g += __shfl_xor_sync(0xffffffffu, l_g, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(loss_acc + 0, l_tot * inv_batch);
+    atomicAdd(loss_acc + 1, l_dir * inv_batch);
+    atomicAdd(loss_acc + 2, l_r * inv_batch);
+    atomicAdd(loss_acc + 3, l_g * inv_batch);
+  }
+}
+
+// dZ3 = silu'(Z3) * (dout . W4)
+__global__ void l4_bwd_dx(const float* __restrict__ dout, const float* __restrict__ P, const float* __restrict__ Z3,
+                          __nv_bfloat16* dZ3, int B) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= B * NH) return;
+  const int b = idx / NH, k = idx - b * NH;
+  float v = 0.f;
+#pragma unroll
+  for (int j = 0; j < NOUT; ++j) v += dout[(size_t)b * NOUT + j] * P[OW4 + j * NH + k];
+  dZ3[idx] = __float2bfloat16_rn(v * mlp::dsilu(Z3[idx]));
+}
+
+// dW4[j][k] += sum_b dout[b][j] H3[b][k], db4[j] += sum_b dout[b][j]; a block
+// of 256 threads (one per k) sweeps ROWS rows.
+constexpr int RED_ROWS = 256;
+__global__ void l4_bwd_w(const float* __restrict__ dout, const __nv_bfloat16* __restrict__ H3, float* G, int B) {
+  const int k = threadIdx.x;
+  const int b0 = blockIdx.x * RED_ROWS, b1 = min(B, b0 + RED_ROWS);
+  float acc[NOUT] = {0, 0, 0, 0, 0, 0}, db[NOUT] = {0, 0, 0, 0, 0, 0};
+  for (int b = b0; b < b1; ++b) {
+    const float h = __bfloat162float(H3[(size_t)b * NH + k]);
+#pragma unroll
+    for (int j = 0; j < NOUT; ++j) {
+      const float d = dout[(size_t)b * NOUT + j];
+      acc[j] += d * h;
+      if (k == 0) db[j] += d;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NOUT; ++j) {
+    atomicAdd(G + OW4 + j * NH + k, acc[j]);
+    if (k == 0) atomicAdd(G + OB4 + j, db[j]);
+  }
+}
+
+// column sums of a bf16 [B][256] matrix into G[off + n]
+__global__ void colsum_bf16(const __nv_bfloat16* __restrict__ D, float* G, size_t off, int B) {
+  const int n = threadIdx.x;
+  const int b0 = blockIdx.x * RED_ROWS, b1 = min(B, b0 + RED_ROWS);
+  float s = 0.f;
+  for (int b = b0; b < b1; ++b) s += __bfloat162float(D[(size_t)b * NH + n]);
+  atomicAdd(G + off + n, s);
+}
+
+// dW0[n][i] += sum_b dZ0[b][n] X[b][i], db0[n] += sum_b dZ0[b][n]
+__global__ void l0_bwd(const __nv_bfloat16* __restrict__ dZ0, const float* __restrict__ X, float* G, int B) {
+  const int n = threadIdx.x;
+  const int b0 = blockIdx.x * RED_ROWS, b1 = min(B, b0 + RED_ROWS);
+  float acc[NIN] = {0, 0, 0, 0, 0, 0}, db = 0.f;
+  for (int b = b0; b < b1; ++b) {
+    const float d = __bfloat162float(dZ0[(size_t)b * NH + n]);
+    db += d;
+#pragma unroll
+    for (int i = 0; i < NIN; ++i) acc[i] += d * X[b * NIN + i];
+  }
+#pragma unroll
+  for (int i = 0; i < NIN; ++i) atomicAdd(G + OW0 + n * NIN + i, acc[i]);
+  atomicAdd(G + OB0 + n, db);
+}
+
+__global__ void adamw(float* P, const float* G, float* Mm, float* Vv, size_t n, float lr, float b1, float b2,
+                      float eps, float wd, float bc1, float bc2) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float g = G[i];
+  const float m = b1 * Mm[i] + (1.f - b1) * g;
+  const float v = b2 * Vv[i] + (1.f - b2) * g * g;
+  Mm[i] = m;
+  Vv[i] = v;
+  // decoupled weight decay on the weight matrices only (biases are exempt)
+  const bool is_bias = (i >= OB0 && i < OW1) || (i >= OB1 && i < OW2) || (i >= OB2 && i < OW3) ||
+                       (i >= OB3 && i < OW4) || i >= OB4;
+  float p = P[i];
+  if (!is_bias) p -= lr * wd * p;
+  P[i] = p - lr * (m / bc1) / (sqrtf(v / bc2) + eps);
+}
+
+__global__ void to_bf16(const float* __restrict__ src, __nv_bfloat16* dst, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = __float2bfloat16_rn(src[i]);
+}
+
+// ---------------------------------------------------------------------------
+// Sobol points and FP64 labels
+// ---------------------------------------------------------------------------
+
+constexpr int SOBOL_DIMS = 5;
+__constant__ uint32_t c_sobol_v[SOBOL_DIMS][32];
+
+// Direction numbers from primitive polynomials (degree s, coefficient bits a,
+// initial m_k), Bratley-Fox recurrence; dimension 0 is van der Corput.
+static void sobol_directions(uint32_t v[SOBOL_DIMS][32]) {
+  struct Poly { int s, a; uint32_t m[4]; };
+  const Poly polys[SOBOL_DIMS - 1] = {{1, 0, {1}}, {2, 1, {1, 3}}, {3, 1, {1, 3, 1}}, {3, 2, {1, 1, 1}}};
+  for (int k = 0; k < 32; ++k) v[0][k] = 1u << (31 - k);
+  for (int d = 1; d < SOBOL_DIMS; ++d) {
+    const Poly& P = polys[d - 1];
+    uint32_t m[33];
+    for (int k = 1; k <= P.s; ++k) m[k] = P.m[k - 1];
+    for (int k = P.s + 1; k <= 32; ++k) {
+      uint32_t mk = m[k - P.s] ^ (m[k - P.s] << P.s);
+      for (int j = 1; j < P.s; ++j)
+        if ((P.a >> (P.s - 1 - j)) & 1) mk ^= m[k - j] << j;
+      m[k] = mk;
+    }
+    for (int k = 1; k <= 32; ++k) v[d][k - 1] = m[k] << (32 - k);
+  }
+}
+
+__device__ __forceinline__ float sobol(uint32_t i, int d) {
+  uint32_t x = 0;
+#pragma unroll 4
+  for (int k = 0; k < 32; ++k)
+    if ((i >> k) & 1u) x ^= c_sobol_v[d][k];
+  return (float)((x >> 8) + 0.5f) * (1.0f / 16777216.0f);
+}
+
+// Static observer's orthonormal frame in Kerr-Schild form at pos (valid
+// where f <= 0.72, i.e. r >= 4 M here); Gram-Schmidt of (e1, e2, e3) under g.
+template <typename D>
+__device__ void static_frame(const D* pos, const D* e1, const D* e2, const D* e3, D M, D a, D* U, D* E1, D* E2,
+                             D* E3) {
+  D l[3], f;
+  if (a != D(0)) {
+    const D rk2 = ks_r2(pos[0], pos[1], pos[2], a);
+    const D rk = sqrt_(max_(rk2, D(1e-12)));
+    const D ira = D(1) / (rk2 + a * a);
+    l[0] = (rk * pos[0] + a * pos[1]) * ira;
+    l[1] = (rk * pos[1] - a * pos[0]) * ira;
+    l[2] = pos[2] / rk;
+    f = D(2) * M * rk2 * rk / (rk2 * rk2 + a * a * pos[2] * pos[2]);
+  } else {
+    const D r = sqrt_(pos[0] * pos[0] + pos[1] * pos[1] + pos[2] * pos[2]);
+    l[0] = pos[0] / r; l[1] = pos[1] / r; l[2] = pos[2] / r;
+    f = D(2) * M / r;
+  }
+  auto gd = [&](const D* A, const D* B) {
+    const D la = A[0] + l[0] * A[1] + l[1] * A[2] + l[2] * A[3];
+    const D lb = B[0] + l[0] * B[1] + l[1] * B[2] + l[2] * B[3];
+    return -A[0] * B[0] + A[1] * B[1] + A[2] * B[2] + A[3] * B[3] + f * la * lb;
+  };
+  U[0] = D(1) / sqrt_(D(1) - f); U[1] = U[2] = U[3] = D(0);
+  D a1[4] = {D(0), e1[0], e1[1], e1[2]}, a2[4] = {D(0), e2[0], e2[1], e2[2]}, a3[4] = {D(0), e3[0], e3[1], e3[2]};
+  D c = gd(a1, U);
+  for (int k = 0; k < 4; ++k) a1[k] += c * U[k];
+  c = sqrt_(gd(a1, a1));
+  for (int k = 0; k < 4; ++k) E1[k] = a1[k] / c;
+  c = gd(a2, U);
+  for (int k = 0; k < 4; ++k) a2[k] += c * U[k];
+  c = gd(a2, E1);
+  for (int k = 0; k < 4; ++k) a2[k] -= c * E1[k];
+  c = sqrt_(gd(a2, a2));
+  for (int k = 0; k < 4; ++k) E2[k] = a2[k] / c;
+  c = gd(a3, U);
+  for (int k = 0; k < 4; ++k) a3[k] += c * U[k];
+  const D c1 = gd(a3, E1), c2 = gd(a3, E2);
+  for (int k = 0; k < 4; ++k) a3[k] -= c1 * E1[k] + c2 * E2[k];
+  c = sqrt_(gd(a3, a3));
+  for (int k = 0; k < 4; ++k) E3[k] = a3[k] / c;
+}
+
+// Frame axes of a camera at inclination theta (azimuth 0): radial, polar
+// (increasing theta) and azimuthal unit vectors of the Cartesian position.
+template <typename D>
+__device__ __forceinline__ void frame_axes(const D* pos, D* e1, D* e2, D* e3) {
+  const D rr = sqrt_(pos[0] * pos[0] + pos[1] * pos[1] + pos[2] * pos[2]);
+  const D ct = pos[2] / rr, st = sqrt_(max_(D(1) - ct * ct, D(0)));
+  e1[0] = pos[0] / rr; e1[1] = pos[1] / rr; e1[2] = ct;
+  e2[0] = ct; e2[1] = D(0); e2[2] = -st;
+  e3[0] = D(0); e3[1] = D(1); e3[2] = D(0);
+}
+
+struct LabelParams {
+  long long n;
+  long long offset;   // Sobol index of the first sample
+  float* X;           // [n][6] normalised inputs
+  float* T;           // [n][8] targets
+  float* raw;         // optional [n][12]: r, theta, a, n0, n1, n2, flags, steps, exit dir (3), r_cross
+  double dt;
+};
+
+__device__ __forceinline__ void normalise_inputs(float r, float th, float a, const float* n, float* x) {
+  x[0] = (r - 27.0f) / 23.0f;
+  x[1] = th / 0.78539816f - 1.0f;
+  x[2] = a / 0.495f - 1.0f;
+  x[3] = n[0];
+  x[4] = n[1];
+  x[5] = n[2];
+}
+
+// FP64 integration of one sample with the kernel's rules (no gas, no disc
+// shading): exit direction on r_escape (landed), first z = 0 crossing radius
+// and 1/(1+z) of the exact emitter there.
+__global__ void label_kernel(const LabelParams lp) {
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (tid >= lp.n) return;
+  const uint32_t idx = (uint32_t)(lp.offset + tid + 1);  // skip the origin point
+  const float u0 = sobol(idx, 0), u1 = sobol(idx, 1), u2 = sobol(idx, 2), u3 = sobol(idx, 3), u4 = sobol(idx, 4);
+  const double r = 4.0 + 46.0 * u0;
+  const double th = 1.5707963267948966 * u1;
+  const double a = 0.99 * u2;
+  const double nz = 2.0 * u3 - 1.0, ph = 6.283185307179586 * u4, sr = sqrt(fmax(1.0 - nz * nz, 0.0));
+  const double nv[3] = {sr * cos(ph), sr * sin(ph), nz};
+  const double M = 1.0;
+  const double pos[3] = {sqrt(r * r + a * a) * sin(th), 0.0, r * cos(th)};
+  double e1[3], e2[3], e3[3], U[4], E1[4], E2[4], E3[4];
+  frame_axes(pos, e1, e2, e3);
+  static_frame(pos, e1, e2, e3, M, a, U, E1, E2, E3);
+  double q[4];
+  for (int k = 0; k < 4; ++k) q[k] = nv[0] * E1[k] + nv[1] * E2[k] + nv[2] * E3[k] - U[k];
+  double y[6], pt;
+  if (a != 0.0) lower_photon<1>(pos, q, M, a, y, &pt);
+  else lower_photon<0>(pos, q, M, a, y, &pt);
+  bool cap0 = false, graze0 = false;
+  if (a != 0.0) bardeen(y, pt, M, a, &cap0, &graze0);
+  // initial coordinate direction (the residual's base)
+  double k1[6];
+  rhs_kerr(y, pt, M, a, k1);
+  const double v0n = sqrt(k1[0] * k1[0] + k1[1] * k1[1] + k1[2] * k1[2]);
+  const double d0[3] = {k1[0] / v0n, k1[1] / v0n, k1[2] / v0n};
+  // rules of the kernel (src/metal.jl:347-357, 1201-1260, 2058-2062)
+  const double rph = (a == 0.0) ? 3.0 * M : 2.0 * M * (1.0 + cos((2.0 / 3.0) * acos(-a / M)));
+  const float rkf = (float)(0.995 * rph);
+  const double rkill2 = (double)(rkf * rkf);
+  const double rpos = sqrt(pos[0] * pos[0] + pos[1] * pos[1] + pos[2] * pos[2]);
+  const double r_esc = (double)(float)(2.0 * fmax(rpos, 15.0 * M));
+  const int nmax = (int)fmin(fmax(1000.0, ceil((75.0 + 6.5 * log(r_esc / M)) * M / lp.dt)), 40000.0);
+  double r_isco, E_isco, L_isco;
+  {
+    auto cb = [](double x) { return exp(log(fmax(x, 1e-12)) / 3.0); };
+    const double qq = a / M;
+    const double z1 = 1.0 + cb(1.0 - qq * qq) * (cb(1.0 + qq) + cb(1.0 - qq));
+    const double z2 = sqrt(3.0 * qq * qq + z1 * z1);
+    r_isco = M * (3.0 + z2 - sqrt(fmax((3.0 - z1) * (3.0 + z1 + 2.0 * z2), 0.0)));
+    E_isco = sqrt(1.0 - 2.0 * M / (3.0 * r_isco));
+    L_isco = (2.0 * M / (3.0 * sqrt(3.0))) * (1.0 + 2.0 * sqrt(3.0 * r_isco / M - 2.0));
+  }
+  int flags = 0, steps = 0;
+  float r_cross = -1.f, g_cross = 0.f;
+  bool done = false;
+  for (; steps < nmax && !done; ++steps) {
+    const double r2 = y[0] * y[0] + y[1] * y[1] + y[2] * y[2];
+    const double rr = sqrt(r2);
+    const double rk2 = ks_r2(y[0], y[1], y[2], a);
+    if (rk2 < rkill2) { flags |= ST_RAY_CAPTURED; break; }
+    if (rr > r_esc) { flags |= ST_RAY_ESCAPED; break; }
+    double h = lp.dt * fmin(fmax(0.16 * rr / M, 1.0), 8.0);
+    const double fr = fmin(fmax((rk2 - rkill2) / fmax(rkill2, 1e-6), 0.0), 1.0);
+    h *= 0.12 + 0.88 * fr;
+    double yp[6], inc[6];
+    for (int k = 0; k < 6; ++k) yp[k] = y[k];
+    rhs_kerr(y, pt, M, a, k1);
+    rk4_inc<1>(y, pt, M, a, h, k1, inc);
+    for (int k = 0; k < 6; ++k) y[k] += inc[k];
+    if (!(y[0] == y[0]) || !(y[3] == y[3])) { flags |= ST_RAY_CAPTURED; break; }
+    if (r_cross < 0.f && yp[2] * y[2] < 0.0) {
+      const double cfz = yp[2] / (yp[2] - y[2]);
+      const double xh = yp[0] + cfz * (y[0] - yp[0]), yh = yp[1] + cfz * (y[1] - yp[1]);
+      const double pxh = yp[3] + cfz * (y[3] - yp[3]), pyh = yp[4] + cfz * (y[4] - yp[4]);
+      r_cross = (float)sqrt(xh * xh + yh * yh);
+      g_cross = (float)(1.0 / emitter_opz(xh, yh, pxh, pyh, -pt, M, a, r_isco, E_isco, L_isco));
+    }
+    const double rn = sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+    if (rn > r_esc) {
+      // land on r_escape (two secant iterations), as the render path does
+      double ha = h, ra = rn, hb = (rn > rr) ? h * (r_esc - rr) / (rn - rr) : h, yt[6];
+      for (int it = 0; it < 2; ++it) {
+        rk4_inc<1>(yp, pt, M, a, hb, k1, inc);
+        for (int k = 0; k < 6; ++k) yt[k] = yp[k] + inc[k];
+        const double rb = sqrt(yt[0] * yt[0] + yt[1] * yt[1] + yt[2] * yt[2]);
+        if (it == 1 || rb == ra) break;
+        const double hn = hb + (r_esc - rb) * (hb - ha) / (rb - ra);
+        ha = hb; ra = rb; hb = hn;
+      }
+      for (int k = 0; k < 6; ++k) y[k] = yt[k];
+      flags |= ST_RAY_ESCAPED;
+      done = true;
+    }
+  }
+  if (!(flags & (ST_RAY_ESCAPED | ST_RAY_CAPTURED))) flags |= ST_RAY_BUDGET;
+  if (cap0) flags |= ST_RAY_BCAPT;
+  if (graze0) flags |= ST_RAY_GRAZE;
+  double vel[6];
+  rhs_kerr(y, pt, M, a, vel);
+  const double vl = fmax(sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]), 1e-20);
+  const bool ok = (flags & ST_RAY_ESCAPED) && !cap0 && !(flags & ST_RAY_BUDGET);
+  float x[6];
+  const float nf[3] = {(float)nv[0], (float)nv[1], (float)nv[2]};
+  normalise_inputs((float)r, (float)th, (float)a, nf, x);
+  float* Xo = lp.X + tid * NIN;
+  for (int k = 0; k < NIN; ++k) Xo[k] = x[k];
+  float* To = lp.T + tid * NT;
+  for (int k = 0; k < 3; ++k) To[k] = ok ? (float)(vel[k] / vl - d0[k]) : 0.f;
+  To[3] = (r_cross > 0.f ? fminf(r_cross, 45.f) : 45.f) / 15.f - 1.f;
+  To[4] = r_cross > 0.f ? g_cross - 1.f : 0.f;
+  To[5] = ok ? 1.f : 0.f;
+  To[6] = r_cross > 0.f ? 1.f : 0.f;
+  To[7] = 0.f;
+  if (lp.raw) {
+    float* Ro = lp.raw + tid * 12;
+    Ro[0] = (float)r; Ro[1] = (float)th; Ro[2] = (float)a;
+    Ro[3] = nf[0]; Ro[4] = nf[1]; Ro[5] = nf[2];
+    Ro[6] = (float)flags; Ro[7] = (float)steps;
+    Ro[8] = (float)(vel[0] / vl); Ro[9] = (float)(vel[1] / vl); Ro[10] = (float)(vel[2] / vl);
+    Ro[11] = r_cross;
+  }
+}
+
+}  // namespace sur
+}  // namespace st
+
+// ---------------------------------------------------------------------------
+// Host object and C ABI
+// ---------------------------------------------------------------------------
+
+extern "C" void st_surrogate_destroy(st_surrogate* s);
+
+struct st_surrogate {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  float *P = nullptr, *G = nullptr, *Mm = nullptr, *Vv = nullptr;
+  __nv_bfloat16* Wb[3] = {nullptr, nullptr, nullptr};
+  int cap = 0;  // rows of the work buffers
+  float* X = nullptr;
+  float* Z[4] = {nullptr, nullptr, nullptr, nullptr};
+  __nv_bfloat16* H[4] = {nullptr, nullptr, nullptr, nullptr};
+  __nv_bfloat16 *dZa = nullptr, *dZb = nullptr;
+  float *out = nullptr, *dout = nullptr, *T = nullptr, *loss = nullptr;
+  // training set (device)
+  float *DX = nullptr, *DT = nullptr;
+  long long ndata = 0;
+  long long step = 0;
+  unsigned long long seed = 0;
+};
+
+namespace {
+
+using namespace st::sur;
+
+#define SC(call)                               \
+  do {                                         \
+    if ((call) != cudaSuccess) return ST_ECUDA; \
+  } while (0)
+
+int ensure_work(st_surrogate* s, int rows) {
+  if (rows <= s->cap) return ST_OK;
+  cudaFree(s->X);
+  for (int l = 0; l < 4; ++l) { cudaFree(s->Z[l]); cudaFree(s->H[l]); }
+  cudaFree(s->dZa); cudaFree(s->dZb); cudaFree(s->out); cudaFree(s->dout); cudaFree(s->T);
+  s->cap = 0;
+  const size_t R = rows;
+  if (cudaMalloc(&s->X, R * NIN * 4) != cudaSuccess) return ST_ENOMEM;
+  for (int l = 0; l < 4; ++l) {
+    if (cudaMalloc(&s->Z[l], R * NH * 4) != cudaSuccess) return ST_ENOMEM;
+    if (cudaMalloc(&s->H[l], R * NH * 2) != cudaSuccess) return ST_ENOMEM;
+  }
+  if (cudaMalloc(&s->dZa, R * NH * 2) != cudaSuccess || cudaMalloc(&s->dZb, R * NH * 2) != cudaSuccess)
+    return ST_ENOMEM;
+  if (cudaMalloc(&s->out, R * NOUT * 4) != cudaSuccess || cudaMalloc(&s->dout, R * NOUT * 4) != cudaSuccess ||
+      cudaMalloc(&s->T, R * NT * 4) != cudaSuccess)
+    return ST_ENOMEM;
+  s->cap = rows;
+  return ST_OK;
+}
+
+int sync_bf16(st_surrogate* s) {
+  for (int l = 0; l < 3; ++l) {
+    to_bf16<<<(NH * NH + 255) / 256, 256, 0, s->stream>>>(s->P + OWH[l], s->Wb[l], NH * NH);
+    SC(cudaGetLastError());
+  }
+  return ST_OK;
+}
+
+// forward of B rows (B multiple of 128) from s->X-like input pointer
+int forward(st_surrogate* s, const float* X, int B, bool keep_z) {
+  cudaStream_t st = s->stream;
+  l0_fwd<<<(B * NH + 255) / 256, 256, 0, st>>>(X, s->P, keep_z ? s->Z[0] : nullptr, s->H[0], B);
+  SC(cudaGetLastError());
+  for (int l = 1; l <= 3; ++l) {
+    EpiHidden e{s->P + OBH[l - 1], keep_z ? s->Z[l] : nullptr, s->H[l], NH};
+    st::mlp::gemm_bf16_kernel<true, true, EpiHidden>
+        <<<dim3(NH / st::mlp::TN, B / st::mlp::TM, 1), st::mlp::GEMM_THREADS, 0, st>>>(s->H[l - 1], NH, s->Wb[l - 1],
+                                                                                      NH, NH, e);
+    SC(cudaGetLastError());
+  }
+  l4_fwd<<<(B * 32 + 255) / 256, 256, 0, st>>>(s->H[3], s->P, s->out, B);
+  SC(cudaGetLastError());
+  return ST_OK;
+}
+
+// backward from s->dout (already scaled by 1/B); accumulates into s->G
+int backward(st_surrogate* s, const float* X, int B) {
+  cudaStream_t st = s->stream;
+  SC(cudaMemsetAsync(s->G, 0, NPARAM * 4, st));
+  l4_bwd_dx<<<(B * NH + 255) / 256, 256, 0, st>>>(s->dout, s->P, s->Z[3], s->dZa, B);
+  SC(cudaGetLastError());
+  const int nred = (B + RED_ROWS - 1) / RED_ROWS;
+  l4_bwd_w<<<nred, NH, 0, st>>>(s->dout, s->H[3], s->G, B);
+  SC(cudaGetLastError());
+  __nv_bfloat16* dZ = s->dZa;
+  __nv_bfloat16* dZn = s->dZb;
+  const int splits = std::max(1, std::min(64, B / 1024));
+  for (int l = 3; l >= 1; --l) {
+    // dW_l = dZ_l^T H_{l-1}
+    EpiAccum ea{s->G + OWH[l - 1], NH};
+    st::mlp::gemm_bf16_kernel<false, false, EpiAccum>
+        <<<dim3(NH / st::mlp::TN, NH / st::mlp::TM, splits), st::mlp::GEMM_THREADS, 0, st>>>(dZ, NH, s->H[l - 1], NH,
+                                                                                              B, ea);
+    SC(cudaGetLastError());
+    colsum_bf16<<<nred, NH, 0, st>>>(dZ, s->G, OBH[l - 1], B);
+    SC(cudaGetLastError());
+    // dZ_{l-1} = (dZ_l W_l) * silu'(Z_{l-1})
+    EpiBackDX eb{s->Z[l - 1], dZn, NH};
+    st::mlp::gemm_bf16_kernel<true, false, EpiBackDX>
+        <<<dim3(NH / st::mlp::TN, B / st::mlp::TM, 1), st::mlp::GEMM_THREADS, 0, st>>>(dZ, NH, s->Wb[l - 1], NH, NH,
+                                                                                      eb);
+    SC(cudaGetLastError());
+    std::swap(dZ, dZn);
+  }
+  l0_bwd<<<nred, NH, 0, st>>>(dZ, X, s->G, B);
+  SC(cudaGetLastError());
+  return ST_OK;
+}
+
+int pad128(long long n) { return (int)((n + 127) / 128 * 128); }
+
+}  // namespace
+
+extern "C" {
+
+int st_surrogate_create(st_surrogate** out, int device, unsigned long long seed) {
+  if (!out) return ST_EINVAL;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return ST_ECUDA;
+  if (device < 0 || device >= ndev) return ST_EINVAL;
+  st_surrogate* s = new (std::nothrow) st_surrogate();
+  if (!s) return ST_ENOMEM;
+  s->device = device;
+  s->seed = seed;
+  auto fail = [&](int c) { st_surrogate_destroy(s); return c; };
+  if (cudaSetDevice(device) != cudaSuccess) return fail(ST_ECUDA);
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(ST_ECUDA);
+  if (cudaMalloc(&s->P, NPARAM * 4) != cudaSuccess || cudaMalloc(&s->G, NPARAM * 4) != cudaSuccess ||
+      cudaMalloc(&s->Mm, NPARAM * 4) != cudaSuccess || cudaMalloc(&s->Vv, NPARAM * 4) != cudaSuccess ||
+      cudaMalloc(&s->loss, 16 * 4) != cudaSuccess)
+    return fail(ST_ENOMEM);
+  for (int l = 0; l < 3; ++l)
+    if (cudaMalloc(&s->Wb[l], NH * NH * 2) != cudaSuccess) return fail(ST_ENOMEM);
+  // He-style uniform initialisation from a splitmix64 stream (host)
+  std::vector<float> P(NPARAM, 0.f);
+  uint64_t z = seed * 0x9e3779b97f4a7c15ull + 12345;
+  auto rnd = [&]() {
+    z += 0x9e3779b97f4a7c15ull;
+    uint64_t x = z;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return (double)(x >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+  };
+  auto fill = [&](size_t off, int fan_out, int fan_in, double gain) {
+    const double lim = gain * std::sqrt(3.0 / fan_in);
+    for (int i = 0; i < fan_out * fan_in; ++i) P[off + i] = (float)(lim * rnd());
+  };
+  fill(OW0, NH, NIN, 1.6);
+  fill(OW1, NH, NH, 1.6);
+  fill(OW2, NH, NH, 1.6);
+  fill(OW3, NH, NH, 1.6);
+  fill(OW4, NOUT, NH, 0.1);
+  P[OB4 + 5] = -6.0f;  // start the log-variance small
+  if (cudaMemcpy(s->P, P.data(), NPARAM * 4, cudaMemcpyHostToDevice) != cudaSuccess) return fail(ST_ECUDA);
+  if (cudaMemset(s->Mm, 0, NPARAM * 4) != cudaSuccess || cudaMemset(s->Vv, 0, NPARAM * 4) != cudaSuccess)
+    return fail(ST_ECUDA);
+  uint32_t v[SOBOL_DIMS][32];
+  sobol_directions(v);
+  if (cudaMemcpyToSymbol(c_sobol_v, v, sizeof v) != cudaSuccess) return fail(ST_ECUDA);
+  if (sync_bf16(s) != ST_OK || cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(ST_ECUDA);
+  *out = s;
+  return ST_OK;
+}
+
+void st_surrogate_destroy(st_surrogate* s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  cudaFree(s->P); cudaFree(s->G); cudaFree(s->Mm); cudaFree(s->Vv); cudaFree(s->loss);
+  for (int l = 0; l < 3; ++l) cudaFree(s->Wb[l]);
+  cudaFree(s->X);
+  for (int l = 0; l < 4; ++l) { cudaFree(s->Z[l]); cudaFree(s->H[l]); }
+  cudaFree(s->dZa); cudaFree(s->dZb); cudaFree(s->out); cudaFree(s->dout); cudaFree(s->T);
+  cudaFree(s->DX); cudaFree(s->DT);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+int st_surrogate_num_params(void) { return (int)NPARAM; }
+
+int st_surrogate_get_params(st_surrogate* s, float* host) {
+  if (!s || !host) return ST_EINVAL;
+  if (cudaSetDevice(s->device) != cudaSuccess) return ST_ECUDA;
+  SC(cudaMemcpy(host, s->P, NPARAM * 4, cudaMemcpyDeviceToHost));
+  return ST_OK;
+}
+
+int st_surrogate_set_params(st_surrogate* s, const float* host) {
+  if (!s || !host) return ST_EINVAL;
+  if (cudaSetDevice(s->device) != cudaSuccess) return ST_ECUDA;
+  SC(cudaMemcpy(s->P, host, NPARAM * 4, cudaMemcpyHostToDevice));
+  if (sync_bf16(s) != ST_OK) return ST_ECUDA;
+  SC(cudaStreamSynchronize(s->stream));
+  return ST_OK;
+}
+
+int st_surrogate_forward(st_surrogate* s, const float* X, int n, float* out) {
+  if (!s || !X || !out || n <= 0) return ST_EINVAL;
+  if (cudaSetDevice(s->device) != cudaSuccess) return ST_ECUDA;
+  const int B = pad128(n);
+  int rc = ensure_work(s, B);
+  if (rc != ST_OK) return rc;
+  SC(cudaMemsetAsync(s->X, 0, (size_t)B * NIN * 4, s->stream));
+  SC(cudaMemcpyAsync(s->X, X, (size_t)n * NIN * 4, cudaMemcpyHostToDevice, s->stream));
+  if ((rc = forward(s, s->X, B, false)) != ST_OK) return rc;
+  SC(cudaMemcpyAsync(out, s->out, (size_t)n * NOUT * 4, cudaMemcpyDeviceToHost, s->stream));
+  SC(cudaStreamSynchronize(s->stream));
+  return ST_OK;
+}
+
+// Loss and parameter gradient on n rows (rows beyond n are masked padding).
+int st_surrogate_loss_grad(st_surrogate* s, const float* X, const float* T, int n, float* loss4, float* grad) {
+  if (!s || !X || !T || n <= 0) return ST_EINVAL;
+  if (cudaSetDevice(s->device) != cudaSuccess) return ST_ECUDA;
+  const int B = pad128(n);
+  int rc = ensure_work(s, B);
+  if (rc != ST_OK) return rc;
+  cudaStream_t st = s->stream;
+  SC(cudaMemsetAsync(s->X, 0, (size_t)B * NIN * 4, st));
+  SC(cudaMemsetAsync(s->T, 0, (size_t)B * NT * 4, st));
+  SC(cudaMemcpyAsync(s->X, X, (size_t)n * NIN * 4, cudaMemcpyHostToDevice, st));
+  SC(cudaMemcpyAsync(s->T, T, (size_t)n * NT * 4, cudaMemcpyHostToDevice, st));
+  if ((rc = forward(s, s->X, B, true)) != ST_OK) return rc;
+  SC(cudaMemsetAsync(s->loss, 0, 16 * 4, st));
+  loss_grad<<<(B + 255) / 256, 256, 0, st>>>(s->out, s->T, s->dout, s->loss, n, 1.0f / n);
+  SC(cudaGetLastError());
+  // padding rows carry no gradient
+  if (B > n) SC(cudaMemsetAsync(s->dout + (size_t)n * NOUT, 0, (size_t)(B - n) * NOUT * 4, st));
+  if ((rc = backward(s, s->X, B)) != ST_OK) return rc;
+  if (loss4) SC(cudaMemcpyAsync(loss4, s->loss, 4 * 4, cudaMemcpyDeviceToHost, st));
+  if (grad) SC(cudaMemcpyAsync(grad, s->G, NPARAM * 4, cudaMemcpyDeviceToHost, st));
+  SC(cudaStreamSynchronize(st));
+  return ST_OK;
+}
+
+// Generate n labelled samples (Sobol indices offset..offset+n-1) on the
+// device and keep them as the training set; optionally copy to the host.
+int st_surrogate_generate(st_surrogate* s, long long n, long long offset, double dt, float* host_x, float* host_t,
+                          float* host_raw) {
+  if (!s || n <= 0 || !(dt > 0.0)) return ST_EINVAL;
+  if (cudaSetDevice(s->device) != cudaSuccess) return ST_ECUDA;
+  cudaFree(s->DX);
+  cudaFree(s->DT);
+  s->DX = s->DT = nullptr;
+  s->ndata = 0;
+  if (cudaMalloc(&s->DX, (size_t)n * NIN * 4) != cudaSuccess || cudaMalloc(&s->DT, (size_t)n * NT * 4) != cudaSuccess)
+    return ST_ENOMEM;
+  float* raw = nullptr;
+  if (host_raw && cudaMalloc(&raw, (size_t)n * 12 * 4) != cudaSuccess) return ST_ENOMEM;
+  LabelParams lp{n, offset, s->DX, s->DT, raw, dt};
+  label_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s->stream>>>(lp);
+  SC(cudaGetLastError());
+  if (host_x) SC(cudaMemcpyAsync(host_x, s->DX, (size_t)n * NIN * 4, cudaMemcpyDeviceToHost, s->stream));
+  if (host_t) SC(cudaMemcpyAsync(host_t, s->DT, (size_t)n * NT * 4, cudaMemcpyDeviceToHost, s->stream));
+  if (raw) SC(cudaMemcpyAsync(host_raw, raw, (size_t)n * 12 * 4, cudaMemcpyDeviceToHost, s->stream));
+  SC(cudaStreamSynchronize(s->stream));
+  cudaFree(raw);
+  s->ndata = n;
+  return ST_OK;
+}
+
+// `steps` AdamW steps on batches drawn (cyclically, in order of a per-epoch
+// stride) from the generated set; loss_hist[k] gets each step's loss.
+int st_surrogate_train(st_surrogate* s, int steps, int batch, float lr, float weight_decay, float* loss_hist) {
+  if (!s || steps <= 0 || batch < 128 || batch % 128 != 0) return ST_EINVAL;
+  if (s->ndata < batch) return ST_ESTATE;
+  if (cudaSetDevice(s->device) != cudaSuccess) return ST_ECUDA;
+  int rc = ensure_work(s, batch);
+  if (rc != ST_OK) return rc;
+  cudaStream_t st = s->stream;
+  const long long nb = s->ndata / batch;
+  std::vector<float> lh(steps > 0 ? steps : 1);
+  for (int k = 0; k < steps; ++k) {
+    const long long bi = (s->step * 7919LL) % nb;  // stride through the batches
+    const float* X = s->DX + bi * batch * NIN;
+    const float* T = s->DT + bi * batch * NT;
+    if ((rc = forward(s, X, batch, true)) != ST_OK) return rc;
+    SC(cudaMemsetAsync(s->loss, 0, 16 * 4, st));
+    loss_grad<<<(batch + 255) / 256, 256, 0, st>>>(s->out, T, s->dout, s->loss, batch, 1.0f / batch);
+    SC(cudaGetLastError());
+    if ((rc = backward(s, X, batch)) != ST_OK) return rc;
+    ++s->step;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float bc1 = 1.f - std::pow(b1, (float)s->step), bc2 = 1.f - std::pow(b2, (float)s->step);
+    adamw<<<(unsigned)((NPARAM + 255) / 256), 256, 0, st>>>(s->P, s->G, s->Mm, s->Vv, NPARAM, lr, b1, b2, 1e-8f,
+                                                           weight_decay, bc1, bc2);
+    SC(cudaGetLastError());
+    if ((rc = sync_bf16(s)) != ST_OK) return rc;
+    if (loss_hist) SC(cudaMemcpyAsync(&lh[k], s->loss, 4, cudaMemcpyDeviceToHost, st));
+  }
+  SC(cudaStreamSynchronize(st));
+  if (loss_hist) std::memcpy(loss_hist, lh.data(), steps * sizeof(float));
+  return ST_OK;
+}
+
+}  // extern "C"

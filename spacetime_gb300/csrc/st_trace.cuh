@@ -652,6 +652,38 @@ __device__ __forceinline__ void null_renorm(double* y, double pt, double M, doub
   if (lam > 0.9 && lam < 1.1) { y[3] *= lam; y[4] *= lam; y[5] *= lam; }
 }
 
+// FP64 guard step on the float-float state.
+template <int KERR>
+__device__ __forceinline__ void guard_step_fp64(float* y, float* lo, float pt, double M, double a, float h) {
+  double yd[6], k1d[6], inc[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) yd[k] = (double)y[k] + (double)lo[k];
+  const double ptd = (double)pt;
+  rhs<KERR>(yd, ptd, M, a, k1d);
+  rk4_inc<KERR>(yd, ptd, M, a, (double)h, k1d, inc);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const double v = yd[k] + inc[k];
+    const float hi = (float)v;
+    y[k] = hi;
+    lo[k] = (float)(v - (double)hi);
+  }
+}
+
+template <int KERR>
+__device__ __forceinline__ void renorm_fp64(float* y, float* lo, float pt, double M, double a) {
+  double yd[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) yd[k] = (double)y[k] + (double)lo[k];
+  null_renorm<KERR>(yd, (double)pt, M, a);
+#pragma unroll
+  for (int k = 3; k < 6; ++k) {
+    const float hi = (float)yd[k];
+    y[k] = hi;
+    lo[k] = (float)(yd[k] - (double)hi);
+  }
+}
+
 // One integration step for the variant; returns true when the ray is done.
 // Mirrors the step loop of src/metal.jl:1201-1572 (DRAFT) and the callback
 // structure of src/raytrace.jl:339-373 (RENDER).
@@ -715,19 +747,7 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
   }
   if (fp64_step) {
     if constexpr (PREC == ST_PREC_FP32_GUARDED) {
-      double yd[6], k1d[6], inc[6];
-#pragma unroll
-      for (int k = 0; k < 6; ++k) yd[k] = (double)y[k] + (double)st.lo[k];
-      const double ptd = (double)st.pt;
-      rhs<KERR>(yd, ptd, p.M, p.a, k1d);
-      rk4_inc<KERR>(yd, ptd, p.M, p.a, (double)h, k1d, inc);
-#pragma unroll
-      for (int k = 0; k < 6; ++k) {
-        const double v = yd[k] + inc[k];
-        const float hi = (float)v;
-        y[k] = hi;
-        st.lo[k] = (float)(v - (double)hi);
-      }
+      guard_step_fp64<KERR>(y, st.lo, st.pt, p.M, p.a, h);
       ++st.fp64_steps;
     }
   } else {
@@ -743,18 +763,7 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
   }
   ++st.steps;
   if constexpr (PREC == ST_PREC_FP32_GUARDED) {
-    if (p.renorm_every > 0 && (st.steps % p.renorm_every) == 0) {
-      double yd[6];
-#pragma unroll
-      for (int k = 0; k < 6; ++k) yd[k] = (double)y[k] + (double)st.lo[k];
-      null_renorm<KERR>(yd, (double)st.pt, p.M, p.a);
-#pragma unroll
-      for (int k = 3; k < 6; ++k) {
-        const float hi = (float)yd[k];
-        y[k] = hi;
-        st.lo[k] = (float)(yd[k] - (double)hi);
-      }
-    }
+    if (p.renorm_every > 0 && (st.steps % p.renorm_every) == 0) renorm_fp64<KERR>(y, st.lo, st.pt, p.M, p.a);
   }
   if (!(y[0] == y[0]) || !(y[2] == y[2]) || !(y[3] == y[3])) { st.flags |= ST_RAY_CAPTURED; return true; }
 

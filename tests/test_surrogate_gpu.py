@@ -1,0 +1,126 @@
+"""The learned surrogate on the GPU: BF16 tensor-core forward/backward against
+the FP64 numpy MLP (oracle/mlp_oracle.py), FP64 GPU labels against the FP64
+oracle integrator, and training that reduces the loss.
+
+Tolerances: BF16 hidden activations and weights (8-bit mantissa) bound the
+agreement with the FP64 reference at ~1e-2 relative; gradients are compared
+per parameter tensor by relative L2 error <= 5e-2 and cosine >= 0.995.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as MO
+from oracle import oracle as O
+from spacetime_gb300 import scene
+from spacetime_gb300.surrogate import Surrogate
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sur(built_lib):
+    s = Surrogate(0, seed=3)
+    yield s
+    s.close()
+
+
+def _random_batch(n, rng):
+    X = rng.uniform(-1, 1, (n, 6)).astype(np.float32)
+    T = np.zeros((n, 8), np.float32)
+    T[:, :3] = rng.normal(0, 0.3, (n, 3))
+    T[:, 3] = rng.uniform(-1, 2, n)
+    T[:, 4] = rng.normal(0, 0.2, n)
+    T[:, 5] = (rng.random(n) < 0.9)
+    T[:, 6] = (rng.random(n) < 0.5)
+    return X, T
+
+
+def test_param_roundtrip_and_count(sur):
+    P = sur.get_params()
+    assert P.size == MO.NPARAM == 200710
+    sur.set_params(P)
+    assert np.array_equal(sur.get_params(), P)
+
+
+def test_forward_matches_fp64(sur):
+    rng = np.random.default_rng(1)
+    X, _ = _random_batch(300, rng)     # not a multiple of 128: exercises padding
+    P = sur.get_params()
+    out = sur.forward(X)
+    ref, _, _ = MO.forward(P, X)
+    err = np.abs(out - ref).max() / np.abs(ref).max()
+    assert err < 2e-2, err
+
+
+def test_gradients_match_fp64(sur):
+    rng = np.random.default_rng(2)
+    X, T = _random_batch(512, rng)
+    P = sur.get_params()
+    loss, g = sur.loss_grad(X, T)
+    rloss, rg = MO.loss_grad(P, X, T)
+    assert abs(loss[0] - rloss[0]) <= 2e-2 * abs(rloss[0]) + 1e-6
+    o = 0
+    for name, shape in MO.SIZES:
+        n = int(np.prod(shape))
+        a, b = g[o:o + n].astype(np.float64), rg[o:o + n]
+        o += n
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        cos = a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30)
+        assert rel <= 5e-2 and cos >= 0.995, (name, rel, cos)
+
+
+def _oracle_exit(r, th, a, nvec):
+    """Exit direction of one label ray from the oracle's fixed-step FP64 twin
+    (kernel rules), posed as a 1x1 fisheye camera with a 180 deg edge angle."""
+    pos = np.array([math.sqrt(r * r + a * a) * math.sin(th), 0.0, r * math.cos(th)])
+    rr = np.linalg.norm(pos)
+    ct = pos[2] / rr
+    st = math.sqrt(max(1 - ct * ct, 0.0))
+    e1 = pos / rr
+    e2 = np.array([ct, 0.0, -st])
+    e3 = np.array([0.0, 1.0, 0.0])
+    cam = scene.Camera(pos, e1, e2, e3, 1.0, np.zeros(3), projection=1, fisheye_deg=180.0)
+    thp = math.acos(max(-1.0, min(1.0, nvec[0])))
+    rho = thp / math.pi
+    s = math.hypot(nvec[1], nvec[2])
+    uu, vv = (rho * nvec[1] / s, rho * nvec[2] / s) if s > 0 else (0.0, 0.0)
+    sky = np.ones((4, 8, 3), np.float32)
+    sc = O.Scene(cam=cam, M=1.0, a=a, sky=sky, width=1, height=1, semantics=O.SEM_DRAFT, integrator=O.INT_RK4,
+                 exit_landing=1, ju=(uu + 1) / 2, jv=(vv + 1) / 2)
+    _, rays = sc.render(nthreads=1)
+    return rays[0, 0]
+
+
+def test_labels_match_oracle_integrator(sur):
+    """FP64 GPU labels against the oracle's FP64 fixed-step twin on the same
+    initial rays (absolute exit directions, stored in float32)."""
+    x, t, raw = sur.generate(4096, offset=0)
+    assert np.isfinite(x).all() and np.isfinite(t).all()
+    ok = t[:, 5] > 0
+    assert ok.mean() > 0.5
+    rng = np.random.default_rng(5)
+    idx = rng.choice(np.nonzero(ok)[0], 60, replace=False)
+    errs = []
+    for i in idx:
+        r, th, a = float(raw[i, 0]), float(raw[i, 1]), float(raw[i, 2])
+        n = raw[i, 3:6].astype(np.float64)
+        n /= np.linalg.norm(n)
+        rec = _oracle_exit(r, th, a, n)
+        assert rec["flags"] & O.RAY_ESCAPED
+        d = raw[i, 8:11].astype(np.float64)
+        errs.append(2 * math.asin(min(1.0, np.linalg.norm(d - rec["dir"]) / 2)))
+    errs = np.array(errs)
+    # float32 inputs/outputs of the label rows bound the agreement at ~1e-6 rad,
+    # more for the few rays that wind near the photon shell
+    assert np.median(errs) < 1e-5, np.sort(errs)[-5:]
+    assert (errs < 1e-3).mean() > 0.95
+
+
+def test_training_reduces_loss(sur):
+    sur.generate(1 << 16, offset=1 << 20)
+    hist = sur.train(300, batch=4096, lr=2e-3, weight_decay=1e-5)
+    assert np.isfinite(hist).all()
+    first, last = hist[:10].mean(), hist[-10:].mean()
+    assert last < first - 1.0, (first, last)
