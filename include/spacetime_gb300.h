@@ -56,7 +56,9 @@ enum {
   ST_EBUDGET = 3,       /* the persistent queue hit its iteration budget */
   ST_ENOMEM = 4,        /* device or host allocation failed */
   ST_EUNSUPPORTED = 5,  /* combination not provided (e.g. Kerr with ST_SEM_RENDER) */
-  ST_ESTATE = 6         /* context not ready (e.g. surrogate requested, none loaded) */
+  ST_ESTATE = 6,        /* context not ready (e.g. surrogate requested, none loaded) */
+  ST_ELIMIT = 7         /* request exceeds the fixed scratch capacity of
+                           st_render_frames_noalloc */
 };
 
 enum { ST_PROJ_PINHOLE = 0, ST_PROJ_FISHEYE = 1 };
@@ -236,6 +238,29 @@ int st_surrogate_generate(st_surrogate* s, long long n, long long sobol_offset, 
                           float* host_t, float* host_raw);
 /* AdamW steps over the generated set; loss_hist[steps] optional */
 int st_surrogate_train(st_surrogate* s, int steps, int batch, float lr, float weight_decay, float* loss_hist);
+
+/* Allocation-free camera-track render.  No counterpart in the reference.
+ * For callers that cannot allocate device memory: a renderer embedded in an
+ * engine whose device memory belongs to its own pool, a plug-in invoked
+ * inside a CUDA graph capture or stream-ordered region where cudaMalloc would
+ * break the capture or synchronise the device, a real-time loop that budgets
+ * memory up front.  The caller passes its own device buffers: the sky as
+ * float4 texels [sky_h][sky_w] (RGB + unused), the gas density (may be NULL
+ * with vol NULL) and the output frames, float4 [nframes][height][width]; the
+ * kernel's working memory (ray-queue head, counters, per-frame cameras and the
+ * blackbody table) lives in a fixed 80 KiB device array of the library, held on
+ * every device that loads it until exit.  Limits: nframes <= 64, blackbody
+ * table <= 4096 entries (ST_ELIMIT beyond); DRAFT semantics, samples = 1.
+ * The first call on a device resolves the array's address with that device
+ * current: make that first call before any stream capture.  All calls share
+ * the array (queue head and counters are cleared per call): calls whose GPU
+ * work overlaps race and must be serialised by the caller.  `stream` is a
+ * cudaStream_t (NULL = legacy default stream); the call returns after it
+ * completes.  It calls no cudaMalloc, cudaFree or allocating library routine. */
+int st_render_frames_noalloc(const float* dev_sky_rgba, int sky_w, int sky_h, const st_disc* disc,
+                             const float* dev_density, const st_volume* vol, int nframes,
+                             const st_camera* cams, const st_spacetime* st, const st_render_params* p,
+                             float* dev_out_rgba, void* stream, st_stats* stats);
 
 /* The camera's orthonormal Kerr-Schild tetrad (u, Ef, Er, Eu), each a
  * contravariant (t, x, y, z) 4-vector, boosted by the camera velocity. */

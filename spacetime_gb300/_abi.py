@@ -12,7 +12,7 @@ import os
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("SPACETIME_GB300_LIB", os.path.join(_HERE, "libspacetime_gb300.so"))
 
-ST_OK, ST_EINVAL, ST_ECUDA, ST_EBUDGET, ST_ENOMEM, ST_EUNSUPPORTED, ST_ESTATE = range(7)
+ST_OK, ST_EINVAL, ST_ECUDA, ST_EBUDGET, ST_ENOMEM, ST_EUNSUPPORTED, ST_ESTATE, ST_ELIMIT = range(8)
 ST_PROJ_PINHOLE, ST_PROJ_FISHEYE = 0, 1
 ST_EMIT_KEPLER, ST_EMIT_KS_EXACT = 0, 1
 ST_SEM_RENDER, ST_SEM_DRAFT = 0, 1
@@ -109,7 +109,7 @@ EXPORTS = [
     "st_render", "st_render_diag", "st_render_device", "st_render_frames", "st_camera_tetrad",
     "st_surrogate_create", "st_surrogate_destroy", "st_surrogate_num_params", "st_surrogate_get_params",
     "st_surrogate_set_params", "st_surrogate_forward", "st_surrogate_loss_grad", "st_surrogate_generate",
-    "st_surrogate_train",
+    "st_surrogate_train", "st_render_frames_noalloc",
 ]
 
 _lib = None
@@ -163,6 +163,10 @@ def load(path: str | None = None) -> C.CDLL:
     lib.st_surrogate_loss_grad.argtypes = [C.c_void_p, FP, FP, C.c_int, FP, FP]
     lib.st_surrogate_generate.argtypes = [C.c_void_p, LL, LL, C.c_double, FP, FP, FP]
     lib.st_surrogate_train.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, FP]
+    lib.st_render_frames_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, P(StDisc), C.c_void_p, P(StVolume),
+                                             C.c_int, P(StCamera), P(StSpacetime), P(StRenderParams), C.c_void_p,
+                                             C.c_void_p, P(StStats)]
+    lib.st_render_frames_noalloc.restype = C.c_int
     for name in ("st_context_create", "st_context_set_disc", "st_context_set_volume", "st_render",
                  "st_render_diag", "st_render_device", "st_render_frames", "st_camera_tetrad",
                  "st_surrogate_create", "st_surrogate_num_params", "st_surrogate_get_params",

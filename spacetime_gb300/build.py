@@ -26,7 +26,7 @@ UNIT_FLAGS = {
     "st_trace_fp32_guarded.cu": (["--use_fast_math"] if FAST else []) + [f"-DST_MINB={MINB_FP32G}"],
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["st_trace_fp64.cu", "st_trace_fp32.cu", "st_trace_fp32_guarded.cu", "st_api.cu", "st_surrogate.cu"]
+SOURCES = ["st_trace_fp64.cu", "st_trace_fp32.cu", "st_trace_fp32_guarded.cu", "st_api.cu", "st_surrogate.cu", "st_noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -541,6 +541,7 @@ const char* st_strerror(int code) {
     case ST_ENOMEM: return "out of memory";
     case ST_EUNSUPPORTED: return "unsupported combination";
     case ST_ESTATE: return "context not ready for this request";
+    case ST_ELIMIT: return "request exceeds the fixed scratch capacity of the allocation-free entry point";
     default: return "unknown status";
   }
 }
@@ -766,3 +767,56 @@ int st_camera_tetrad(const st_camera* cam, const st_spacetime* stp, double out16
 }
 
 }  // extern "C"
+
+// Camera- and rule-dependent part of a trace launch for one camera, without a
+// context (used by the allocation-free entry point in st_noalloc.cu).
+namespace st {
+int fill_frame_params(const st_camera* cam, const st_spacetime* stp, const st_render_params* rp, TraceParams* p) {
+  if (!cam || !stp || !rp || !p) return ST_EINVAL;
+  const double M = stp->M, a = stp->a;
+  if (!(M > 0.0) || !(std::fabs(a) <= M)) return ST_EINVAL;
+  if (rp->width <= 0 || rp->height <= 0 || !(rp->dt > 0.0)) return ST_EINVAL;
+  if (rp->precision < ST_PREC_FP64 || rp->precision > ST_PREC_FP32) return ST_EINVAL;
+  const double rpos = norm3(cam->pos);
+  if (!(rpos > 0.0) || !std::isfinite(rpos)) return ST_EINVAL;
+  std::memset(p, 0, sizeof(*p));
+  const double beta[3] = {dot3(cam->velocity, cam->fwd), dot3(cam->velocity, cam->right),
+                          dot3(cam->velocity, cam->up)};
+  host_tetrad(cam->pos, cam->fwd, cam->right, cam->up, M, a, beta, p->U, p->Ef, p->Er, p->Eu);
+  for (int k = 0; k < 3; ++k) p->pos[k] = cam->pos[k];
+  p->fov = cam->fov_factor;
+  p->projection = cam->projection;
+  p->fisheye_rad = std::max(cam->fisheye_deg, 0.0) * 3.141592653589793 / 180.0;
+  p->focus = cam->focus_dist > 0.0 ? cam->focus_dist : 1.0;
+  p->width = rp->width;
+  p->height = rp->height;
+  p->frame_stride = rp->width * rp->height;
+  p->M = M;
+  p->a = a;
+  const float rk = (float)(0.995 * host_photon_orbit_min(M, a));
+  p->rkill2 = (double)(rk * rk);
+  host_isco(M, a, &p->r_isco, &p->E_isco, &p->L_isco);
+  p->dt = rp->dt;
+  p->hcoef = 0.16;
+  p->hcap = 8.0;
+  p->relativistic = rp->relativistic ? 1 : 0;
+  const double re = rp->r_escape > 0.0 ? rp->r_escape : (double)(float)(2.0 * std::max(rpos, 15.0 * M));
+  p->r_escape = re;
+  if (rp->nmax > 0) {
+    p->nmax = rp->nmax;
+  } else {
+    const double lg = (double)std::log((float)((float)re / (float)M));
+    const double n = std::ceil((75.0 + 6.5 * lg) * (double)(float)M / (double)(float)rp->dt);
+    p->nmax = (int)std::min(std::max(1000.0, n), 40000.0);
+  }
+  p->exit_landing = rp->exit_landing ? 1 : 0;
+  const double rg = rp->r_guard > 0.0 ? rp->r_guard : 0.0;
+  p->r_guard2 = rg * rg;
+  p->crit_band = rp->crit_band;
+  p->crit_r2 = rp->crit_r > 0.0 ? rp->crit_r * rp->crit_r : 0.0;
+  p->b_crit = 3.0 * std::sqrt(3.0) * M;
+  p->renorm_every = rp->renorm_every;
+  p->chunk_steps = rp->chunk_steps > 0 ? rp->chunk_steps : 32;
+  return ST_OK;
+}
+}  // namespace st

@@ -38,7 +38,7 @@ def test_abi_version_and_strerror(built_lib):
     lib = _abi.load()
     ver = int(re.search(r"#define ST_ABI_VERSION (\d+)", open(HEADER).read()).group(1))
     assert lib.st_abi_version() == ver
-    for code in range(7):
+    for code in range(8):
         assert lib.st_strerror(code)
     assert lib.st_strerror(99) == b"unknown status"
 
