@@ -124,14 +124,16 @@ def dist_env():
     return rank, world, local
 
 
-def cpu_baseline(seconds_target: float = 15.0, threads: int | None = None) -> dict:
-    """The FP64 oracle (Tsit5 rtol 1e-10, kernel rules) on a crop of the
-    workload, sized for ~10-30 s of host work."""
+def cpu_baseline(seconds_target: float = 15.0, threads: int | None = None, gpu_frame=None,
+                 gpu_diag=None) -> dict:
+    """The FP64 oracle (Tsit5 rtol 1e-10, kernel rules) on a central crop of
+    the workload, sized for ~10-30 s of host work.  When the GPU frame and its
+    per-ray records are given, the same crop also yields the GPU path's
+    exit-direction and radiance error against the oracle."""
     from oracle import oracle as O
     from spacetime_gb300 import workloads
     w = workloads.config1()
     threads = threads or os.cpu_count() or 1
-    # probe a small crop, then size the measured crop
     cw, ch = 48, 27
     sc = O.scene_for(w, workloads.sky(), O.INT_TSIT5, rect=(936, cw, 526, ch))
     t0 = time.perf_counter()
@@ -144,11 +146,26 @@ def cpu_baseline(seconds_target: float = 15.0, threads: int | None = None) -> di
     c0, r0 = (1920 - cw) // 2, (1080 - ch) // 2
     sc = O.scene_for(w, workloads.sky(), O.INT_TSIT5, rect=(c0, cw, r0, ch))
     t0 = time.perf_counter()
-    sc.render(nthreads=threads, records=False)
+    ref, rays = sc.render(nthreads=threads, records=gpu_frame is not None)
     dt = time.perf_counter() - t0
-    return {"value": cw * ch / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"central {cw}x{ch} crop of the 1920x1080 frame, FP64 Tsit5 rtol 1e-10, "
-                      f"{dt:.1f} s on {threads} threads"}
+    out = {"value": cw * ch / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"central {cw}x{ch} crop of the 1920x1080 frame, FP64 Tsit5 rtol 1e-10, "
+                     f"{dt:.1f} s on {threads} threads"}
+    if gpu_frame is not None:
+        import numpy as np
+        g = gpu_frame[r0:r0 + ch, c0:c0 + cw].astype(np.float64)
+        d = gpu_diag[r0:r0 + ch, c0:c0 + cw]
+        both = ((d["flags"] & 1) > 0) & ((rays["flags"] & O.RAY_ESCAPED) > 0)
+        a = d["dir"][both]
+        b = rays["dir"][both]
+        ang = 2 * np.arcsin(np.clip(np.linalg.norm(a - b, axis=-1) / 2, 0, 1))
+        rel = np.abs(g - ref).sum(-1) / np.maximum(ref.sum(-1), 1e-6)
+        out["accuracy_vs_oracle"] = {
+            "rays": int(cw * ch), "escaped_both": int(both.sum()),
+            "dir_median_rad": float(np.median(ang)), "dir_p99_rad": float(np.percentile(ang, 99)),
+            "radiance_rel_median": float(np.median(rel)), "radiance_rel_p99": float(np.percentile(rel, 99)),
+            "class_mismatch": int((((d["flags"] & 8) > 0) != ((rays["flags"] & O.RAY_BLACK) > 0)).sum())}
+    return out
 
 
 def run_reference(args):
@@ -183,12 +200,14 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp32g", choices=["fp64", "fp32", "fp32g"])
+    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "fp32g"])
+    ap.add_argument("--no-variants", action="store_true", help="skip the FP32G / FP64 comparison runs")
     ap.add_argument("--schedule", default="pixel", choices=["pixel", "persistent"])
     ap.add_argument("--size", default="1920x1080", help="frame WxH (profiling uses a smaller case)")
     ap.add_argument("--r-guard", type=float, default=3.0)
     ap.add_argument("--crit-band", type=float, default=0.05)
-    ap.add_argument("--renorm", type=int, default=64)
+    ap.add_argument("--crit-r", type=float, default=4.0)
+    ap.add_argument("--renorm", type=int, default=256)
     ap.add_argument("--chunk", type=int, default=32)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -217,8 +236,8 @@ def main(argv=None):
     sched = _abi.ST_SCHED_PERSISTENT if args.schedule == "persistent" else _abi.ST_SCHED_PIXEL
     ctx = Context(workloads.sky(), disc=w.disc, volume=w.vol, emitter=w.emitter, device=local)
     p = ctx.params(w.semantics, width=w.width, height=w.height, precision=prec, schedule=sched,
-                   r_guard=args.r_guard, crit_band=args.crit_band, renorm_every=args.renorm,
-                   chunk_steps=args.chunk, **w.params)
+                   r_guard=args.r_guard, crit_band=args.crit_band, crit_r=args.crit_r,
+                   renorm_every=args.renorm, chunk_steps=args.chunk, **w.params)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def barrier():
@@ -278,10 +297,34 @@ def main(argv=None):
     fp32_peak = sms * 128 * 2 * sm_max * 1e6 / 1e12
     if rank != 0:
         return 0
+    variants = {}
+    if not args.no_variants and (W, H) == (1920, 1080):
+        # the same frame with FP64 guards (renormalisation every 256 steps, steps
+        # inside 3 M, near-critical rays inside 4 M) and all in FP64
+        for name, kw, reps in (("fp32_fp64_guarded", dict(precision=_abi.ST_PREC_FP32_GUARDED), 3),
+                               ("fp64", dict(precision=_abi.ST_PREC_FP64), 1)):
+            pv = ctx.params(w.semantics, width=W, height=H, schedule=sched, r_guard=3.0, crit_band=0.05,
+                            crit_r=4.0, renorm_every=256, **w.params, **kw)
+            ctx.render_device(w.cam, w.bh, pv)
+            ts = []
+            for _ in range(reps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                _, stv = ctx.render_device(w.cam, w.bh, pv)
+                ts.append(stv["kernel_ms"])
+            ms = float(np.mean(ts))
+            variants[name] = {"value": rays / (ms * 1e-3) / 1e6, "ms_per_step": ms,
+                              "fp64_steps_per_frame": stv["fp64_steps"]}
+        for name in variants:
+            variants[name]["speedup_of_value"] = value / variants[name]["value"]
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         try:
-            cpu = cpu_baseline()
+            pd = ctx.params(w.semantics, width=W, height=H, precision=prec, schedule=sched,
+                            r_guard=args.r_guard, crit_band=args.crit_band, crit_r=args.crit_r,
+                            renorm_every=args.renorm, chunk_steps=args.chunk, **w.params)
+            rd = ctx.render_raw(w.cam, w.bh, pd, diag=True)
+            cpu = cpu_baseline(gpu_frame=rd.image, gpu_diag=rd.diag) if (W, H) == (1920, 1080) else cpu_baseline()
         except Exception as e:  # report, do not fail the bench
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
     line = {
@@ -291,9 +334,11 @@ def main(argv=None):
         "config": {
             "workload": f"config1: Kerr a=0.9 M=1, static camera r=15 M i=80 deg, Lens(24), {W}x{H}, "
                         "gas 256x64x32 ISCO-25M h=0.05r, sky 2048x1024, kernel rules, samples=1",
-            "precision": {"fp64": "FP64", "fp32": "FP32", "fp32g": "FP32 bulk + FP64 guards"}[args.precision],
+            "precision": {"fp64": "FP64", "fp32": "FP32 (MUFU sqrt/rcp/exp/log)",
+                          "fp32g": "FP32 RHS, float-float state, FP64 guards"}[args.precision],
             "guards": {"r_guard": args.r_guard, "crit_band": args.crit_band, "renorm_every": args.renorm},
-            "surrogate": False,
+            "surrogate": "not applied: every ray of this frame starts inside the gas slab, and the gas "
+                         "line integral needs the integrated path (the surrogate serves gas-free rays)",
             "schedule": args.schedule,
             "parallelism": f"replicas{world}",
             "l2": "flushed between timed steps (256 MiB write)",
@@ -314,6 +359,7 @@ def main(argv=None):
         "gpu_launches": args.steps,
         "clocks": clk,
         "cpu_baseline": cpu,
+        "variants": variants,
     }
     print(json.dumps(line))
     ctx.close()
