@@ -219,7 +219,11 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams,
  * azimuthal frame) to the exit-direction residual over the initial coordinate
  * direction (3), the first equatorial-crossing radius, the redshift there and
  * the log-variance of the direction error.  Hidden layers run on the tensor
- * cores in BF16 with FP32 accumulation; training runs on the GPU. */
+ * cores in BF16 with FP32 accumulation; training runs on the GPU.
+ * With st_context_set_surrogate and p.surrogate = 1, st_render serves camera
+ * rays the gate accepts (predicted std-dev < p.surrogate_sigma, not near the
+ * critical curve, predicted not to cross the disc annulus, no gas) from the
+ * network and integrates the rest (DRAFT rules, samples = 1). */
 typedef struct st_surrogate st_surrogate;
 int st_surrogate_create(st_surrogate** out, int device, unsigned long long seed);
 void st_surrogate_destroy(st_surrogate* s);
@@ -238,6 +242,8 @@ int st_surrogate_generate(st_surrogate* s, long long n, long long sobol_offset, 
                           float* host_t, float* host_raw);
 /* AdamW steps over the generated set; loss_hist[steps] optional */
 int st_surrogate_train(st_surrogate* s, int steps, int batch, float lr, float weight_decay, float* loss_hist);
+/* Attach (or detach, NULL) a surrogate to a context for p.surrogate = 1. */
+int st_context_set_surrogate(st_context* ctx, st_surrogate* s);
 
 /* Allocation-free camera-track render.  No counterpart in the reference.
  * For callers that cannot allocate device memory: a renderer embedded in an

@@ -109,7 +109,7 @@ EXPORTS = [
     "st_render", "st_render_diag", "st_render_device", "st_render_frames", "st_camera_tetrad",
     "st_surrogate_create", "st_surrogate_destroy", "st_surrogate_num_params", "st_surrogate_get_params",
     "st_surrogate_set_params", "st_surrogate_forward", "st_surrogate_loss_grad", "st_surrogate_generate",
-    "st_surrogate_train", "st_render_frames_noalloc",
+    "st_surrogate_train", "st_render_frames_noalloc", "st_context_set_surrogate",
 ]
 
 _lib = None
@@ -167,6 +167,8 @@ def load(path: str | None = None) -> C.CDLL:
                                              C.c_int, P(StCamera), P(StSpacetime), P(StRenderParams), C.c_void_p,
                                              C.c_void_p, P(StStats)]
     lib.st_render_frames_noalloc.restype = C.c_int
+    lib.st_context_set_surrogate.argtypes = [C.c_void_p, C.c_void_p]
+    lib.st_context_set_surrogate.restype = C.c_int
     for name in ("st_context_create", "st_context_set_disc", "st_context_set_volume", "st_render",
                  "st_render_diag", "st_render_device", "st_render_frames", "st_camera_tetrad",
                  "st_surrogate_create", "st_surrogate_num_params", "st_surrogate_get_params",

@@ -155,6 +155,13 @@ class Context:
         _abi.check(self._lib.st_context_set_volume(self._h, C.byref(v)), "st_context_set_volume")
         self.volume = vol
 
+    def set_surrogate(self, sur):
+        """Attach a trained surrogate (spacetime_gb300.surrogate.Surrogate) for
+        renders with surrogate=1; None detaches it."""
+        _abi.check(self._lib.st_context_set_surrogate(self._h, sur._h if sur is not None else None),
+                   "st_context_set_surrogate")
+        self._sur = sur
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.st_context_destroy(self._h)

@@ -199,6 +199,61 @@ static double host_photon_orbit_min(double M, double a) {
   return 2.0 * M * (1.0 + std::cos((2.0 / 3.0) * std::acos(-a / M)));
 }
 
+// The static observer's orthonormal frame at pos with radial / polar /
+// azimuthal axes (Gram-Schmidt under the KS metric), lowered to covectors, and
+// the camera's KS radius, polar angle and azimuth: the surrogate's frame.
+static void host_static_frame(const double* pos, double M, double a, SurFrame* f) {
+  const double rr = std::sqrt(dot3(pos, pos));
+  const double ct = pos[2] / rr, stt = std::sqrt(std::max(1.0 - ct * ct, 0.0));
+  const double ph = std::atan2(pos[1], pos[0]), cp = std::cos(ph), sp = std::sin(ph);
+  const double e[3][3] = {{pos[0] / rr, pos[1] / rr, ct}, {ct * cp, ct * sp, -stt}, {-sp, cp, 0.0}};
+  double l[3], fk, rk;
+  if (a != 0.0) {
+    const double w = dot3(pos, pos) - a * a;
+    const double rk2 = 0.5 * (w + std::sqrt(w * w + 4.0 * a * a * pos[2] * pos[2]));
+    rk = std::sqrt(std::max(rk2, 1e-12));
+    const double ira = 1.0 / (rk2 + a * a);
+    l[0] = (rk * pos[0] + a * pos[1]) * ira;
+    l[1] = (rk * pos[1] - a * pos[0]) * ira;
+    l[2] = pos[2] / rk;
+    fk = 2.0 * M * rk2 * rk / (rk2 * rk2 + a * a * pos[2] * pos[2]);
+  } else {
+    rk = rr;
+    for (int k = 0; k < 3; ++k) l[k] = pos[k] / rr;
+    fk = 2.0 * M / rr;
+  }
+  auto g = [&](const double* A, const double* B) {
+    const double la = A[0] + l[0] * A[1] + l[1] * A[2] + l[2] * A[3];
+    const double lb = B[0] + l[0] * B[1] + l[1] * B[2] + l[2] * B[3];
+    return -A[0] * B[0] + A[1] * B[1] + A[2] * B[2] + A[3] * B[3] + fk * la * lb;
+  };
+  double U[4] = {1.0 / std::sqrt(1.0 - fk), 0, 0, 0}, E[3][4];
+  for (int m = 0; m < 3; ++m) {
+    double v[4] = {0.0, e[m][0], e[m][1], e[m][2]};
+    double c = g(v, U);
+    for (int k = 0; k < 4; ++k) v[k] += c * U[k];
+    for (int q = 0; q < m; ++q) {
+      c = g(v, E[q]);
+      for (int k = 0; k < 4; ++k) v[k] -= c * E[q][k];
+    }
+    c = std::sqrt(g(v, v));
+    for (int k = 0; k < 4; ++k) E[m][k] = v[k] / c;
+  }
+  auto lower = [&](const double* V, double* out) {
+    const double lv = V[0] + l[0] * V[1] + l[1] * V[2] + l[2] * V[3];
+    out[0] = -V[0] + fk * lv;
+    for (int k = 0; k < 3; ++k) out[k + 1] = V[k + 1] + fk * lv * l[k];
+  };
+  lower(U, f->Ul);
+  lower(E[0], f->E1l);
+  lower(E[1], f->E2l);
+  lower(E[2], f->E3l);
+  f->r = rk;
+  f->th = std::acos(std::min(std::max(pos[2] / rk, -1.0), 1.0));
+  f->cphi = cp;
+  f->sphi = sp;
+}
+
 // splitmix64 for the host-side pass shuffles
 struct Rng {
   uint64_t s;
@@ -246,6 +301,10 @@ struct st_context {
   unsigned long long* d_counters = nullptr;
   unsigned int* d_queue = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  st_surrogate* sur = nullptr;  // attached surrogate (not owned)
+  int* d_list = nullptr;        // surrogate fallback pixels
+  size_t list_cap = 0;
+  int* d_count = nullptr;
 };
 
 namespace {
@@ -288,7 +347,10 @@ int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, 
     if (a != 0.0) return ST_EUNSUPPORTED;
     if (ctx->vol_on) return ST_EUNSUPPORTED;
   }
-  if (rp->surrogate) return ST_ESTATE;
+  if (rp->surrogate) {
+    if (!ctx->sur) return ST_ESTATE;
+    if (rp->semantics != ST_SEM_DRAFT || rp->samples != 1 || ctx->vol_on) return ST_EUNSUPPORTED;
+  }
   std::memset(p, 0, sizeof(*p));
   const double beta[3] = {st::dot3(cam->velocity, cam->fwd), st::dot3(cam->velocity, cam->right),
                           st::dot3(cam->velocity, cam->up)};
@@ -447,6 +509,18 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
   p.diag = host_diag ? ctx->d_diag : nullptr;
   p.ap_r = cam->aperture_world > 0.0 ? cam->aperture_world / 2.0 : 0.0;
   cudaStream_t s = ctx->stream;
+  st::SurFrame sf{};
+  if (rp->surrogate) {
+    // network domain: camera r in [4, 50] M, above the plane, 0 <= a <= 0.99
+    st::host_static_frame(cam->pos, stp->M, stp->a, &sf);
+    if (!(sf.r >= 4.0 * stp->M && sf.r <= 50.0 * stp->M && sf.th <= 1.5707963267948966 && stp->a >= 0.0 &&
+          stp->a <= 0.99 * stp->M && stp->M == 1.0))
+      return ST_EUNSUPPORTED;
+    sf.sigma_max = rp->surrogate_sigma > 0.0 ? rp->surrogate_sigma : 1e-4;
+    if ((rc = ensure(&ctx->d_list, &ctx->list_cap, npix)) != ST_OK) return rc;
+    if (!ctx->d_count && cudaMalloc(&ctx->d_count, sizeof(int)) != cudaSuccess) return ST_ENOMEM;
+    v.sched = ST_SCHED_PIXEL;
+  }
   ST_CUDA(cudaMemsetAsync(ctx->d_counters, 0, st::CNT_N * sizeof(unsigned long long), s));
   const std::vector<PassPlan> passes = plan_passes(rp, cam);
   p.weight = (float)(1.0 / passes.size());
@@ -457,6 +531,13 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
     p.ju = pp.ju; p.jv = pp.jv; p.jw = pp.jw; p.jseed = pp.jseed;
     p.lens_u0 = pp.lens_u0; p.lens_v0 = pp.lens_v0; p.lens_w = pp.lens_w; p.lens_seed = pp.lens_seed;
     p.first_pass = (k == 0) ? 1 : 0;
+    if (rp->surrogate) {
+      const PassPlan& pp0 = passes[0];
+      (void)pp0;
+      if ((rc = st::surrogate_frame(ctx->sur, p, v, sf, ctx->d_list, ctx->d_count, s)) != ST_OK) return rc;
+      p.pix_list = ctx->d_list;
+      p.n_list = ctx->d_count;
+    }
     if (v.sched == ST_SCHED_PERSISTENT) {
       ST_CUDA(cudaMemsetAsync(ctx->d_queue, 0, sizeof(unsigned int), s));
       const long long tiles = (long long)((rp->width + 7) / 8) * ((rp->height + 3) / 4);
@@ -469,6 +550,8 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
   ST_CUDA(cudaEventRecord(ctx->ev1, s));
   unsigned long long cnt[st::CNT_N];
   ST_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
+  int n_fallback = 0;
+  if (rp->surrogate) ST_CUDA(cudaMemcpyAsync(&n_fallback, ctx->d_count, sizeof(int), cudaMemcpyDeviceToHost, s));
   unsigned long long d2h = 0;
   if (host_rgb) {
     ST_CUDA(st::launch_pack_rgb(ctx->d_fb, ctx->d_rgb, (int)npix, s));
@@ -491,7 +574,8 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
     stats->steps = cnt[st::CNT_STEPS];
     stats->fp64_steps = cnt[st::CNT_FP64];
     stats->gas_samples = cnt[st::CNT_GAS];
-    stats->surrogate_rays = cnt[st::CNT_SURR];
+    stats->surrogate_rays = rp->surrogate ? (unsigned long long)(npix - (size_t)n_fallback) : 0ull;
+    if (rp->surrogate) stats->rays += stats->surrogate_rays;
     stats->launches = launches;
     stats->status = status;
     stats->h2d_bytes = sizeof(TraceParams) * launches;
@@ -656,6 +740,8 @@ void st_context_destroy(st_context* ctx) {
   cudaFree(ctx->d_frames);
   cudaFree(ctx->d_counters);
   cudaFree(ctx->d_queue);
+  cudaFree(ctx->d_list);
+  cudaFree(ctx->d_count);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -754,6 +840,12 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
     stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
   return status;
+}
+
+int st_context_set_surrogate(st_context* ctx, st_surrogate* s) {
+  if (!ctx) return ST_EINVAL;
+  ctx->sur = s;
+  return ST_OK;
 }
 
 int st_camera_tetrad(const st_camera* cam, const st_spacetime* stp, double out16[16]) {

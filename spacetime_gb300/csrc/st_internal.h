@@ -69,6 +69,9 @@ struct TraceParams {
   float4* out;               // [height][width] (x frames)
   st_ray_diag* diag;         // optional
   unsigned long long* counters;  // CNT_N slots
+  // pixel schedule over a compacted list (surrogate fallback rays)
+  const int* pix_list;       // optional pixel indices (device)
+  const int* n_list;         // their count (device)
   // persistent schedule
   const FrameCam* frames;    // optional per-frame cameras (device)
   int n_rays;                // rays in the queue (frames x pixels)
@@ -86,6 +89,21 @@ struct Variant {
   int sem;        // ST_SEM_*
   int sched;      // ST_SCHED_*
 };
+
+// Surrogate frame constants: the static observer's frame at the camera,
+// lowered (covariant) so g(q, E) is a plain dot product, and the camera's
+// azimuth rotation of the network's azimuth-0 frame.
+struct SurFrame {
+  double Ul[4], E1l[4], E2l[4], E3l[4];
+  double r, th, cphi, sphi;
+  double sigma_max;
+};
+
+// Surrogate pass over the frame (st_surrogate.cu): network inputs, batched
+// inference, and the gate, which writes served pixels to p.out and compacts
+// the rest into list / *count (device).  Returns an ST_* status.
+int surrogate_frame(struct ::st_surrogate* s, const TraceParams& p, const Variant& v, const SurFrame& f,
+                    int* list, int* count, cudaStream_t stream);
 
 // Launch one trace pass; returns a cudaError_t.
 cudaError_t launch_trace(const Variant& v, const TraceParams& p, int block_x, int block_y,

@@ -37,8 +37,19 @@ __device__ __forceinline__ void flush_counters(const TraceParams& p, unsigned lo
 template <int PREC, int KERR, int VOL, int SEM>
 __global__ void __launch_bounds__(128, ST_MINB) trace_pixel_kernel(const __grid_constant__ TraceParams p) {
   using R = typename RealOf<PREC>::T;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (p.pix_list) {  // 1-D over a compacted pixel list
+    const int t = blockIdx.x * (blockDim.x * blockDim.y) + threadIdx.y * blockDim.x + threadIdx.x;
+    if (t < *p.n_list) {
+      const int pix = p.pix_list[t];
+      i = pix % p.width;
+      j = pix / p.width;
+    } else {
+      i = p.width;  // idle
+      j = 0;
+    }
+  }
   unsigned long long steps = 0, f64 = 0, gas = 0, rays = 0;
   if (i < p.width && j < p.height) {
     RayState<R> st;
@@ -134,6 +145,7 @@ cudaError_t launch_variant(const TraceParams& p, int sched, int bx, int by, int 
     if (bx <= 0 || by <= 0 || bx * by != 128) { bx = 16; by = 8; }
     dim3 block(bx, by);
     dim3 grid((p.width + bx - 1) / bx, (p.height + by - 1) / by);
+    if (p.pix_list) grid = dim3((unsigned)(((long long)p.width * p.height + 127) / 128), 1);
     trace_pixel_kernel<PREC, KERR, VOL, SEM><<<grid, block, 0, s>>>(p);
   }
   return cudaGetLastError();

@@ -5,8 +5,9 @@
 //             spin a in [0, 0.99], unit ray direction n in the static observer's
 //             frame (radial, polar, azimuthal axes), normalised to O(1)
 //   outputs : exit-direction residual (3) over the ray's initial coordinate
-//             direction, first equatorial-crossing radius (scaled), redshift
-//             g - 1 there, and the log-variance of the direction error.
+//             direction, first equatorial-crossing radius as 10/s - 1 (a ray
+//             that never crosses is the s -> inf limit, -1), redshift g - 1
+//             there, and the log-variance of the direction error.
 // The three 256x256 layers run on the tensor cores in BF16 with FP32
 // accumulation (st_mlp.cuh); the 6->256 and 256->6 layers, the loss and AdamW
 // run in FP32.  Master weights and optimiser state are FP32.
@@ -424,7 +425,7 @@ __global__ void label_kernel(const LabelParams lp) {
   for (int k = 0; k < NIN; ++k) Xo[k] = x[k];
   float* To = lp.T + tid * NT;
   for (int k = 0; k < 3; ++k) To[k] = ok ? (float)(vel[k] / vl - d0[k]) : 0.f;
-  To[3] = (r_cross > 0.f ? fminf(r_cross, 45.f) : 45.f) / 15.f - 1.f;
+  To[3] = (r_cross > 0.f ? fminf(10.f / r_cross, 5.f) : 0.f) - 1.f;  // 10/s - 1; no crossing = s -> inf
   To[4] = r_cross > 0.f ? g_cross - 1.f : 0.f;
   To[5] = ok ? 1.f : 0.f;
   To[6] = r_cross > 0.f ? 1.f : 0.f;
@@ -436,6 +437,120 @@ __global__ void label_kernel(const LabelParams lp) {
     Ro[6] = (float)flags; Ro[7] = (float)steps;
     Ro[8] = (float)(vel[0] / vl); Ro[9] = (float)(vel[1] / vl); Ro[10] = (float)(vel[2] / vl);
     Ro[11] = r_cross;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Frame pass: camera rays -> network inputs -> gate
+// ---------------------------------------------------------------------------
+
+// Inputs of every pixel's camera ray: the ray is built exactly as the trace
+// kernel builds it (init_ray, FP64 construction), raised to its tangent
+// q = (-p_t + f l, p - f l L), projected on the static observer's frame.
+template <int KERR>
+__global__ void sur_inputs_kernel(const __grid_constant__ TraceParams p, const __grid_constant__ SurFrame f,
+                                  float* X, float4* aux, int* aflags, int npix) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= npix) return;
+  const int i = pix % p.width, j = pix / p.width;
+  RayState<float> st;
+  const CamView cam{p.pos, p.Ef, p.Er, p.Eu, p.U, p.r_escape, p.nmax};
+  init_ray<ST_PREC_FP32_GUARDED, KERR, ST_SEM_DRAFT>(p, cam, i, j, st);
+  double y[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) y[k] = (double)st.y[k] + (double)st.lo[k];
+  const double pt = (double)st.pt, a = p.a, M = p.M;
+  double L[3], fk;
+  if (KERR) {
+    const double r2 = fmax(ks_r2(y[0], y[1], y[2], a), 1e-12), r = sqrt(r2), ira = 1.0 / (r2 + a * a);
+    L[0] = (r * y[0] + a * y[1]) * ira;
+    L[1] = (r * y[1] - a * y[0]) * ira;
+    L[2] = y[2] / r;
+    fk = 2.0 * M * r2 * r / (r2 * r2 + a * a * y[2] * y[2]);
+  } else {
+    const double r = sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+    L[0] = y[0] / r; L[1] = y[1] / r; L[2] = y[2] / r;
+    fk = 2.0 * M / r;
+  }
+  const double ell = -pt + L[0] * y[3] + L[1] * y[4] + L[2] * y[5];
+  const double q[4] = {-pt + fk * ell, y[3] - fk * ell * L[0], y[4] - fk * ell * L[1], y[5] - fk * ell * L[2]};
+  auto dot4 = [&](const double* c) { return q[0] * c[0] + q[1] * c[1] + q[2] * c[2] + q[3] * c[3]; };
+  const double al = fabs(dot4(f.Ul));
+  const float n[3] = {(float)(dot4(f.E1l) / al), (float)(dot4(f.E2l) / al), (float)(dot4(f.E3l) / al)};
+  float x[6];
+  normalise_inputs((float)f.r, (float)f.th, (float)a, n, x);
+#pragma unroll
+  for (int k = 0; k < NIN; ++k) X[(size_t)pix * NIN + k] = x[k];
+  const double qn = sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  aux[pix] = make_float4((float)(q[1] / qn), (float)(q[2] / qn), (float)(q[3] / qn), st.scam);
+  int fl = st.flags & (ST_RAY_BCAPT | ST_RAY_GRAZE);
+  if (!KERR) {
+    // Schwarzschild critical band: b = |x cross p| / E against 3 sqrt(3) M
+    const double Lx = y[1] * y[5] - y[2] * y[4], Ly = y[2] * y[3] - y[0] * y[5], Lz = y[0] * y[4] - y[1] * y[3];
+    const double b = sqrt(Lx * Lx + Ly * Ly + Lz * Lz) / fabs(pt);
+    if (b < p.b_crit) fl |= ST_RAY_BCAPT;
+    if (fabs(b - p.b_crit) < fmax(p.crit_band, 0.05)) fl |= ST_RAY_GRAZE;
+  }
+  aflags[pix] = fl;
+}
+
+// Gate: serve a pixel from the network when it is not near the critical
+// curve, the predicted std-dev of its exit direction is below sigma_max and it
+// is predicted not to cross the disc annulus; otherwise append it (warp-
+// ordered) to the list the trace kernel integrates.
+__global__ void sur_gate_kernel(const __grid_constant__ TraceParams p, const __grid_constant__ SurFrame f,
+                                const float* __restrict__ out, const float4* __restrict__ aux,
+                                const int* __restrict__ aflags, int* list, int* count, int npix) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  bool serve = false;
+  float4 rgba = make_float4(0.f, 0.f, 0.f, 1.f);
+  double dird[3] = {0, 0, 0};
+  if (pix < npix) {
+    const float* o = out + (size_t)pix * NOUT;
+    const float sig = __expf(0.5f * fminf(fmaxf(o[5], -30.f), 12.f));
+    serve = (aflags[pix] & (ST_RAY_BCAPT | ST_RAY_GRAZE)) == 0 && sig < (float)f.sigma_max;
+    if (serve && p.disc_on) {
+      const float u = o[3] + 1.f;  // 10 / s
+      const float s = u > 0.02f ? 10.f / u : 1e9f;
+      if (s > (float)p.disc_inner - 1.5f && s < (float)p.disc_outer + 3.0f) serve = false;
+    }
+    if (serve) {
+      const float4 a4 = aux[pix];
+      const float c = (float)f.cphi, sn = (float)f.sphi;
+      const float dx = a4.x + (c * o[0] - sn * o[1]);
+      const float dy = a4.y + (sn * o[0] + c * o[1]);
+      const float dz = a4.z + o[2];
+      const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
+      const float d0 = dx * inv, d1 = dy * inv, d2 = dz * inv;
+      dird[0] = d0; dird[1] = d1; dird[2] = d2;
+      float sky[3];
+      sample_sky(p, acosf(fminf(fmaxf(d2, -1.f), 1.f)), atan2f(d1, d0), sky);
+      const float g = a4.w;
+      if (g != 1.f) {
+        sky[0] *= 57.4f / (__expf(4.067f / g) - 1.f);
+        sky[1] *= 90.2f / (__expf(4.513f / g) - 1.f);
+        sky[2] *= 206.5f / (__expf(5.335f / g) - 1.f);
+      }
+      rgba = make_float4(p.weight * sky[0], p.weight * sky[1], p.weight * sky[2], 1.f);
+    }
+  }
+  const unsigned want = __ballot_sync(0xffffffffu, pix < npix && !serve);
+  int base = 0;
+  if ((threadIdx.x & 31) == 0 && want) base = atomicAdd(count, __popc(want));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (pix >= npix) return;
+  if (serve) {
+    p.out[pix] = rgba;
+    if (p.diag) {
+      st_ray_diag d;
+      d.dir[0] = dird[0]; d.dir[1] = dird[1]; d.dir[2] = dird[2];
+      d.r_final = 0.f; d.alpha = 1.f; d.r_cross = -1.f; d.g_cross = 0.f; d.lambda = 0.f;
+      d.flags = ST_RAY_SURROGATE | ST_RAY_ESCAPED;
+      d.steps = 0; d.fp64_steps = 0; d.pad[0] = d.pad[1] = 0;
+      p.diag[pix] = d;
+    }
+  } else {
+    list[base + __popc(want & ((1u << (threadIdx.x & 31)) - 1u))] = pix;
   }
 }
 
@@ -459,6 +574,10 @@ struct st_surrogate {
   __nv_bfloat16* H[4] = {nullptr, nullptr, nullptr, nullptr};
   __nv_bfloat16 *dZa = nullptr, *dZb = nullptr;
   float *out = nullptr, *dout = nullptr, *T = nullptr, *loss = nullptr;
+  // frame pass buffers (device)
+  float4* aux = nullptr;  // per pixel: initial direction (3), camera shift
+  int* aflags = nullptr;  // per pixel: ST_RAY_* launch flags
+  int aux_cap = 0;
   // training set (device)
   float *DX = nullptr, *DT = nullptr;
   long long ndata = 0;
@@ -505,8 +624,7 @@ int sync_bf16(st_surrogate* s) {
 }
 
 // forward of B rows (B multiple of 128) from s->X-like input pointer
-int forward(st_surrogate* s, const float* X, int B, bool keep_z) {
-  cudaStream_t st = s->stream;
+int forward(st_surrogate* s, const float* X, int B, bool keep_z, cudaStream_t st) {
   l0_fwd<<<(B * NH + 255) / 256, 256, 0, st>>>(X, s->P, keep_z ? s->Z[0] : nullptr, s->H[0], B);
   SC(cudaGetLastError());
   for (int l = 1; l <= 3; ++l) {
@@ -622,6 +740,7 @@ void st_surrogate_destroy(st_surrogate* s) {
   for (int l = 0; l < 4; ++l) { cudaFree(s->Z[l]); cudaFree(s->H[l]); }
   cudaFree(s->dZa); cudaFree(s->dZb); cudaFree(s->out); cudaFree(s->dout); cudaFree(s->T);
   cudaFree(s->DX); cudaFree(s->DT);
+  cudaFree(s->aux); cudaFree(s->aflags);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
 }
@@ -652,7 +771,7 @@ int st_surrogate_forward(st_surrogate* s, const float* X, int n, float* out) {
   if (rc != ST_OK) return rc;
   SC(cudaMemsetAsync(s->X, 0, (size_t)B * NIN * 4, s->stream));
   SC(cudaMemcpyAsync(s->X, X, (size_t)n * NIN * 4, cudaMemcpyHostToDevice, s->stream));
-  if ((rc = forward(s, s->X, B, false)) != ST_OK) return rc;
+  if ((rc = forward(s, s->X, B, false, s->stream)) != ST_OK) return rc;
   SC(cudaMemcpyAsync(out, s->out, (size_t)n * NOUT * 4, cudaMemcpyDeviceToHost, s->stream));
   SC(cudaStreamSynchronize(s->stream));
   return ST_OK;
@@ -670,7 +789,7 @@ int st_surrogate_loss_grad(st_surrogate* s, const float* X, const float* T, int 
   SC(cudaMemsetAsync(s->T, 0, (size_t)B * NT * 4, st));
   SC(cudaMemcpyAsync(s->X, X, (size_t)n * NIN * 4, cudaMemcpyHostToDevice, st));
   SC(cudaMemcpyAsync(s->T, T, (size_t)n * NT * 4, cudaMemcpyHostToDevice, st));
-  if ((rc = forward(s, s->X, B, true)) != ST_OK) return rc;
+  if ((rc = forward(s, s->X, B, true, s->stream)) != ST_OK) return rc;
   SC(cudaMemsetAsync(s->loss, 0, 16 * 4, st));
   loss_grad<<<(B + 255) / 256, 256, 0, st>>>(s->out, s->T, s->dout, s->loss, n, 1.0f / n);
   SC(cudaGetLastError());
@@ -724,7 +843,7 @@ int st_surrogate_train(st_surrogate* s, int steps, int batch, float lr, float we
     const long long bi = (s->step * 7919LL) % nb;  // stride through the batches
     const float* X = s->DX + bi * batch * NIN;
     const float* T = s->DT + bi * batch * NT;
-    if ((rc = forward(s, X, batch, true)) != ST_OK) return rc;
+    if ((rc = forward(s, X, batch, true, s->stream)) != ST_OK) return rc;
     SC(cudaMemsetAsync(s->loss, 0, 16 * 4, st));
     loss_grad<<<(batch + 255) / 256, 256, 0, st>>>(s->out, T, s->dout, s->loss, batch, 1.0f / batch);
     SC(cudaGetLastError());
@@ -744,3 +863,37 @@ int st_surrogate_train(st_surrogate* s, int steps, int batch, float lr, float we
 }
 
 }  // extern "C"
+
+namespace st {
+
+// Surrogate pass of one frame on `stream` (see st_internal.h).
+int surrogate_frame(st_surrogate* s, const TraceParams& p, const Variant& v, const SurFrame& f, int* list, int* count,
+                    cudaStream_t stream) {
+  const int npix = p.width * p.height;
+  const int B = pad128(npix);
+  int rc = ensure_work(s, B);
+  if (rc != ST_OK) return rc;
+  if (s->aux_cap < npix) {
+    cudaFree(s->aux);
+    cudaFree(s->aflags);
+    s->aux = nullptr;
+    s->aflags = nullptr;
+    s->aux_cap = 0;
+    if (cudaMalloc(&s->aux, (size_t)npix * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&s->aflags, (size_t)npix * sizeof(int)) != cudaSuccess)
+      return ST_ENOMEM;
+    s->aux_cap = npix;
+  }
+  const unsigned nb = (unsigned)((npix + 127) / 128);
+  if (B > npix) SC(cudaMemsetAsync(s->X + (size_t)npix * sur::NIN, 0, (size_t)(B - npix) * sur::NIN * 4, stream));
+  if (v.kerr) sur::sur_inputs_kernel<1><<<nb, 128, 0, stream>>>(p, f, s->X, s->aux, s->aflags, npix);
+  else sur::sur_inputs_kernel<0><<<nb, 128, 0, stream>>>(p, f, s->X, s->aux, s->aflags, npix);
+  SC(cudaGetLastError());
+  if ((rc = forward(s, s->X, B, false, stream)) != ST_OK) return rc;
+  SC(cudaMemsetAsync(count, 0, sizeof(int), stream));
+  sur::sur_gate_kernel<<<nb, 128, 0, stream>>>(p, f, s->out, s->aux, s->aflags, list, count, npix);
+  SC(cudaGetLastError());
+  return ST_OK;
+}
+
+}  // namespace st

@@ -1,0 +1,75 @@
+"""The surrogate inside st_render (camera-ray mode): gating, compaction of
+the integrated remainder, and what a trained network gains.
+
+- An untrained network is never confident, so every ray falls back to the
+  integrator and the frame must equal the plain render bit for bit.
+- With a trained network (trained here, on the GPU, in seconds) served rays
+  skip the integration: the trace kernel's step count drops, and the served
+  rays' exit directions stay within the gate's error level against the FP64
+  oracle's Tsit5.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from spacetime_gb300 import _abi, workloads
+from spacetime_gb300.api import Context
+from spacetime_gb300.surrogate import Surrogate
+
+from .helpers import angle
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene():
+    w = workloads.config1_thin().scaled(192, 108)
+    w.params = dict(samples=1, pixel_jitter=0, exit_landing=1)
+    return w
+
+
+def test_untrained_surrogate_falls_back_everywhere(built_lib):
+    w = _scene()
+    sky = workloads.sky(512, 256)
+    sur = Surrogate(0, seed=9)
+    with Context(sky, disc=w.disc, emitter=w.emitter) as ctx:
+        ctx.set_surrogate(sur)
+        p0 = ctx.params(w.semantics, width=w.width, height=w.height, precision=_abi.ST_PREC_FP32, **w.params)
+        a = ctx.render_raw(w.cam, w.bh, p0, diag=True)
+        p1 = ctx.params(w.semantics, width=w.width, height=w.height, precision=_abi.ST_PREC_FP32, surrogate=1,
+                        surrogate_sigma=1e-4, **w.params)
+        b = ctx.render_raw(w.cam, w.bh, p1, diag=True)
+    assert b.stats["surrogate_rays"] == 0
+    np.testing.assert_array_equal(a.image, b.image)
+    assert a.stats["steps"] == b.stats["steps"]
+    sur.close()
+
+
+def test_trained_surrogate_gain(built_lib):
+    w = _scene()
+    sky = workloads.sky(512, 256)
+    sur = Surrogate(0, seed=1)
+    sur.generate(1 << 20, offset=0, copy=False)
+    for k in range(10):
+        lr = 1e-5 + 0.5 * (2e-3 - 1e-5) * (1 + np.cos(np.pi * k / 9))
+        sur.train(1000, batch=16384, lr=lr, weight_decay=1e-6)
+    with Context(sky, disc=w.disc, emitter=w.emitter) as ctx:
+        ctx.set_surrogate(sur)
+        p0 = ctx.params(w.semantics, width=w.width, height=w.height, precision=_abi.ST_PREC_FP32, **w.params)
+        a = ctx.render_raw(w.cam, w.bh, p0, diag=True)
+        p1 = ctx.params(w.semantics, width=w.width, height=w.height, precision=_abi.ST_PREC_FP32, surrogate=1,
+                        surrogate_sigma=3e-4, **w.params)
+        b = ctx.render_raw(w.cam, w.bh, p1, diag=True)
+    served = (b.diag["flags"] & _abi.ST_RAY_SURROGATE) > 0
+    print("served fraction", served.mean(), "steps", a.stats["steps"], "->", b.stats["steps"],
+          "kernel ms", a.stats["kernel_ms"], "->", b.stats["kernel_ms"])
+    assert served.mean() > 0.05
+    assert b.stats["steps"] < a.stats["steps"]
+    assert np.isfinite(b.image).all()
+    ref, rays = O.scene_for(w, sky, O.INT_TSIT5).render()
+    ok = served & ((rays["flags"] & O.RAY_ESCAPED) > 0)
+    d = angle(b.diag["dir"][ok], rays["dir"][ok])
+    print("served dir error median", np.median(d), "p99", np.percentile(d, 99))
+    assert np.median(d) < 3e-4
+    # unserved pixels are the integrator's, bit for bit
+    np.testing.assert_array_equal(a.image[~served], b.image[~served])
+    sur.close()
