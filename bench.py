@@ -125,31 +125,34 @@ def dist_env():
 
 
 def cpu_baseline(seconds_target: float = 15.0, threads: int | None = None, gpu_frame=None,
-                 gpu_diag=None) -> dict:
+                 gpu_diag=None, workload: str = "config1", frame_size=(1920, 1080)) -> dict:
     """The FP64 oracle (Tsit5 rtol 1e-10, kernel rules) on a central crop of
     the workload, sized for ~10-30 s of host work.  When the GPU frame and its
     per-ray records are given, the same crop also yields the GPU path's
     exit-direction and radiance error against the oracle."""
     from oracle import oracle as O
     from spacetime_gb300 import workloads
-    w = workloads.config1()
+    FW, FH = frame_size
+    w = {"config1": workloads.config1, "config1_thin": workloads.config1_thin,
+         "config2": lambda: workloads.config2(nframes=240), "config4": workloads.config4}[workload]()
+    w = w.scaled(FW, FH)
     threads = threads or os.cpu_count() or 1
     cw, ch = 48, 27
-    sc = O.scene_for(w, workloads.sky(), O.INT_TSIT5, rect=(936, cw, 526, ch))
+    sc = O.scene_for(w, workloads.sky(), O.INT_TSIT5, rect=((FW - cw) // 2, cw, (FH - ch) // 2, ch))
     t0 = time.perf_counter()
     sc.render(nthreads=threads, records=False)
     dt = time.perf_counter() - t0
     rate = cw * ch / max(dt, 1e-6)
     n = int(min(max(rate * seconds_target, 2000), 200000))
-    cw = int(min(1920, max(48, round(math.sqrt(n * 16 / 9)))))
-    ch = int(min(1080, max(27, round(cw * 9 / 16))))
-    c0, r0 = (1920 - cw) // 2, (1080 - ch) // 2
+    cw = int(min(FW, max(48, round(math.sqrt(n * 16 / 9)))))
+    ch = int(min(FH, max(27, round(cw * 9 / 16))))
+    c0, r0 = (FW - cw) // 2, (FH - ch) // 2
     sc = O.scene_for(w, workloads.sky(), O.INT_TSIT5, rect=(c0, cw, r0, ch))
     t0 = time.perf_counter()
     ref, rays = sc.render(nthreads=threads, records=gpu_frame is not None)
     dt = time.perf_counter() - t0
     out = {"value": cw * ch / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-           "sample": f"central {cw}x{ch} crop of the 1920x1080 frame, FP64 Tsit5 rtol 1e-10, "
+           "sample": f"central {cw}x{ch} crop of the {FW}x{FH} frame ({workload}), FP64 Tsit5 rtol 1e-10, "
                      f"{dt:.1f} s on {threads} threads"}
     if gpu_frame is not None:
         import numpy as np
@@ -194,6 +197,71 @@ def run_reference(args):
     return 0
 
 
+def run_track(args):
+    """config2 (240 frames 1280x720 free fall, Schwarzschild, thin disc) or
+    config4 (8 frames 3840x2160, Kerr a=0.99, boosted 0.3c, gas 512x128x64):
+    one step = the whole track in one launch (st_render_frames), with the
+    autotuned schedule and CUDA-graph replay."""
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from spacetime_gb300 import _abi, autotune, workloads
+    from spacetime_gb300.api import Context
+    w = workloads.config2() if args.workload == "config2" else workloads.config4()
+    prec = {"fp64": _abi.ST_PREC_FP64, "fp32": _abi.ST_PREC_FP32, "fp32g": _abi.ST_PREC_FP32_GUARDED}[args.precision]
+    ctx = Context(workloads.sky(), disc=w.disc, volume=w.vol, emitter=w.emitter, device=local)
+    p = ctx.params(w.semantics, width=w.width, height=w.height, precision=prec, r_guard=args.r_guard,
+                   crit_band=args.crit_band, crit_r=args.crit_r, renorm_every=args.renorm, **w.params)
+    tuned = autotune.tune(ctx, w.cams, w.bh, p, sample_frames=min(8, len(w.cams)), repeats=1)
+    autotune.apply(p, tuned)
+    p.graph = 1
+    for _ in range(args.warmup):
+        ctx.render_frames_raw(w.cams, w.bh, p)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local, args.clocks_csv)
+    clocks.start()
+    kms, tot = [], []
+    for _ in range(args.steps):
+        r = ctx.render_frames_raw(w.cams, w.bh, p)
+        kms.append(r.stats["kernel_ms"])
+        tot.append(r.stats["total_ms"])
+        st = r.stats
+    clk = clocks.stop()
+    rays = len(w.cams) * w.width * w.height
+    ms = float(np.mean(kms))
+    value = rays / (ms * 1e-3) / 1e6
+    kerr = getattr(w.bh, "a", 0.0) != 0.0
+    flops = st["steps"] * flops_per_step(kerr) + st["gas_samples"] * FLOPS_GAS_SAMPLE
+    achieved = flops / (ms * 1e-3) / 1e12
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_max = measured_peaks().get("sm_max_mhz", 2070.0)
+    fp32_peak = sms * 128 * 2 * sm_max * 1e6 / 1e12
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(workload=args.workload, frame_size=(w.width, w.height))
+        except Exception as e:
+            cpu = {"value": None, "sample": f"failed: {e}"}
+    line = {
+        "metric": f"Mrays/s {args.workload} track", "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if args.precision != "fp64" else "f64", "data": "synthetic",
+        "config": {"workload": w.name, "frames": len(w.cams), "size": f"{w.width}x{w.height}",
+                   "schedule": tuned, "graph": True, "steps_per_track": st["steps"],
+                   "gas_samples_per_track": st["gas_samples"], "per_frame_ms": ms / len(w.cams),
+                   "l2": "inputs stay L2-resident by design; per-step time is kernel time of the whole track"},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": None},
+        "e2e": {"value": rays / (float(np.mean(tot)) * 1e-3) / 1e6, "unit": UNIT,
+                "h2d_bytes_per_step": int(st["h2d_bytes"]), "d2h_bytes_per_step": int(rays * 12)},
+        "gpu_launches": args.steps * 2, "clocks": clk, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -213,10 +281,16 @@ def main(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--clocks-csv", default=None)
+    ap.add_argument("--workload", default="config1", choices=["config1", "config1_thin", "config2", "config4"],
+                    help="config1 is the headline; the others are the remaining benchmark configurations")
+    ap.add_argument("--surrogate", default=None, help="trained surrogate parameters (.npy) for config1_thin")
+    ap.add_argument("--sigma", type=float, default=1e-4, help="surrogate gate: max predicted std-dev (rad)")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload in ("config2", "config4"):
+        return run_track(args)
 
     import numpy as np
     import torch
@@ -229,15 +303,23 @@ def main(argv=None):
     from spacetime_gb300 import _abi, workloads
     from spacetime_gb300.api import Context
 
-    w = workloads.config1()
+    w = workloads.config1() if args.workload == "config1" else workloads.config1_thin()
     W, H = (int(x) for x in args.size.lower().split("x"))
     w = w.scaled(W, H)
     prec = {"fp64": _abi.ST_PREC_FP64, "fp32": _abi.ST_PREC_FP32, "fp32g": _abi.ST_PREC_FP32_GUARDED}[args.precision]
     sched = _abi.ST_SCHED_PERSISTENT if args.schedule == "persistent" else _abi.ST_SCHED_PIXEL
     ctx = Context(workloads.sky(), disc=w.disc, volume=w.vol, emitter=w.emitter, device=local)
+    sur = None
+    extra = {}
+    if args.surrogate:
+        from spacetime_gb300.surrogate import Surrogate
+        sur = Surrogate(local)
+        sur.set_params(np.load(args.surrogate))
+        ctx.set_surrogate(sur)
+        extra = dict(surrogate=1, surrogate_sigma=args.sigma)
     p = ctx.params(w.semantics, width=w.width, height=w.height, precision=prec, schedule=sched,
                    r_guard=args.r_guard, crit_band=args.crit_band, crit_r=args.crit_r,
-                   renorm_every=args.renorm, chunk_steps=args.chunk, **w.params)
+                   renorm_every=args.renorm, chunk_steps=args.chunk, **w.params, **extra)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def barrier():
@@ -258,6 +340,7 @@ def main(argv=None):
         _, st = ctx.render_device(w.cam, w.bh, p)
         kernel_ms.append(st["kernel_ms"])
         stats_last = st
+    served = stats_last.get("surrogate_rays", 0)
     barrier()
     wall = time.perf_counter() - t_wall0
     # e2e: through st_render into pinned host memory
@@ -298,7 +381,7 @@ def main(argv=None):
     if rank != 0:
         return 0
     variants = {}
-    if not args.no_variants and (W, H) == (1920, 1080):
+    if not args.no_variants and (W, H) == (1920, 1080) and args.workload == "config1":
         # the same frame with FP64 guards (renormalisation every 256 steps, steps
         # inside 3 M, near-critical rays inside 4 M) and all in FP64
         for name, kw, reps in (("fp32_fp64_guarded", dict(precision=_abi.ST_PREC_FP32_GUARDED), 3),
@@ -324,7 +407,8 @@ def main(argv=None):
                             r_guard=args.r_guard, crit_band=args.crit_band, crit_r=args.crit_r,
                             renorm_every=args.renorm, chunk_steps=args.chunk, **w.params)
             rd = ctx.render_raw(w.cam, w.bh, pd, diag=True)
-            cpu = cpu_baseline(gpu_frame=rd.image, gpu_diag=rd.diag) if (W, H) == (1920, 1080) else cpu_baseline()
+            cpu = cpu_baseline(gpu_frame=rd.image, gpu_diag=rd.diag, workload=args.workload) \
+                if (W, H) == (1920, 1080) else cpu_baseline(workload=args.workload)
         except Exception as e:  # report, do not fail the bench
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
     line = {
@@ -337,8 +421,11 @@ def main(argv=None):
             "precision": {"fp64": "FP64", "fp32": "FP32 (MUFU sqrt/rcp/exp/log)",
                           "fp32g": "FP32 RHS, float-float state, FP64 guards"}[args.precision],
             "guards": {"r_guard": args.r_guard, "crit_band": args.crit_band, "renorm_every": args.renorm},
-            "surrogate": "not applied: every ray of this frame starts inside the gas slab, and the gas "
-                         "line integral needs the integrated path (the surrogate serves gas-free rays)",
+            "surrogate": ("not applied: every ray of this frame starts inside the gas slab, and the gas "
+                          "line integral needs the integrated path (the surrogate serves gas-free rays)")
+                         if args.workload == "config1" else
+                         ({"params": os.path.basename(args.surrogate), "sigma_gate_rad": args.sigma,
+                           "served_fraction": served / (W * H)} if args.surrogate else False),
             "schedule": args.schedule,
             "parallelism": f"replicas{world}",
             "l2": "flushed between timed steps (256 MiB write)",

@@ -144,6 +144,9 @@ typedef struct {
   double surrogate_sigma;    /* gate: max predicted std-dev (rad) served */
   int block_x, block_y;      /* ST_SCHED_PIXEL tile; 0 = tuned default */
   int chunk_steps;           /* ST_SCHED_PERSISTENT steps per refill check */
+  int graph;                 /* st_render_frames: capture the device work in a
+                                CUDA graph and replay it while the frame count,
+                                sizes and rules are unchanged */
 } st_render_params;
 
 typedef struct {

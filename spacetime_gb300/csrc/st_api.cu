@@ -301,6 +301,14 @@ struct st_context {
   unsigned long long* d_counters = nullptr;
   unsigned int* d_queue = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // camera-track path: pinned staging and the captured graph
+  st::FrameCam* h_frames = nullptr;
+  size_t h_frames_cap = 0;
+  unsigned long long* h_cnt = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  st::TraceParams gkey{};
+  st::Variant gvar{};
+  size_t gbytes = 0;
   st_surrogate* sur = nullptr;  // attached surrogate (not owned)
   int* d_list = nullptr;        // surrogate fallback pixels
   size_t list_cap = 0;
@@ -742,6 +750,9 @@ void st_context_destroy(st_context* ctx) {
   cudaFree(ctx->d_queue);
   cudaFree(ctx->d_list);
   cudaFree(ctx->d_count);
+  if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  cudaFreeHost(ctx->h_frames);
+  cudaFreeHost(ctx->h_cnt);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -769,7 +780,7 @@ int st_render_device(st_context* ctx, const st_camera* cam, const st_spacetime* 
 int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const st_spacetime* stp,
                      const st_render_params* rp, float* out_rgb, st_stats* stats) {
   if (!ctx || nframes <= 0 || !cams || !stp || !rp || !out_rgb) return ST_EINVAL;
-  if (rp->semantics != ST_SEM_DRAFT || rp->samples != 1) return ST_EUNSUPPORTED;
+  if (rp->semantics != ST_SEM_DRAFT || rp->samples != 1 || rp->surrogate) return ST_EUNSUPPORTED;
   const auto t0 = std::chrono::steady_clock::now();
   TraceParams p;
   st::Variant v;
@@ -778,7 +789,16 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
   const size_t npix = (size_t)rp->width * rp->height;
   if (npix * (size_t)nframes > (size_t)1 << 31) return ST_EINVAL;
   if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
-  std::vector<st::FrameCam> fc(nframes);
+  if (ctx->h_frames_cap < (size_t)nframes) {
+    cudaFreeHost(ctx->h_frames);
+    ctx->h_frames = nullptr;
+    ctx->h_frames_cap = 0;
+    if (cudaMallocHost(&ctx->h_frames, nframes * sizeof(st::FrameCam)) != cudaSuccess) return ST_ENOMEM;
+    ctx->h_frames_cap = nframes;
+  }
+  if (!ctx->h_cnt && cudaMallocHost(&ctx->h_cnt, st::CNT_N * sizeof(unsigned long long)) != cudaSuccess)
+    return ST_ENOMEM;
+  st::FrameCam* fc = ctx->h_frames;
   int nmax_max = 0;
   for (int f = 0; f < nframes; ++f) {
     TraceParams q;
@@ -792,15 +812,13 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
     std::memcpy(fc[f].U, q.U, sizeof q.U);
     fc[f].r_escape = q.r_escape;
     fc[f].nmax = q.nmax;
+    fc[f].pad = 0;
     nmax_max = std::max(nmax_max, q.nmax);
   }
   if ((rc = ensure(&ctx->d_frames, &ctx->frames_cap, (size_t)nframes)) != ST_OK) return rc;
   if ((rc = ensure(&ctx->d_fb, &ctx->fb_cap, npix * nframes)) != ST_OK) return rc;
   if ((rc = ensure(&ctx->d_rgb, &ctx->rgb_cap, 3 * npix * nframes)) != ST_OK) return rc;
   cudaStream_t s = ctx->stream;
-  ST_CUDA(cudaMemcpyAsync(ctx->d_frames, fc.data(), nframes * sizeof(st::FrameCam), cudaMemcpyHostToDevice, s));
-  ST_CUDA(cudaMemsetAsync(ctx->d_counters, 0, st::CNT_N * sizeof(unsigned long long), s));
-  ST_CUDA(cudaMemsetAsync(ctx->d_queue, 0, sizeof(unsigned int), s));
   const std::vector<PassPlan> passes = plan_passes(rp, &cams[0]);
   const PassPlan& pp = passes[0];
   p.ju = pp.ju; p.jv = pp.jv; p.jw = pp.jw; p.jseed = pp.jseed;
@@ -808,21 +826,61 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
   p.first_pass = 1;
   p.out = ctx->d_fb;
   p.frames = ctx->d_frames;
+  p.n_frames = nframes;
   p.frame_stride = (int)npix;
+  // the frame-independent camera fields are unused with a frame table: zero
+  // them so the graph key depends only on sizes and rules
+  std::memset(p.pos, 0, sizeof p.pos);
+  std::memset(p.Ef, 0, sizeof p.Ef);
+  std::memset(p.Er, 0, sizeof p.Er);
+  std::memset(p.Eu, 0, sizeof p.Eu);
+  std::memset(p.U, 0, sizeof p.U);
+  p.r_escape = 0.0;
   const long long tiles = (long long)((rp->width + 7) / 8) * ((rp->height + 3) / 4);
   p.n_rays = (int)(tiles * 32 * nframes);
   p.chunk_steps = rp->chunk_steps > 0 ? rp->chunk_steps : 32;
   p.budget_iters = ((long long)p.n_rays + 32) * ((long long)nmax_max / p.chunk_steps + 2);
   p.nmax = nmax_max;
-  v.sched = ST_SCHED_PERSISTENT;
-  ST_CUDA(cudaEventRecord(ctx->ev0, s));
-  ST_CUDA(st::launch_trace(v, p, 0, 0, ctx->num_sms, s));
-  ST_CUDA(cudaEventRecord(ctx->ev1, s));
-  unsigned long long cnt[st::CNT_N];
-  ST_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
-  ST_CUDA(st::launch_pack_rgb(ctx->d_fb, ctx->d_rgb, (int)(npix * nframes), s));
+  v.sched = rp->schedule == ST_SCHED_PIXEL ? ST_SCHED_PIXEL : ST_SCHED_PERSISTENT;
+  // the device work of one call: stage cameras, clear queue and counters,
+  // trace all frames in one launch, pack, read the counters
+  auto enqueue = [&]() -> int {
+    ST_CUDA(cudaMemcpyAsync(ctx->d_frames, ctx->h_frames, nframes * sizeof(st::FrameCam), cudaMemcpyHostToDevice, s));
+    ST_CUDA(cudaMemsetAsync(ctx->d_counters, 0, st::CNT_N * sizeof(unsigned long long), s));
+    ST_CUDA(cudaMemsetAsync(ctx->d_queue, 0, sizeof(unsigned int), s));
+    ST_CUDA(cudaEventRecord(ctx->ev0, s));
+    ST_CUDA(st::launch_trace(v, p, rp->block_x, rp->block_y, ctx->num_sms, s));
+    ST_CUDA(cudaEventRecord(ctx->ev1, s));
+    ST_CUDA(st::launch_pack_rgb(ctx->d_fb, ctx->d_rgb, (int)(npix * nframes), s));
+    ST_CUDA(cudaMemcpyAsync(ctx->h_cnt, ctx->d_counters, st::CNT_N * sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, s));
+    return ST_OK;
+  };
+  if (rp->graph) {
+    const size_t key_bytes = (size_t)nframes;
+    const bool same = ctx->gexec && ctx->gbytes == key_bytes && std::memcmp(&ctx->gkey, &p, sizeof p) == 0 &&
+                      std::memcmp(&ctx->gvar, &v, sizeof v) == 0;
+    if (!same) {
+      if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+      cudaGraph_t g = nullptr;
+      ST_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      const int erc = enqueue();
+      const cudaError_t ec = cudaStreamEndCapture(s, &g);
+      if (erc != ST_OK || ec != cudaSuccess) { if (g) cudaGraphDestroy(g); return ST_ECUDA; }
+      const cudaError_t ei = cudaGraphInstantiate(&ctx->gexec, g, 0);
+      cudaGraphDestroy(g);
+      if (ei != cudaSuccess) { ctx->gexec = nullptr; return ST_ECUDA; }
+      ctx->gkey = p;
+      ctx->gvar = v;
+      ctx->gbytes = key_bytes;
+    }
+    ST_CUDA(cudaGraphLaunch(ctx->gexec, s));
+  } else {
+    if ((rc = enqueue()) != ST_OK) return rc;
+  }
   ST_CUDA(cudaMemcpyAsync(out_rgb, ctx->d_rgb, 3 * npix * nframes * sizeof(float), cudaMemcpyDeviceToHost, s));
   ST_CUDA(cudaStreamSynchronize(s));
+  const unsigned long long* cnt = ctx->h_cnt;
   const int status = cnt[st::CNT_STATUS] ? (int)cnt[st::CNT_STATUS] : ST_OK;
   if (stats) {
     float ms = 0.f;
@@ -835,8 +893,8 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
     stats->gas_samples = cnt[st::CNT_GAS];
     stats->launches = 1;
     stats->status = status;
-    stats->h2d_bytes = sizeof(TraceParams) + nframes * sizeof(st::FrameCam);
-    stats->d2h_bytes = 3 * npix * nframes * sizeof(float) + sizeof cnt;
+    stats->h2d_bytes = nframes * sizeof(st::FrameCam) + (rp->graph ? 0 : sizeof(TraceParams));
+    stats->d2h_bytes = 3 * npix * nframes * sizeof(float) + st::CNT_N * sizeof(unsigned long long);
     stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
   return status;

@@ -74,6 +74,7 @@ struct TraceParams {
   const int* n_list;         // their count (device)
   // persistent schedule
   const FrameCam* frames;    // optional per-frame cameras (device)
+  int n_frames;              // frames in the table (pixel schedule: grid z)
   int n_rays;                // rays in the queue (frames x pixels)
   int chunk_steps;
   unsigned int* queue;       // queue head (device)

@@ -53,12 +53,18 @@ __global__ void __launch_bounds__(128, ST_MINB) trace_pixel_kernel(const __grid_
   unsigned long long steps = 0, f64 = 0, gas = 0, rays = 0;
   if (i < p.width && j < p.height) {
     RayState<R> st;
-    const CamView cam{p.pos, p.Ef, p.Er, p.Eu, p.U, p.r_escape, p.nmax};
+    CamView cam{p.pos, p.Ef, p.Er, p.Eu, p.U, p.r_escape, p.nmax};
+    int base = 0;
+    if (p.frames) {  // batched track: one frame per grid z-slice
+      const FrameCam& fc = p.frames[blockIdx.z];
+      cam = CamView{fc.pos, fc.Ef, fc.Er, fc.Eu, fc.U, fc.r_escape, fc.nmax};
+      base = blockIdx.z * p.frame_stride;
+    }
     init_ray<PREC, KERR, SEM>(p, cam, i, j, st);
-    st.pix = j * p.width + i;
+    st.pix = base + j * p.width + i;
     while (!step_ray<PREC, KERR, VOL, SEM>(p, st)) {
     }
-    finish_ray<PREC, KERR, SEM>(p, st, st.pix, st.pix);
+    finish_ray<PREC, KERR, SEM>(p, st, st.pix, p.frames ? st.pix : j * p.width + i);
     steps = st.steps; f64 = st.fp64_steps; gas = st.gas; rays = 1;
   }
   flush_counters(p, steps, f64, gas, rays);
@@ -146,6 +152,7 @@ cudaError_t launch_variant(const TraceParams& p, int sched, int bx, int by, int 
     dim3 block(bx, by);
     dim3 grid((p.width + bx - 1) / bx, (p.height + by - 1) / by);
     if (p.pix_list) grid = dim3((unsigned)(((long long)p.width * p.height + 127) / 128), 1);
+    else if (p.frames) grid.z = (unsigned)(p.n_frames > 0 ? p.n_frames : 1);
     trace_pixel_kernel<PREC, KERR, VOL, SEM><<<grid, block, 0, s>>>(p);
   }
   return cudaGetLastError();

@@ -3,7 +3,9 @@
 // MLP 6 -> 256 -> 256 -> 256 -> 256 -> 6 (SiLU), 200,710 parameters.
 //   inputs  : camera KS radius r in [4, 50] M, inclination theta in [0, 90] deg,
 //             spin a in [0, 0.99], unit ray direction n in the static observer's
-//             frame (radial, polar, azimuthal axes), normalised to O(1)
+//             frame (radial, polar, azimuthal axes) within 75 degrees of the
+//             inward radial direction (the rays of a camera looking at the
+//             hole), normalised to O(1)
 //   outputs : exit-direction residual (3) over the ray's initial coordinate
 //             direction, first equatorial-crossing radius as 10/s - 1 (a ray
 //             that never crosses is the s -> inf limit, -1), redshift g - 1
@@ -333,8 +335,11 @@ __global__ void label_kernel(const LabelParams lp) {
   const double r = 4.0 + 46.0 * u0;
   const double th = 1.5707963267948966 * u1;
   const double a = 0.99 * u2;
-  const double nz = 2.0 * u3 - 1.0, ph = 6.283185307179586 * u4, sr = sqrt(fmax(1.0 - nz * nz, 0.0));
-  const double nv[3] = {sr * cos(ph), sr * sin(ph), nz};
+  // directions uniform on the 75-degree cap around the inward radial axis:
+  // every camera that looks at the hole sees its whole frame inside it
+  const double cmin = 0.25881904510252074;  // cos 75 deg
+  const double ca = 1.0 - u3 * (1.0 - cmin), sa = sqrt(fmax(1.0 - ca * ca, 0.0)), ph = 6.283185307179586 * u4;
+  const double nv[3] = {-ca, sa * cos(ph), sa * sin(ph)};
   const double M = 1.0;
   const double pos[3] = {sqrt(r * r + a * a) * sin(th), 0.0, r * cos(th)};
   double e1[3], e2[3], e3[3], U[4], E1[4], E2[4], E3[4];
@@ -453,43 +458,46 @@ __global__ void sur_inputs_kernel(const __grid_constant__ TraceParams p, const _
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= npix) return;
   const int i = pix % p.width, j = pix / p.width;
+  // FP32 construction (the network input is float; GB300's FP64 rate would
+  // make an FP64 pass over every pixel cost more than the network)
   RayState<float> st;
   const CamView cam{p.pos, p.Ef, p.Er, p.Eu, p.U, p.r_escape, p.nmax};
-  init_ray<ST_PREC_FP32_GUARDED, KERR, ST_SEM_DRAFT>(p, cam, i, j, st);
-  double y[6];
-#pragma unroll
-  for (int k = 0; k < 6; ++k) y[k] = (double)st.y[k] + (double)st.lo[k];
-  const double pt = (double)st.pt, a = p.a, M = p.M;
-  double L[3], fk;
+  init_ray<ST_PREC_FP32, KERR, ST_SEM_DRAFT>(p, cam, i, j, st);
+  const float* y = st.y;
+  const float pt = st.pt, a = (float)p.a, M = (float)p.M;
+  float L[3], fk;
   if (KERR) {
-    const double r2 = fmax(ks_r2(y[0], y[1], y[2], a), 1e-12), r = sqrt(r2), ira = 1.0 / (r2 + a * a);
+    const float r2 = fmaxf(ks_r2(y[0], y[1], y[2], a), 1e-12f), r = sqrtf(r2), ira = 1.f / (r2 + a * a);
     L[0] = (r * y[0] + a * y[1]) * ira;
     L[1] = (r * y[1] - a * y[0]) * ira;
     L[2] = y[2] / r;
-    fk = 2.0 * M * r2 * r / (r2 * r2 + a * a * y[2] * y[2]);
+    fk = 2.f * M * r2 * r / (r2 * r2 + a * a * y[2] * y[2]);
   } else {
-    const double r = sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+    const float r = sqrtf(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
     L[0] = y[0] / r; L[1] = y[1] / r; L[2] = y[2] / r;
-    fk = 2.0 * M / r;
+    fk = 2.f * M / r;
   }
-  const double ell = -pt + L[0] * y[3] + L[1] * y[4] + L[2] * y[5];
-  const double q[4] = {-pt + fk * ell, y[3] - fk * ell * L[0], y[4] - fk * ell * L[1], y[5] - fk * ell * L[2]};
-  auto dot4 = [&](const double* c) { return q[0] * c[0] + q[1] * c[1] + q[2] * c[2] + q[3] * c[3]; };
-  const double al = fabs(dot4(f.Ul));
-  const float n[3] = {(float)(dot4(f.E1l) / al), (float)(dot4(f.E2l) / al), (float)(dot4(f.E3l) / al)};
+  const float ell = -pt + L[0] * y[3] + L[1] * y[4] + L[2] * y[5];
+  const float q[4] = {-pt + fk * ell, y[3] - fk * ell * L[0], y[4] - fk * ell * L[1], y[5] - fk * ell * L[2]};
+  auto dot4 = [&](const double* c) {
+    return q[0] * (float)c[0] + q[1] * (float)c[1] + q[2] * (float)c[2] + q[3] * (float)c[3];
+  };
+  const float al = fabsf(dot4(f.Ul));
+  const float n[3] = {dot4(f.E1l) / al, dot4(f.E2l) / al, dot4(f.E3l) / al};
   float x[6];
   normalise_inputs((float)f.r, (float)f.th, (float)a, n, x);
 #pragma unroll
   for (int k = 0; k < NIN; ++k) X[(size_t)pix * NIN + k] = x[k];
-  const double qn = sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-  aux[pix] = make_float4((float)(q[1] / qn), (float)(q[2] / qn), (float)(q[3] / qn), st.scam);
+  const float qn = sqrtf(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  aux[pix] = make_float4(q[1] / qn, q[2] / qn, q[3] / qn, st.scam);
   int fl = st.flags & (ST_RAY_BCAPT | ST_RAY_GRAZE);
   if (!KERR) {
     // Schwarzschild critical band: b = |x cross p| / E against 3 sqrt(3) M
-    const double Lx = y[1] * y[5] - y[2] * y[4], Ly = y[2] * y[3] - y[0] * y[5], Lz = y[0] * y[4] - y[1] * y[3];
-    const double b = sqrt(Lx * Lx + Ly * Ly + Lz * Lz) / fabs(pt);
-    if (b < p.b_crit) fl |= ST_RAY_BCAPT;
-    if (fabs(b - p.b_crit) < fmax(p.crit_band, 0.05)) fl |= ST_RAY_GRAZE;
+    const float Lx = y[1] * y[5] - y[2] * y[4], Ly = y[2] * y[3] - y[0] * y[5], Lz = y[0] * y[4] - y[1] * y[3];
+    const float b = sqrtf(Lx * Lx + Ly * Ly + Lz * Lz) / fabsf(pt);
+    const float bc = (float)p.b_crit;
+    if (b < bc) fl |= ST_RAY_BCAPT;
+    if (fabsf(b - bc) < fmaxf((float)p.crit_band, 0.05f)) fl |= ST_RAY_GRAZE;
   }
   aflags[pix] = fl;
 }

@@ -73,7 +73,8 @@ def test_gradients_match_fp64(sur):
 
 def _oracle_exit(r, th, a, nvec):
     """Exit direction of one label ray from the oracle's fixed-step FP64 twin
-    (kernel rules), posed as a 1x1 fisheye camera with a 180 deg edge angle."""
+    (kernel rules), posed as a 1x1 fisheye camera with a 180 deg edge angle
+    looking along the radial axis."""
     pos = np.array([math.sqrt(r * r + a * a) * math.sin(th), 0.0, r * math.cos(th)])
     rr = np.linalg.norm(pos)
     ct = pos[2] / rr
