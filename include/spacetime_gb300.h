@@ -147,6 +147,11 @@ typedef struct {
   int graph;                 /* st_render_frames: capture the device work in a
                                 CUDA graph and replay it while the frame count,
                                 sizes and rules are unchanged */
+  int order;                 /* integrator, render_draft_mtl's `order`: 4 = RK4,
+                                45 / 46 = adaptive Tsitouras 5(4) capped at the
+                                radius-adaptive step / free up to 50 dt
+                                (DRAFT, FP32 or FP64, pixel schedule) */
+  double tol;                /* adaptive tolerance (`tol`, default 1e-4) */
 } st_render_params;
 
 typedef struct {

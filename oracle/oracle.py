@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libst_oracle.so")
 
 SEM_RENDER, SEM_DRAFT = 0, 1
-INT_RK4, INT_TSIT5 = 0, 1
+INT_RK4, INT_TSIT5, INT_TSIT5_K45, INT_TSIT5_K46 = 0, 1, 2, 3
 EMIT_KEPLER, EMIT_KS_EXACT = 0, 1
 RAY_ESCAPED, RAY_CAPTURED, RAY_BUDGET, RAY_BLACK, RAY_CROSSED, RAY_GRAZE, RAY_BCAPT = 1, 2, 4, 8, 16, 32, 64
 
@@ -44,7 +44,7 @@ class OrcScene(C.Structure):
         ("semantics", C.c_int), ("integrator", C.c_int), ("dt", C.c_double), ("nmax", C.c_int),
         ("r_escape", C.c_double), ("tspan", C.c_double), ("hstep_coef", C.c_double),
         ("hstep_cap", C.c_double), ("rtol", C.c_double), ("atol", C.c_double), ("relativistic", C.c_int),
-        ("exit_landing", C.c_int),
+        ("exit_landing", C.c_int), ("tol", C.c_double),
     ]
 
 
@@ -182,7 +182,7 @@ class Scene:
     def __init__(self, *, cam, M, a, sky, width, height, semantics, integrator, dt=0.02, nmax=0,
                  r_escape=0.0, tspan=0.0, disc=None, emitter=EMIT_KEPLER, lut=None, volume=None,
                  relativistic=False, exit_landing=None, ju=None, jv=None, rtol=1e-10, atol=1e-12,
-                 rect=None):
+                 rect=None, tol=1e-4):
         s = OrcScene()
         s.pos[:] = list(map(float, cam.pos))
         s.fwd[:] = list(map(float, cam.fwd))
@@ -250,6 +250,7 @@ class Scene:
         s.nmax = nmax
         s.hstep_coef, s.hstep_cap = 0.16, 8.0
         s.rtol, s.atol = rtol, atol
+        s.tol = tol
         s.relativistic = int(relativistic)
         self.s = s
 

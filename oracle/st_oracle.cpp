@@ -309,6 +309,7 @@ struct Scene {
   double r_isco, E_isco, L_isco;
   double hcoef, hcap;
   bool draft, tsit5, disc_on, vol_on, kepler;
+  int ksteps;  // 0, or 45 / 46: the kernel's adaptive twin
   double ds_gas, vol_rb2;
   int nmax;
 };
@@ -733,6 +734,7 @@ void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
   int rhs_evals = 1;
   int steps = 0;
   double h_carry = -1.0;
+  double kerr_prev = 1e-4;   // kernel twin: previous accepted error (PI)
   // RENDER boundary function (r - 2.00001)(r_max - r) and its sign at launch
   auto gb = [&](const double* st) { const double r = rnorm(st); return (r - 2.00001) * (s->r_escape - r); };
   const double gb0 = gb(y);
@@ -786,7 +788,33 @@ void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
 
     double yn[6], kn[6];
     double h_used = h;
-    if (!S.tsit5) {
+    if (S.ksteps) {
+      // src/metal.jl:1278-1381 restated in double
+      double hmax = h;
+      if (S.ksteps == 46) {
+        hmax = 50.0 * s->dt;
+        if (S.disc_on && !S.vol_on) hmax = std::min(hmax, std::max(h, 0.5 * (r - s->disc_outer)));
+      }
+      double hh = std::min(h_carry > 0.0 ? h_carry : h, hmax);
+      const double pn = std::sqrt(y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
+      const double sc = std::max(s->tol * (1.0 + std::max(r, pn)), 1e-30);
+      for (int att = 0; att < 4; ++att) {
+        double e[6];
+        tsit5_step(P, y, pt, hh, k1, yn, kn, e);
+        rhs_evals += 6;
+        h_used = hh;
+        const double ex = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+        const double ep = std::sqrt(e[3] * e[3] + e[4] * e[4] + e[5] * e[5]);
+        const double err = std::max(ex, ep) / sc;  // e carries the factor h already
+        if (err <= 1.0 || hh <= 1e-4 * s->dt) {
+          const double g = err > 1e-12 ? 0.9 * std::exp(-0.14 * std::log(err) + 0.08 * std::log(kerr_prev)) : 4.0;
+          h_carry = std::min(hh * clampd(g, 0.2, 4.0), hmax);
+          kerr_prev = std::max(err, 1e-4);
+          break;
+        }
+        hh = std::max(hh * std::max(0.9 * std::exp(-0.2 * std::log(err)), 0.2), 1e-4 * s->dt);
+      }
+    } else if (!S.tsit5) {
       rk4_step(P, y, pt, h, k1, yn);
       rhs_evals += 3;
     } else {
@@ -816,7 +844,7 @@ void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
 
     auto step_from = [&](double hx, double* out) {
       if (S.tsit5) { double kx[6], ex[6]; tsit5_step(P, y, pt, hx, k1, out, kx, ex); }
-      else rk4_step(P, y, pt, hx, k1, out);
+      else rk4_step(P, y, pt, hx, k1, out);  // the kernel lands with RK4 in every mode
     };
 
     if (!S.draft) {
@@ -887,7 +915,7 @@ void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
       }
     }
     for (int c = 0; c < 6; ++c) y[c] = yn[c];
-    if (S.tsit5) { for (int c = 0; c < 6; ++c) k1[c] = kn[c]; }
+    if (S.tsit5 || S.ksteps) { for (int c = 0; c < 6; ++c) k1[c] = kn[c]; }
     else { P.rhs(y, pt, k1); rhs_evals += 1; }
     ++steps;
   }
@@ -939,6 +967,7 @@ int orc_render(const orc_scene* s, float* out_rgb, orc_ray* rays, int nthreads) 
   S.hcoef = s->hstep_coef; S.hcap = s->hstep_cap;
   S.draft = s->semantics == ORC_SEM_DRAFT;
   S.tsit5 = s->integrator == ORC_INT_TSIT5;
+  S.ksteps = s->integrator == ORC_INT_TSIT5_K45 ? 45 : (s->integrator == ORC_INT_TSIT5_K46 ? 46 : 0);
   S.vol_on = S.draft && s->vol_on && s->vol != nullptr;
   S.disc_on = s->disc_on && s->disc_inner > 0.0 && s->disc_outer > s->disc_inner && s->bb_lut;
   S.kepler = s->emitter == ORC_EMIT_KEPLER;

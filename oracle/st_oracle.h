@@ -35,7 +35,10 @@ extern "C" {
 #endif
 
 enum { ORC_SEM_RENDER = 0, ORC_SEM_DRAFT = 1 };
-enum { ORC_INT_RK4 = 0, ORC_INT_TSIT5 = 1 };
+enum { ORC_INT_RK4 = 0, ORC_INT_TSIT5 = 1,
+       /* twins of the kernel's own adaptive modes (render_draft_mtl order 45 / 46,
+        * src/metal.jl:1278-1381): same controller, same step caps */
+       ORC_INT_TSIT5_K45 = 2, ORC_INT_TSIT5_K46 = 3 };
 enum { ORC_EMIT_KEPLER = 0, ORC_EMIT_KS_EXACT = 1 };
 
 /* per-ray outcome flags */
@@ -94,6 +97,7 @@ typedef struct {
   double rtol, atol;
   int relativistic;
   int exit_landing;        /* land exactly on r_escape (DRAFT) */
+  double tol;              /* kernel-twin adaptive tolerance */
 } orc_scene;
 
 typedef struct {

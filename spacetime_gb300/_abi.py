@@ -72,6 +72,7 @@ class StRenderParams(C.Structure):
         ("r_guard", C.c_double), ("crit_band", C.c_double), ("crit_r", C.c_double), ("renorm_every", C.c_int),
         ("surrogate", C.c_int), ("surrogate_sigma", C.c_double),
         ("block_x", C.c_int), ("block_y", C.c_int), ("chunk_steps", C.c_int), ("graph", C.c_int),
+        ("order", C.c_int), ("tol", C.c_double),
     ]
 
 

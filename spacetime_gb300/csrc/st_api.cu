@@ -355,6 +355,11 @@ int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, 
     if (a != 0.0) return ST_EUNSUPPORTED;
     if (ctx->vol_on) return ST_EUNSUPPORTED;
   }
+  const int order = rp->order == 0 ? 4 : rp->order;
+  if (order != 4 && order != 45 && order != 46) return ST_EINVAL;
+  if (order != 4 && (rp->semantics != ST_SEM_DRAFT || rp->precision == ST_PREC_FP32_GUARDED ||
+                     rp->schedule == ST_SCHED_PERSISTENT))
+    return ST_EUNSUPPORTED;
   if (rp->surrogate) {
     if (!ctx->sur) return ST_ESTATE;
     if (rp->semantics != ST_SEM_DRAFT || rp->samples != 1 || ctx->vol_on) return ST_EUNSUPPORTED;
@@ -383,6 +388,8 @@ int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, 
   p->dt = rp->dt;
   p->hcoef = 0.16;
   p->hcap = 8.0;
+  p->order = order;
+  p->tol = rp->tol > 0.0 ? rp->tol : 1e-4;
   p->relativistic = rp->relativistic ? 1 : 0;
   if (rp->semantics == ST_SEM_DRAFT) {
     // src/metal.jl:2058-2062: r_escape = 2 max(|pos|, 15M) (Float32);
@@ -575,7 +582,8 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
   const int status = cnt[st::CNT_STATUS] ? (int)cnt[st::CNT_STATUS] : ST_OK;
   if (stats) {
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    // a failed query must not leave an error pending for the next launch check
+    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) != cudaSuccess) { (void)cudaGetLastError(); ms = 0.f; }
     std::memset(stats, 0, sizeof(*stats));
     stats->kernel_ms = ms;
     stats->rays = cnt[st::CNT_RAYS];
@@ -652,6 +660,8 @@ void st_render_params_default(st_render_params* p, int semantics) {
   p->renorm_every = 64;
   p->surrogate_sigma = 1e-4;
   p->chunk_steps = 32;
+  p->order = 4;
+  p->tol = 1e-4;
   if (semantics == ST_SEM_RENDER) {
     // render(...; width=400, height=200, samples=1): FP64 like the CPU path
     p->width = 400; p->height = 200;
@@ -781,6 +791,7 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
                      const st_render_params* rp, float* out_rgb, st_stats* stats) {
   if (!ctx || nframes <= 0 || !cams || !stp || !rp || !out_rgb) return ST_EINVAL;
   if (rp->semantics != ST_SEM_DRAFT || rp->samples != 1 || rp->surrogate) return ST_EUNSUPPORTED;
+  if (rp->order != 0 && rp->order != 4 && rp->schedule == ST_SCHED_PERSISTENT) return ST_EUNSUPPORTED;
   const auto t0 = std::chrono::steady_clock::now();
   TraceParams p;
   st::Variant v;
@@ -844,13 +855,16 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
   v.sched = rp->schedule == ST_SCHED_PIXEL ? ST_SCHED_PIXEL : ST_SCHED_PERSISTENT;
   // the device work of one call: stage cameras, clear queue and counters,
   // trace all frames in one launch, pack, read the counters
-  auto enqueue = [&]() -> int {
+  // Under stream capture a plain event record only orders streams; the
+  // external flag makes it an event-record node, so replays are timed too.
+  auto enqueue = [&](bool capturing) -> int {
+    const unsigned ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     ST_CUDA(cudaMemcpyAsync(ctx->d_frames, ctx->h_frames, nframes * sizeof(st::FrameCam), cudaMemcpyHostToDevice, s));
     ST_CUDA(cudaMemsetAsync(ctx->d_counters, 0, st::CNT_N * sizeof(unsigned long long), s));
     ST_CUDA(cudaMemsetAsync(ctx->d_queue, 0, sizeof(unsigned int), s));
-    ST_CUDA(cudaEventRecord(ctx->ev0, s));
+    ST_CUDA(cudaEventRecordWithFlags(ctx->ev0, s, ev_flags));
     ST_CUDA(st::launch_trace(v, p, rp->block_x, rp->block_y, ctx->num_sms, s));
-    ST_CUDA(cudaEventRecord(ctx->ev1, s));
+    ST_CUDA(cudaEventRecordWithFlags(ctx->ev1, s, ev_flags));
     ST_CUDA(st::launch_pack_rgb(ctx->d_fb, ctx->d_rgb, (int)(npix * nframes), s));
     ST_CUDA(cudaMemcpyAsync(ctx->h_cnt, ctx->d_counters, st::CNT_N * sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost, s));
@@ -864,7 +878,7 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
       if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
       cudaGraph_t g = nullptr;
       ST_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      const int erc = enqueue();
+      const int erc = enqueue(true);
       const cudaError_t ec = cudaStreamEndCapture(s, &g);
       if (erc != ST_OK || ec != cudaSuccess) { if (g) cudaGraphDestroy(g); return ST_ECUDA; }
       const cudaError_t ei = cudaGraphInstantiate(&ctx->gexec, g, 0);
@@ -876,7 +890,7 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
     }
     ST_CUDA(cudaGraphLaunch(ctx->gexec, s));
   } else {
-    if ((rc = enqueue()) != ST_OK) return rc;
+    if ((rc = enqueue(false)) != ST_OK) return rc;
   }
   ST_CUDA(cudaMemcpyAsync(out_rgb, ctx->d_rgb, 3 * npix * nframes * sizeof(float), cudaMemcpyDeviceToHost, s));
   ST_CUDA(cudaStreamSynchronize(s));
@@ -884,7 +898,8 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
   const int status = cnt[st::CNT_STATUS] ? (int)cnt[st::CNT_STATUS] : ST_OK;
   if (stats) {
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    // a failed query must not leave an error pending for the next launch check
+    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) != cudaSuccess) { (void)cudaGetLastError(); ms = 0.f; }
     std::memset(stats, 0, sizeof(*stats));
     stats->kernel_ms = ms;
     stats->rays = cnt[st::CNT_RAYS];
@@ -949,6 +964,8 @@ int fill_frame_params(const st_camera* cam, const st_spacetime* stp, const st_re
   p->dt = rp->dt;
   p->hcoef = 0.16;
   p->hcap = 8.0;
+  p->order = 4;
+  p->tol = 1e-4;
   p->relativistic = rp->relativistic ? 1 : 0;
   const double re = rp->r_escape > 0.0 ? rp->r_escape : (double)(float)(2.0 * std::max(rpos, 15.0 * M));
   p->r_escape = re;

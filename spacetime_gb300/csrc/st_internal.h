@@ -46,6 +46,8 @@ struct TraceParams {
   double r_escape, tspan;
   double hcoef, hcap, dt;
   int nmax;
+  int order;                 // 4 (RK4) or 45 / 46 (adaptive Tsit5)
+  double tol;                // adaptive tolerance
   double r_isco, E_isco, L_isco;
   int relativistic, exit_landing;
   // FP32_GUARDED policy

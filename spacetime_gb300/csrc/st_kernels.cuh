@@ -34,7 +34,7 @@ __device__ __forceinline__ void flush_counters(const TraceParams& p, unsigned lo
 
 // One thread per pixel over a 2-D grid of tiles (blockDim.x * blockDim.y a
 // multiple of 32; threads are linearised so a warp covers a compact tile).
-template <int PREC, int KERR, int VOL, int SEM>
+template <int PREC, int KERR, int VOL, int SEM, int ORD = 4>
 __global__ void __launch_bounds__(128, ST_MINB) trace_pixel_kernel(const __grid_constant__ TraceParams p) {
   using R = typename RealOf<PREC>::T;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(128, ST_MINB) trace_pixel_kernel(const __grid_
     }
     init_ray<PREC, KERR, SEM>(p, cam, i, j, st);
     st.pix = base + j * p.width + i;
-    while (!step_ray<PREC, KERR, VOL, SEM>(p, st)) {
+    while (!step_ray<PREC, KERR, VOL, SEM, ORD>(p, st)) {
     }
     finish_ray<PREC, KERR, SEM>(p, st, st.pix, p.frames ? st.pix : j * p.width + i);
     steps = st.steps; f64 = st.fp64_steps; gas = st.gas; rays = 1;
@@ -153,6 +153,10 @@ cudaError_t launch_variant(const TraceParams& p, int sched, int bx, int by, int 
     dim3 grid((p.width + bx - 1) / bx, (p.height + by - 1) / by);
     if (p.pix_list) grid = dim3((unsigned)(((long long)p.width * p.height + 127) / 128), 1);
     else if (p.frames) grid.z = (unsigned)(p.n_frames > 0 ? p.n_frames : 1);
+    if constexpr (SEM == ST_SEM_DRAFT && PREC != ST_PREC_FP32_GUARDED) {
+      if (p.order == 45) { trace_pixel_kernel<PREC, KERR, VOL, SEM, 45><<<grid, block, 0, s>>>(p); return cudaGetLastError(); }
+      if (p.order == 46) { trace_pixel_kernel<PREC, KERR, VOL, SEM, 46><<<grid, block, 0, s>>>(p); return cudaGetLastError(); }
+    }
     trace_pixel_kernel<PREC, KERR, VOL, SEM><<<grid, block, 0, s>>>(p);
   }
   return cudaGetLastError();

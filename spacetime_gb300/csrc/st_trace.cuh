@@ -312,6 +312,11 @@ struct RayState {
   int nmax;      // step budget of this ray's frame
   bool inside0;  // RENDER: camera inside r = 2.00001
   bool guard_ray;
+  // adaptive Tsitouras 5(4) state (order 45/46): carried step, previous
+  // error for the PI controller, FSAL slope
+  R h_carry, err_prev;
+  R k1c[6];
+  bool k1_valid;
 };
 
 // Camera tetrad for the current ray; per-frame data lives in TraceParams for
@@ -499,6 +504,9 @@ __device__ void init_ray(const TraceParams& p, const CamView& cam, int i0, int j
   st.lambda = R(0);
   st.r_esc = R(cam.r_escape);
   st.nmax = cam.nmax;
+  st.h_carry = R(-1);
+  st.err_prev = R(1e-4);
+  st.k1_valid = false;
   st.steps = st.fp64_steps = st.gas = 0;
   st.r_cross = -1.f;
   st.g_cross = 0.f;
@@ -652,6 +660,82 @@ __device__ __forceinline__ void null_renorm(double* y, double pt, double M, doub
   if (lam > 0.9 && lam < 1.1) { y[3] *= lam; y[4] *= lam; y[5] *= lam; }
 }
 
+// Tsitouras (2011) 5(4) pair, FSAL (published tableau).
+struct Tsit5C {
+  static constexpr double A21 = 0.161;
+  static constexpr double A31 = -0.008480655492356989, A32 = 0.335480655492357;
+  static constexpr double A41 = 2.897153057105493, A42 = -6.359448489975075, A43 = 4.3622954328695815;
+  static constexpr double A51 = 5.325864828439257, A52 = -11.748883564062828, A53 = 7.4955393428898365,
+                          A54 = -0.09249506636175525;
+  static constexpr double A61 = 5.86145544294642, A62 = -12.92096931784711, A63 = 8.159367898576159,
+                          A64 = -0.071584973281401, A65 = -0.028269050394068383;
+  static constexpr double B1 = 0.09646076681806523, B2 = 0.01, B3 = 0.4798896504144996, B4 = 1.379008574103742,
+                          B5 = -3.290069515436081, B6 = 2.324710524099774;
+  static constexpr double E1 = -0.00178001105222577714, E2 = -0.0008164344596567469, E3 = 0.007880878010261995,
+                          E4 = -0.1447110071732629, E5 = 0.5823571654525552, E6 = -0.45808210592918697,
+                          E7 = 0.015151515151515152;
+};
+
+// The kernel's adaptive step (src/metal.jl:1278-1381): up to four attempts
+// from s0 with first stage k1; mixed absolute/relative error
+// max(h|e_x|, h|e_p|) / (tol (1 + max(r, |p|))), PI growth
+// 0.9 err^-0.14 err_prev^0.08 in [0.2, 4], shrink 0.9 err^-0.2 >= 0.2.
+// Writes the accepted (or last) state to sn, the FSAL slope to k7; returns
+// the step taken.
+template <int KERR, typename R>
+__device__ __forceinline__ R tsit5_adaptive(const R* s0, R pt, R M, R a, R r, R hstart, R hmax, R tol, R dt,
+                                           const R* k1, R* sn, R* k7, R& h_carry, R& err_prev) {
+  using C = Tsit5C;
+  R hh = min_(h_carry > R(0) ? h_carry : hstart, hmax);
+  R h_used = hh;
+  const R pn = sqrt_(s0[3] * s0[3] + s0[4] * s0[4] + s0[5] * s0[5]);
+  const R sc = max_(tol * (R(1) + max_(r, pn)), R(1e-30));
+#pragma unroll 1
+  for (int att = 0; att < 4; ++att) {
+    R k2[6], k3[6], k4[6], k5[6], k6[6], t[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) t[i] = s0[i] + hh * (R(C::A21) * k1[i]);
+    rhs<KERR>(t, pt, M, a, k2);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) t[i] = s0[i] + hh * (R(C::A31) * k1[i] + R(C::A32) * k2[i]);
+    rhs<KERR>(t, pt, M, a, k3);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) t[i] = s0[i] + hh * (R(C::A41) * k1[i] + R(C::A42) * k2[i] + R(C::A43) * k3[i]);
+    rhs<KERR>(t, pt, M, a, k4);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+      t[i] = s0[i] + hh * (R(C::A51) * k1[i] + R(C::A52) * k2[i] + R(C::A53) * k3[i] + R(C::A54) * k4[i]);
+    rhs<KERR>(t, pt, M, a, k5);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+      t[i] = s0[i] + hh * (R(C::A61) * k1[i] + R(C::A62) * k2[i] + R(C::A63) * k3[i] + R(C::A64) * k4[i] +
+                           R(C::A65) * k5[i]);
+    rhs<KERR>(t, pt, M, a, k6);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+      sn[i] = s0[i] + hh * (R(C::B1) * k1[i] + R(C::B2) * k2[i] + R(C::B3) * k3[i] + R(C::B4) * k4[i] +
+                            R(C::B5) * k5[i] + R(C::B6) * k6[i]);
+    rhs<KERR>(sn, pt, M, a, k7);
+    h_used = hh;
+    R e[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+      e[i] = R(C::E1) * k1[i] + R(C::E2) * k2[i] + R(C::E3) * k3[i] + R(C::E4) * k4[i] + R(C::E5) * k5[i] +
+             R(C::E6) * k6[i] + R(C::E7) * k7[i];
+    const R ex = hh * sqrt_(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+    const R ep = hh * sqrt_(e[3] * e[3] + e[4] * e[4] + e[5] * e[5]);
+    const R err = max_(ex, ep) / sc;
+    if (err <= R(1) || hh <= R(1e-4) * dt) {
+      const R g = err > R(1e-12) ? R(0.9) * exp_(R(-0.14) * log_(err) + R(0.08) * log_(err_prev)) : R(4);
+      h_carry = min_(hh * clamp_(g, R(0.2), R(4)), hmax);
+      err_prev = max_(err, R(1e-4));
+      break;
+    }
+    hh = max_(hh * max_(R(0.9) * exp_(R(-0.2) * log_(err)), R(0.2)), R(1e-4) * dt);
+  }
+  return h_used;
+}
+
 // FP64 guard step on the float-float state.
 template <int KERR>
 __device__ __forceinline__ void guard_step_fp64(float* y, float* lo, float pt, double M, double a, float h) {
@@ -687,7 +771,7 @@ __device__ __forceinline__ void renorm_fp64(float* y, float* lo, float pt, doubl
 // One integration step for the variant; returns true when the ray is done.
 // Mirrors the step loop of src/metal.jl:1201-1572 (DRAFT) and the callback
 // structure of src/raytrace.jl:339-373 (RENDER).
-template <int PREC, int KERR, int VOL, int SEM>
+template <int PREC, int KERR, int VOL, int SEM, int ORD = 4>
 __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename RealOf<PREC>::T>& st) {
   using R = typename RealOf<PREC>::T;
   const R M = R(p.M), a = R(p.a);
@@ -738,14 +822,36 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
 #pragma unroll
   for (int k = 0; k < 6; ++k) yp[k] = y[k];
   R k1[6];
-  rhs<KERR>(y, st.pt, M, a, k1);
+  if constexpr (ORD == 45 || ORD == 46) {
+    if (st.k1_valid) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) k1[k] = st.k1c[k];
+    } else {
+      rhs<KERR>(y, st.pt, M, a, k1);
+    }
+  } else {
+    rhs<KERR>(y, st.pt, M, a, k1);
+  }
 
   bool fp64_step = false;
   if constexpr (PREC == ST_PREC_FP32_GUARDED) {
     fp64_step = (st.guard_ray && (p.crit_r2 <= 0.0 || rk2 < R(p.crit_r2))) ||
                 (!(st.flags & ST_RAY_BCAPT) && rk2 < R(p.r_guard2));
   }
-  if (fp64_step) {
+  if constexpr (ORD == 45 || ORD == 46) {
+    // adaptive Tsit5 (src/metal.jl:1278-1381); 45 caps the step at the
+    // radius-adaptive h, 46 runs free up to 50 dt with the thin-disc approach guard
+    R hmax = h;
+    if constexpr (ORD == 46) {
+      hmax = R(50) * R(p.dt);
+      if (!VOL && p.disc_on) hmax = min_(hmax, max_(h, R(0.5) * (r - R(p.disc_outer))));
+    }
+    R sn[6], k7[6];
+    h = tsit5_adaptive<KERR>(yp, st.pt, M, a, r, h, hmax, R(p.tol), R(p.dt), k1, sn, k7, st.h_carry, st.err_prev);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) { y[k] = sn[k]; st.k1c[k] = k7[k]; }
+    st.k1_valid = true;
+  } else if (fp64_step) {
     if constexpr (PREC == ST_PREC_FP32_GUARDED) {
       guard_step_fp64<KERR>(y, st.lo, st.pt, p.M, p.a, h);
       ++st.fp64_steps;

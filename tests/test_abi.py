@@ -54,6 +54,7 @@ int main(void) {
   O(st_camera, focus_dist) O(st_camera, projection) O(st_disc, emitter) O(st_volume, march_stride)
   O(st_render_params, seed) O(st_render_params, chunk_steps) O(st_render_params, surrogate_sigma)
   O(st_stats, d2h_bytes) O(st_ray_diag, flags) O(st_ray_diag, fp64_steps)
+  O(st_render_params, graph) O(st_render_params, order) O(st_render_params, tol)
   return 0;
 }
 """

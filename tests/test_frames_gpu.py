@@ -8,6 +8,8 @@ import pytest
 from oracle import oracle as O
 from spacetime_gb300 import _abi, autotune, workloads
 from spacetime_gb300.api import Context
+from spacetime_gb300.scene import lens_fov
+from spacetime_gb300.ship import free_fall_track
 
 from .helpers import compare, gpu_render, oracle_scene
 
@@ -54,7 +56,11 @@ def test_interior_frames_match_twin(built_lib, track, sky):
     """The last frames sit inside the horizon (r < 2M): rays leave through it,
     the floor is 0.3M, the tetrad is the 2.5M free-faller, boosted."""
     w = track
-    for cam in w.cams[-2:]:
+    inside = [c for c in w.cams if np.linalg.norm(c.pos) < 2.0]
+    assert inside, "the track ends inside the horizon"
+    # two more, released from rest at 3M, at r ~ 1.9M and ~1.0M
+    inside += [c for c in free_fall_track(3.0, 1.0, 5, M=1.0, incl_deg=85.0, fov=lens_fov(24.0))[-2:]]
+    for cam in inside:
         assert np.linalg.norm(cam.pos) < 2.0
         one = workloads.Workload("interior", w.bh, cam, 48, 27, _abi.ST_SEM_DRAFT, w.disc, w.emitter,
                                  params=dict(samples=1, pixel_jitter=0, exit_landing=1, nmax=20000))

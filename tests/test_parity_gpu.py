@@ -93,3 +93,21 @@ def test_persistent_schedule_matches_pixel(built_lib, sky):
     assert b.stats["status"] == _abi.ST_OK
     assert a.stats["steps"] == b.stats["steps"]
     np.testing.assert_array_equal(a.image, b.image)
+
+
+@pytest.mark.parametrize("order,twin", [(45, O.INT_TSIT5_K45), (46, O.INT_TSIT5_K46)])
+def test_adaptive_tsit5_modes_fp64_vs_twin(built_lib, sky, order, twin):
+    """render_draft_mtl(...; order=45/46): the kernel's adaptive Tsitouras 5(4)
+    with FSAL and PI control, against the oracle's restatement of the same
+    controller (src/metal.jl:1278-1381)."""
+    w = workloads.config1_thin().scaled(160, 90)
+    w.params = dict(samples=1, pixel_jitter=0, exit_landing=1)
+    g = gpu_render(w, sky, FP64, order=order, tol=1e-6)
+    ref, rays = oracle_scene(w, sky, twin, tol=1e-6).render()
+    c = compare(g.image, g.diag, ref, rays)
+    assert c["class_mismatch"] <= max(2, 2e-3 * c["n"]), c
+    assert c["dir_median"] <= 1e-9 and c["rad_p99"] <= 1e-5, c
+    # and it is a converged integrator: against the oracle's Tsit5 at rtol 1e-10
+    ts, ts_rays = oracle_scene(w, sky, O.INT_TSIT5).render()
+    c2 = compare(g.image, g.diag, ts, ts_rays)
+    assert c2["dir_median"] <= 1e-6, c2
