@@ -224,9 +224,10 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams,
  * No counterpart in the reference.  A 6 -> 256x4 -> 6 SiLU MLP (200,710
  * parameters) mapping (camera r in [4,50] M, inclination in [0,90] deg, spin
  * a in [0,0.99], unit ray direction in the static observer's radial / polar /
- * azimuthal frame) to the exit-direction residual over the initial coordinate
- * direction (3), the first equatorial-crossing radius, the redshift there and
- * the log-variance of the direction error.  Hidden layers run on the tensor
+ * azimuthal frame) to the exit direction as two angles in the ray's own
+ * plane (in-plane deflection from the launch direction, out-of-plane tilt; the
+ * third direction output is unused), the first equatorial-crossing radius,
+ * the redshift there and the log-variance of the angles.  Hidden layers run on the tensor
  * cores in BF16 with FP32 accumulation; training runs on the GPU.
  * With st_context_set_surrogate and p.surrogate = 1, st_render serves camera
  * rays the gate accepts (predicted std-dev < p.surrogate_sigma, not near the
@@ -241,11 +242,13 @@ int st_surrogate_set_params(st_surrogate* s, const float* host_params);
 /* normalised inputs x[n][6] -> outputs out[n][6] */
 int st_surrogate_forward(st_surrogate* s, const float* x, int n, float* out);
 /* loss (total, direction MSE, radius MSE, g MSE) and parameter gradient of
- * targets t[n][8] = (residual 3, radius, g-1, direction mask, crossing mask, 0) */
+ * targets t[n][8] = (in-plane deflection, out-of-plane tilt, 0, radius, g-1,
+ * direction mask, crossing mask, 0) */
 int st_surrogate_loss_grad(st_surrogate* s, const float* x, const float* t, int n, float* loss4, float* grad);
 /* n FP64-labelled Sobol samples kept on the device as the training set;
- * host copies are optional (raw[n][12] = r, theta, a, n0, n1, n2, flags,
- * steps, exit direction (3), first crossing radius or -1) */
+ * host copies are optional (raw[n][15] = r, theta, a, n0, n1, n2, flags,
+ * steps, exit direction (3), first crossing radius or -1, launch coordinate
+ * direction (3)) */
 int st_surrogate_generate(st_surrogate* s, long long n, long long sobol_offset, double dt, float* host_x,
                           float* host_t, float* host_raw);
 /* AdamW steps over the generated set; loss_hist[steps] optional */

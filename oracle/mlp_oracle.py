@@ -4,8 +4,8 @@ TEST INFRASTRUCTURE ONLY: the checker for the CUDA training kernels in
 spacetime_gb300/csrc/st_surrogate.cu.  Same parameter layout and loss:
     6 -> 256 -> 256 -> 256 -> 256 -> 6, SiLU, flat parameter vector
     [W0(256x6) b0 W1(256x256) b1 W2 b2 W3 b3 W4(6x256) b4]
-    loss = mean_b md (0.5 |o[:3]-t[:3]|^2 e^-s + 1.5 s) + (o3-t3)^2 + mc (o4-t4)^2
-    with s = o5 clamped to [-30, 12].
+    loss = mean_b md (0.5 |o[:2]-t[:2]|^2 e^-s + s) + (o3-t3)^2 + mc (o4-t4)^2
+    with s = o5 clamped to [-30, 12]; o2 is unused (no gradient).
 """
 from __future__ import annotations
 
@@ -65,16 +65,16 @@ def loss_grad(P, X, T):
     s_raw = out[:, 5]
     s = np.clip(s_raw, -30.0, 12.0)
     es = np.exp(-s)
-    e = out[:, :3] - T[:, :3]
+    e = out[:, :2] - T[:, :2]
     e2 = (e * e).sum(1)
     er = out[:, 3] - T[:, 3]
     eg = out[:, 4] - T[:, 4]
-    tot = md * (0.5 * e2 * es + 1.5 * s) + er * er + mc * eg * eg
+    tot = md * (0.5 * e2 * es + s) + er * er + mc * eg * eg
     loss4 = np.array([tot.mean(), (md * e2).mean(), (er * er).mean(), (mc * eg * eg).mean()])
     d = np.zeros_like(out)
-    d[:, :3] = (md * es)[:, None] * e
+    d[:, :2] = (md * es)[:, None] * e
     inside = (s_raw > -30.0) & (s_raw < 12.0)
-    d[:, 5] = np.where(inside, md * (-0.5 * e2 * es + 1.5), 0.0)
+    d[:, 5] = np.where(inside, md * (-0.5 * e2 * es + 1.0), 0.0)
     d[:, 3] = 2.0 * er
     d[:, 4] = 2.0 * mc * eg
     d /= B

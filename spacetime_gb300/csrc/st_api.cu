@@ -250,8 +250,7 @@ static void host_static_frame(const double* pos, double M, double a, SurFrame* f
   lower(E[2], f->E3l);
   f->r = rk;
   f->th = std::acos(std::min(std::max(pos[2] / rk, -1.0), 1.0));
-  f->cphi = cp;
-  f->sphi = sp;
+  for (int k = 0; k < 3; ++k) f->xh[k] = pos[k] / rr;
 }
 
 // splitmix64 for the host-side pass shuffles

@@ -95,10 +95,12 @@ struct Variant {
 
 // Surrogate frame constants: the static observer's frame at the camera,
 // lowered (covariant) so g(q, E) is a plain dot product, and the camera's
-// azimuth rotation of the network's azimuth-0 frame.
+// unit position, which with each ray's launch direction spans the ray plane
+// the network's angles live in.
 struct SurFrame {
   double Ul[4], E1l[4], E2l[4], E3l[4];
-  double r, th, cphi, sphi;
+  double r, th;
+  double xh[3];  // unit Cartesian position of the camera (the ray plane's first axis)
   double sigma_max;
 };
 

@@ -3,13 +3,21 @@
 // MLP 6 -> 256 -> 256 -> 256 -> 256 -> 6 (SiLU), 200,710 parameters.
 //   inputs  : camera KS radius r in [4, 50] M, inclination theta in [0, 90] deg,
 //             spin a in [0, 0.99], unit ray direction n in the static observer's
-//             frame (radial, polar, azimuthal axes) within 75 degrees of the
-//             inward radial direction (the rays of a camera looking at the
-//             hole), normalised to O(1)
-//   outputs : exit-direction residual (3) over the ray's initial coordinate
-//             direction, first equatorial-crossing radius as 10/s - 1 (a ray
-//             that never crosses is the s -> inf limit, -1), redshift g - 1
-//             there, and the log-variance of the direction error.
+//             frame (radial, polar, azimuthal axes), normalised to O(1).
+//             Training directions put 80% of the samples in the 75-degree cone
+//             around the inward radial direction (the rays of a camera looking
+//             at the hole) and 20% on the rest of the sphere.
+//   outputs : exit direction in the ray's own plane -- the plane of the unit
+//             position xh and the launch direction d0, in which a Schwarzschild
+//             ray stays: the in-plane deflection D (radians, wrapped to
+//             [-pi/2, 3pi/2)) and the out-of-plane tilt E (radians), with the
+//             third output unused; then the first equatorial-crossing radius as
+//             10/s - 1 (no crossing is the s -> inf limit, -1), redshift g - 1
+//             there, and the log-variance of the two angles.
+//             exit = cos E (cos(psi + D) xh + sin(psi + D) et) + sin E (xh x et),
+//             with psi the angle from xh to d0 and et the unit part of d0
+//             normal to xh.  For a = 0 the angles depend only on r and n . xh,
+//             so the network's work is the spin's correction, not the geometry.
 // The three 256x256 layers run on the tensor cores in BF16 with FP32
 // accumulation (st_mlp.cuh); the 6->256 and 256->6 layers, the loss and AdamW
 // run in FP32.  Master weights and optimiser state are FP32.
@@ -39,6 +47,7 @@ using mlp::EpiBackDX;
 using mlp::EpiHidden;
 
 constexpr int NIN = 6, NH = 256, NOUT = 6, NT = 8;  // NT: target floats per row
+constexpr int NRAW = 15;  // floats per optional raw label row (LabelParams::raw)
 // parameter offsets (floats)
 constexpr size_t OW0 = 0, OB0 = OW0 + NH * NIN, OW1 = OB0 + NH, OB1 = OW1 + NH * NH, OW2 = OB1 + NH,
                  OB2 = OW2 + NH * NH, OW3 = OB2 + NH, OB3 = OW3 + NH * NH, OW4 = OB3 + NH, OB4 = OW4 + NOUT * NH,
@@ -85,10 +94,11 @@ __global__ void l4_fwd(const __nv_bfloat16* __restrict__ H3, const float* __rest
   }
 }
 
-// Loss per row (targets: t0..t2 direction residual, t3 crossing radius,
-// t4 g - 1, t5 direction mask, t6 crossing mask):
-//   0.5 |o - t|^2 exp(-s) + 1.5 s   (direction, heteroscedastic, s = o5)
+// Loss per row (targets: t0, t1 the in-plane deflection and out-of-plane
+// tilt, t3 crossing radius, t4 g - 1, t5 direction mask, t6 crossing mask):
+//   0.5 |o01 - t01|^2 exp(-s) + s   (two angles, heteroscedastic, s = o5)
 //   + WR (o3 - t3)^2 + WG m (o4 - t4)^2
+// o2 is unused and carries no gradient.
 // loss_acc[0..3] += (total, direction MSE, radius MSE, g MSE) / B
 constexpr float WR = 1.0f, WG = 1.0f;
 __global__ void loss_grad(const float* __restrict__ out, const float* __restrict__ T, float* dout, float* loss_acc,
@@ -103,12 +113,13 @@ __global__ void loss_grad(const float* __restrict__ out, const float* __restrict
     const float es = __expf(-s);
     float e2 = 0.f, g[NOUT];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 2; ++k) {
       const float e = o[k] - t[k];
       e2 += e * e;
       g[k] = md * e * es;
     }
-    g[5] = (o[5] > -30.f && o[5] < 12.f) ? md * (-0.5f * e2 * es + 1.5f) : 0.f;
+    g[2] = 0.f;
+    g[5] = (o[5] > -30.f && o[5] < 12.f) ? md * (-0.5f * e2 * es + 1.f) : 0.f;
     const float er = o[3] - t[3], eg = o[4] - t[4];
     g[3] = 2.f * WR * er;
     g[4] = 2.f * WG * mc * eg;
@@ -117,7 +128,7 @@ __global__ void loss_grad(const float* __restrict__ out, const float* __restrict
     l_dir = md * e2;
     l_r = er * er;
     l_g = mc * eg * eg;
-    l_tot = md * (0.5f * e2 * es + 1.5f * s) + WR * l_r + WG * l_g;
+    l_tot = md * (0.5f * e2 * es + s) + WR * l_r + WG * l_g;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -306,12 +317,54 @@ __device__ __forceinline__ void frame_axes(const D* pos, D* e1, D* e2, D* e3) {
   e3[0] = D(0); e3[1] = D(1); e3[2] = D(0);
 }
 
+// The ray's own plane: unit position xh, the unit part et of the launch
+// direction d0 normal to xh, and en = xh x et; psi is the angle from xh to d0.
+// A (near-)radial launch has no plane; any normal serves, its deflection is 0.
+template <typename D>
+__device__ __forceinline__ void ray_plane(const D* xh, const D* d0, D* et, D* en, D* psi) {
+  const D c = xh[0] * d0[0] + xh[1] * d0[1] + xh[2] * d0[2];
+  D t[3] = {d0[0] - c * xh[0], d0[1] - c * xh[1], d0[2] - c * xh[2]};
+  D sn = sqrt_(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+  if (!(sn > D(1e-7))) {
+    // any unit normal of xh
+    const D ax = fabs_(xh[0]) < D(0.9) ? D(1) : D(0), ay = D(1) - ax;
+    const D cc = xh[0] * ax + xh[1] * ay;
+    t[0] = ax - cc * xh[0]; t[1] = ay - cc * xh[1]; t[2] = -cc * xh[2];
+    const D tn = sqrt_(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+    t[0] /= tn; t[1] /= tn; t[2] /= tn;
+  } else {
+    t[0] /= sn; t[1] /= sn; t[2] /= sn;
+  }
+  et[0] = t[0]; et[1] = t[1]; et[2] = t[2];
+  en[0] = xh[1] * t[2] - xh[2] * t[1];
+  en[1] = xh[2] * t[0] - xh[0] * t[2];
+  en[2] = xh[0] * t[1] - xh[1] * t[0];
+  *psi = atan2_(max_(sn, D(0)), c);
+}
+
+// Exit direction d -> (in-plane deflection, out-of-plane tilt); the
+// deflection is wrapped to [-pi/2, 3pi/2).
+__device__ __forceinline__ void plane_angles(const double* xh, const double* d0, const double* d, double* defl,
+                                             double* tilt) {
+  double et[3], en[3], psi;
+  ray_plane(xh, d0, et, en, &psi);
+  const double cx = d[0] * xh[0] + d[1] * xh[1] + d[2] * xh[2];
+  const double ct = d[0] * et[0] + d[1] * et[1] + d[2] * et[2];
+  const double cn = d[0] * en[0] + d[1] * en[1] + d[2] * en[2];
+  const double two_pi = 6.283185307179586;
+  double D = atan2(ct, cx) - psi;
+  D -= two_pi * floor((D + 1.5707963267948966) / two_pi);
+  *defl = D;
+  *tilt = asin(fmin(fmax(cn, -1.0), 1.0));
+}
+
 struct LabelParams {
   long long n;
   long long offset;   // Sobol index of the first sample
   float* X;           // [n][6] normalised inputs
   float* T;           // [n][8] targets
-  float* raw;         // optional [n][12]: r, theta, a, n0, n1, n2, flags, steps, exit dir (3), r_cross
+  float* raw;         // optional [n][15]: r, theta, a, n0, n1, n2, flags, steps, exit dir (3), r_cross,
+                      // launch coordinate direction d0 (3)
   double dt;
 };
 
@@ -335,10 +388,13 @@ __global__ void label_kernel(const LabelParams lp) {
   const double r = 4.0 + 46.0 * u0;
   const double th = 1.5707963267948966 * u1;
   const double a = 0.99 * u2;
-  // directions uniform on the 75-degree cap around the inward radial axis:
-  // every camera that looks at the hole sees its whole frame inside it
+  // directions: 80% uniform on the 75-degree cone around the inward radial
+  // axis (every camera that looks at the hole sees its whole frame inside it),
+  // 20% uniform on the rest of the sphere
   const double cmin = 0.25881904510252074;  // cos 75 deg
-  const double ca = 1.0 - u3 * (1.0 - cmin), sa = sqrt(fmax(1.0 - ca * ca, 0.0)), ph = 6.283185307179586 * u4;
+  const double ca = (u3 < 0.8f) ? 1.0 - (double)(u3 / 0.8f) * (1.0 - cmin)
+                                : cmin - (double)((u3 - 0.8f) / 0.2f) * (1.0 + cmin);
+  const double sa = sqrt(fmax(1.0 - ca * ca, 0.0)), ph = 6.283185307179586 * u4;
   const double nv[3] = {-ca, sa * cos(ph), sa * sin(ph)};
   const double M = 1.0;
   const double pos[3] = {sqrt(r * r + a * a) * sin(th), 0.0, r * cos(th)};
@@ -401,16 +457,9 @@ __global__ void label_kernel(const LabelParams lp) {
     }
     const double rn = sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
     if (rn > r_esc) {
-      // land on r_escape (two secant iterations), as the render path does
-      double ha = h, ra = rn, hb = (rn > rr) ? h * (r_esc - rr) / (rn - rr) : h, yt[6];
-      for (int it = 0; it < 2; ++it) {
-        rk4_inc<1>(yp, pt, M, a, hb, k1, inc);
-        for (int k = 0; k < 6; ++k) yt[k] = yp[k] + inc[k];
-        const double rb = sqrt(yt[0] * yt[0] + yt[1] * yt[1] + yt[2] * yt[2]);
-        if (it == 1 || rb == ra) break;
-        const double hn = hb + (r_esc - rb) * (hb - ha) / (rb - ra);
-        ha = hb; ra = rb; hb = hn;
-      }
+      // land on r_escape, as the render path does
+      double yt[6];
+      land_on_sphere<1>(yp, pt, M, a, h, k1, rr, rn, r_esc, yt);
       for (int k = 0; k < 6; ++k) y[k] = yt[k];
       flags |= ST_RAY_ESCAPED;
       done = true;
@@ -429,37 +478,46 @@ __global__ void label_kernel(const LabelParams lp) {
   float* Xo = lp.X + tid * NIN;
   for (int k = 0; k < NIN; ++k) Xo[k] = x[k];
   float* To = lp.T + tid * NT;
-  for (int k = 0; k < 3; ++k) To[k] = ok ? (float)(vel[k] / vl - d0[k]) : 0.f;
+  double defl = 0.0, tilt = 0.0;
+  if (ok) {
+    const double xh[3] = {pos[0] / rpos, pos[1] / rpos, pos[2] / rpos};
+    const double dex[3] = {vel[0] / vl, vel[1] / vl, vel[2] / vl};
+    plane_angles(xh, d0, dex, &defl, &tilt);
+  }
+  To[0] = (float)defl;
+  To[1] = (float)tilt;
+  To[2] = 0.f;
   To[3] = (r_cross > 0.f ? fminf(10.f / r_cross, 5.f) : 0.f) - 1.f;  // 10/s - 1; no crossing = s -> inf
   To[4] = r_cross > 0.f ? g_cross - 1.f : 0.f;
   To[5] = ok ? 1.f : 0.f;
   To[6] = r_cross > 0.f ? 1.f : 0.f;
   To[7] = 0.f;
   if (lp.raw) {
-    float* Ro = lp.raw + tid * 12;
+    float* Ro = lp.raw + tid * NRAW;
     Ro[0] = (float)r; Ro[1] = (float)th; Ro[2] = (float)a;
     Ro[3] = nf[0]; Ro[4] = nf[1]; Ro[5] = nf[2];
     Ro[6] = (float)flags; Ro[7] = (float)steps;
     Ro[8] = (float)(vel[0] / vl); Ro[9] = (float)(vel[1] / vl); Ro[10] = (float)(vel[2] / vl);
     Ro[11] = r_cross;
+    Ro[12] = (float)d0[0]; Ro[13] = (float)d0[1]; Ro[14] = (float)d0[2];
   }
 }
 
 // ---------------------------------------------------------------------------
-// Frame pass: camera rays -> network inputs -> gate
+// Frame pass: camera rays -> network inputs -> MLP -> gate, fused
 // ---------------------------------------------------------------------------
 
-// Inputs of every pixel's camera ray: the ray is built exactly as the trace
-// kernel builds it (init_ray, FP64 construction), raised to its tangent
-// q = (-p_t + f l, p - f l L), projected on the static observer's frame.
+// Network inputs of one pixel's camera ray.  The ray is built as the trace
+// kernel builds it (init_ray, in FP32: the network input is float, and an
+// FP64 pass over every pixel would cost more than the network on GB300's
+// FP64 rate), raised to its tangent q = (-p_t + f l, p - f l L) and projected
+// on the static observer's frame.  aux = (unit launch coordinate direction,
+// camera shift); fl = launch flags (Bardeen capture / graze, Schwarzschild
+// critical band).
 template <int KERR>
-__global__ void sur_inputs_kernel(const __grid_constant__ TraceParams p, const __grid_constant__ SurFrame f,
-                                  float* X, float4* aux, int* aflags, int npix) {
-  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= npix) return;
+__device__ __forceinline__ void pixel_inputs(const TraceParams& p, const SurFrame& f, int pix, float* x, float4* aux,
+                                             int* fl) {
   const int i = pix % p.width, j = pix / p.width;
-  // FP32 construction (the network input is float; GB300's FP64 rate would
-  // make an FP64 pass over every pixel cost more than the network)
   RayState<float> st;
   const CamView cam{p.pos, p.Ef, p.Er, p.Eu, p.U, p.r_escape, p.nmax};
   init_ray<ST_PREC_FP32, KERR, ST_SEM_DRAFT>(p, cam, i, j, st);
@@ -484,69 +542,228 @@ __global__ void sur_inputs_kernel(const __grid_constant__ TraceParams p, const _
   };
   const float al = fabsf(dot4(f.Ul));
   const float n[3] = {dot4(f.E1l) / al, dot4(f.E2l) / al, dot4(f.E3l) / al};
-  float x[6];
-  normalise_inputs((float)f.r, (float)f.th, (float)a, n, x);
-#pragma unroll
-  for (int k = 0; k < NIN; ++k) X[(size_t)pix * NIN + k] = x[k];
+  normalise_inputs((float)f.r, (float)f.th, a, n, x);
   const float qn = sqrtf(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-  aux[pix] = make_float4(q[1] / qn, q[2] / qn, q[3] / qn, st.scam);
-  int fl = st.flags & (ST_RAY_BCAPT | ST_RAY_GRAZE);
+  *aux = make_float4(q[1] / qn, q[2] / qn, q[3] / qn, st.scam);
+  int flags = st.flags & (ST_RAY_BCAPT | ST_RAY_GRAZE);
   if (!KERR) {
     // Schwarzschild critical band: b = |x cross p| / E against 3 sqrt(3) M
     const float Lx = y[1] * y[5] - y[2] * y[4], Ly = y[2] * y[3] - y[0] * y[5], Lz = y[0] * y[4] - y[1] * y[3];
     const float b = sqrtf(Lx * Lx + Ly * Ly + Lz * Lz) / fabsf(pt);
     const float bc = (float)p.b_crit;
-    if (b < bc) fl |= ST_RAY_BCAPT;
-    if (fabsf(b - bc) < fmaxf((float)p.crit_band, 0.05f)) fl |= ST_RAY_GRAZE;
+    if (b < bc) flags |= ST_RAY_BCAPT;
+    if (fabsf(b - bc) < fmaxf((float)p.crit_band, 0.05f)) flags |= ST_RAY_GRAZE;
   }
-  aflags[pix] = fl;
+  *fl = flags;
 }
 
-// Gate: serve a pixel from the network when it is not near the critical
-// curve, the predicted std-dev of its exit direction is below sigma_max and it
-// is predicted not to cross the disc annulus; otherwise append it (warp-
-// ordered) to the list the trace kernel integrates.
-__global__ void sur_gate_kernel(const __grid_constant__ TraceParams p, const __grid_constant__ SurFrame f,
-                                const float* __restrict__ out, const float4* __restrict__ aux,
-                                const int* __restrict__ aflags, int* list, int* count, int npix) {
-  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  bool serve = false;
-  float4 rgba = make_float4(0.f, 0.f, 0.f, 1.f);
-  double dird[3] = {0, 0, 0};
-  if (pix < npix) {
-    const float* o = out + (size_t)pix * NOUT;
-    const float sig = __expf(0.5f * fminf(fmaxf(o[5], -30.f), 12.f));
-    serve = (aflags[pix] & (ST_RAY_BCAPT | ST_RAY_GRAZE)) == 0 && sig < (float)f.sigma_max;
-    if (serve && p.disc_on) {
-      const float u = o[3] + 1.f;  // 10 / s
-      const float s = u > 0.02f ? 10.f / u : 1e9f;
-      if (s > (float)p.disc_inner - 1.5f && s < (float)p.disc_outer + 3.0f) serve = false;
-    }
-    if (serve) {
-      const float4 a4 = aux[pix];
-      const float c = (float)f.cphi, sn = (float)f.sphi;
-      const float dx = a4.x + (c * o[0] - sn * o[1]);
-      const float dy = a4.y + (sn * o[0] + c * o[1]);
-      const float dz = a4.z + o[2];
-      const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
-      const float d0 = dx * inv, d1 = dy * inv, d2 = dz * inv;
-      dird[0] = d0; dird[1] = d1; dird[2] = d2;
-      float sky[3];
-      sample_sky(p, acosf(fminf(fmaxf(d2, -1.f), 1.f)), atan2f(d1, d0), sky);
-      const float g = a4.w;
-      if (g != 1.f) {
-        sky[0] *= 57.4f / (__expf(4.067f / g) - 1.f);
-        sky[1] *= 90.2f / (__expf(4.513f / g) - 1.f);
-        sky[2] *= 206.5f / (__expf(5.335f / g) - 1.f);
-      }
-      rgba = make_float4(p.weight * sky[0], p.weight * sky[1], p.weight * sky[2], 1.f);
+// Gate of one pixel: serve it from the network when it is not near the
+// critical curve, the predicted std-dev of its exit angles is below
+// sigma_max and it is predicted not to cross the disc annulus.  A served
+// pixel gets its sky colour (exit direction rebuilt from the ray-plane
+// angles) in *rgba and its direction in dird.
+__device__ __forceinline__ bool gate_pixel(const TraceParams& p, const SurFrame& f, const float* o, float4 a4, int fl,
+                                           float4* rgba, double* dird) {
+  const float sig = __expf(0.5f * fminf(fmaxf(o[5], -30.f), 12.f));
+  bool serve = (fl & (ST_RAY_BCAPT | ST_RAY_GRAZE)) == 0 && sig < (float)f.sigma_max;
+  if (serve && p.disc_on) {
+    const float u = o[3] + 1.f;  // 10 / s
+    const float sc = u > 0.02f ? 10.f / u : 1e9f;
+    if (sc > (float)p.disc_inner - 1.5f && sc < (float)p.disc_outer + 3.0f) serve = false;
+  }
+  if (!serve) return false;
+  const float xh[3] = {(float)f.xh[0], (float)f.xh[1], (float)f.xh[2]};
+  const float dl[3] = {a4.x, a4.y, a4.z};
+  float et[3], en[3], psi;
+  ray_plane(xh, dl, et, en, &psi);
+  float sc, cc, se, ce;
+  __sincosf(psi + o[0], &sc, &cc);
+  __sincosf(o[1], &se, &ce);
+  const float dx = ce * (cc * xh[0] + sc * et[0]) + se * en[0];
+  const float dy = ce * (cc * xh[1] + sc * et[1]) + se * en[1];
+  const float dz = ce * (cc * xh[2] + sc * et[2]) + se * en[2];
+  const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
+  const float d0 = dx * inv, d1 = dy * inv, d2 = dz * inv;
+  dird[0] = d0; dird[1] = d1; dird[2] = d2;
+  float sky[3];
+  sample_sky(p, acosf(fminf(fmaxf(d2, -1.f), 1.f)), atan2f(d1, d0), sky);
+  const float g = a4.w;
+  if (g != 1.f) {
+    sky[0] *= 57.4f / (__expf(4.067f / g) - 1.f);
+    sky[1] *= 90.2f / (__expf(4.513f / g) - 1.f);
+    sky[2] *= 206.5f / (__expf(5.335f / g) - 1.f);
+  }
+  *rgba = make_float4(p.weight * sky[0], p.weight * sky[1], p.weight * sky[2], 1.f);
+  return true;
+}
+
+// One CTA = 128 pixels = 128 network rows, 8 warps; warp w owns rows
+// 16w..16w+15 through all layers.  Shared memory holds the activation tile
+// (bf16, 128 x 256) and one hidden layer's weights (bf16, 256 x 256, loaded
+// with cp.async from L2 while the previous layer's epilogue runs), so no
+// activation leaves the SM.  Hidden layers: mma.sync m16n8k16 BF16 with FP32
+// accumulate, 32 accumulator tiles per warp; the 6 -> 256 and 256 -> 6 edge
+// layers run in FP32 (the last one straight from the layer-3 accumulators,
+// rounded to bf16 as the unfused forward stores them).
+constexpr int FROWS = 128, FTHREADS = 256, FS = NH + 8;
+constexpr size_t F_SMEM = (size_t)FROWS * FS * 2      // activations
+                          + (size_t)NH * FS * 2       // one hidden layer's weights
+                          + (size_t)NOUT * NH * 4     // W4
+                          + (size_t)FROWS * NIN * 4   // inputs
+                          + (size_t)FROWS * NOUT * 4  // outputs
+                          + (size_t)FROWS * 16        // aux
+                          + (size_t)FROWS * 4;        // launch flags
+static_assert(F_SMEM <= 227 * 1024, "fused surrogate tile exceeds shared memory");
+
+__device__ __forceinline__ void load_hidden_weights(__nv_bfloat16* Ws, const __nv_bfloat16* W, int tid) {
+  // 256 rows x 32 chunks of 16 bytes
+#pragma unroll 4
+  for (int c = tid; c < NH * (NH / 8); c += FTHREADS) {
+    const int r = c >> 5, q = c & 31;
+    mlp::cp_async16(Ws + r * FS + q * 8, W + (size_t)r * NH + q * 8);
+  }
+  mlp::cp_async_commit();
+}
+
+template <int KERR>
+__global__ void __launch_bounds__(FTHREADS, 1)
+    sur_frame_kernel(const __grid_constant__ TraceParams p, const __grid_constant__ SurFrame f,
+                     const float* __restrict__ P, const __nv_bfloat16* __restrict__ W1,
+                     const __nv_bfloat16* __restrict__ W2, const __nv_bfloat16* __restrict__ W3, int* list,
+                     int* count) {
+  extern __shared__ __align__(16) unsigned char fsm[];
+  __nv_bfloat16* Hs = reinterpret_cast<__nv_bfloat16*>(fsm);
+  __nv_bfloat16* Ws = Hs + FROWS * FS;
+  float* W4s = reinterpret_cast<float*>(Ws + NH * FS);
+  float* Xs = W4s + NOUT * NH;
+  float* Os = Xs + FROWS * NIN;
+  float4* As = reinterpret_cast<float4*>(Os + FROWS * NOUT);
+  int* Fs = reinterpret_cast<int*>(As + FROWS);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // the CTA's 128 pixels are a 16 x 8 tile; each of the gating warps 0-3
+  // holds an 8 x 4 block, the warp shape of the trace kernel, so the list of
+  // pixels left to integrate keeps that coherence
+  const int tiles_x = (p.width + 15) >> 4;
+  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  int my_pix = -1;
+  if (tid < FROWS) {
+    const int wq = tid >> 5, l = tid & 31;
+    const int i = tx * 16 + (wq & 1) * 8 + (l & 7), j = ty * 8 + (wq >> 1) * 4 + (l >> 3);
+    if (i < p.width && j < p.height) my_pix = j * p.width + i;
+  }
+  load_hidden_weights(Ws, W1, tid);
+  for (int c = tid; c < NOUT * NH; c += FTHREADS) W4s[c] = P[OW4 + c];
+  if (tid < FROWS) {
+    float x[NIN] = {0, 0, 0, 0, 0, 0};
+    float4 a4 = make_float4(0.f, 0.f, 1.f, 1.f);
+    int fl = ST_RAY_GRAZE;
+    if (my_pix >= 0) pixel_inputs<KERR>(p, f, my_pix, x, &a4, &fl);
+#pragma unroll
+    for (int k = 0; k < NIN; ++k) Xs[tid * NIN + k] = x[k];
+    As[tid] = a4;
+    Fs[tid] = fl;
+  }
+  __syncthreads();
+  // layer 0 (FP32): thread = hidden unit n, all 128 rows
+  {
+    const int n = tid;
+    float w0[NIN];
+#pragma unroll
+    for (int i = 0; i < NIN; ++i) w0[i] = P[OW0 + n * NIN + i];
+    const float b0 = P[OB0 + n];
+    for (int r = 0; r < FROWS; ++r) {
+      float z = b0;
+#pragma unroll
+      for (int i = 0; i < NIN; ++i) z += Xs[r * NIN + i] * w0[i];
+      Hs[r * FS + n] = __float2bfloat16_rn(mlp::silu(z));
     }
   }
-  const unsigned want = __ballot_sync(0xffffffffu, pix < npix && !serve);
+  mlp::cp_async_wait0();
+  __syncthreads();
+  const int g = lane >> 2, t2 = (lane & 3) * 2;
+  const int row0 = warp * 16;
+  float o4[2][NOUT];
+#pragma unroll
+  for (int l = 1; l <= 3; ++l) {
+    float acc[32][4];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll 1
+    for (int kk = 0; kk < NH; kk += 16) {
+      uint32_t af[4];
+      mlp::ldsm_x4(af, Hs + (row0 + (lane & 15)) * FS + kk + (lane >> 4) * 8);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        uint32_t bfr[4];
+        mlp::ldsm_x4(bfr, Ws + (j * 16 + (lane & 7) + (lane >> 4) * 8) * FS + kk + ((lane >> 3) & 1) * 8);
+        mlp::mma_bf16(acc[2 * j], af, bfr[0], bfr[1]);
+        mlp::mma_bf16(acc[2 * j + 1], af, bfr[2], bfr[3]);
+      }
+    }
+    __syncthreads();  // every warp is done with this layer's weights
+    if (l < 3) load_hidden_weights(Ws, l == 1 ? W2 : W3, tid);
+    const float* bias = P + (l == 1 ? OB1 : l == 2 ? OB2 : OB3);
+    if (l < 3) {
+      // this warp's rows only: no other warp reads them
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int n = j * 8 + t2;
+        const float bn0 = bias[n], bn1 = bias[n + 1];
+        *reinterpret_cast<__nv_bfloat162*>(Hs + (row0 + g) * FS + n) =
+            __floats2bfloat162_rn(mlp::silu(acc[j][0] + bn0), mlp::silu(acc[j][1] + bn1));
+        *reinterpret_cast<__nv_bfloat162*>(Hs + (row0 + g + 8) * FS + n) =
+            __floats2bfloat162_rn(mlp::silu(acc[j][2] + bn0), mlp::silu(acc[j][3] + bn1));
+      }
+      mlp::cp_async_wait0();
+      __syncthreads();
+    } else {
+      // layer 4 from the accumulators: rows g and g+8 of this warp, 64 columns
+#pragma unroll
+      for (int k = 0; k < NOUT; ++k) o4[0][k] = o4[1][k] = 0.f;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int n = j * 8 + t2;
+        const float bn0 = bias[n], bn1 = bias[n + 1];
+        const float h00 = __bfloat162float(__float2bfloat16_rn(mlp::silu(acc[j][0] + bn0)));
+        const float h01 = __bfloat162float(__float2bfloat16_rn(mlp::silu(acc[j][1] + bn1)));
+        const float h10 = __bfloat162float(__float2bfloat16_rn(mlp::silu(acc[j][2] + bn0)));
+        const float h11 = __bfloat162float(__float2bfloat16_rn(mlp::silu(acc[j][3] + bn1)));
+#pragma unroll
+        for (int k = 0; k < NOUT; ++k) {
+          const float w0 = W4s[k * NH + n], w1 = W4s[k * NH + n + 1];
+          o4[0][k] += h00 * w0 + h01 * w1;
+          o4[1][k] += h10 * w0 + h11 * w1;
+        }
+      }
+    }
+  }
+  // reduce over the quad (the 4 lanes sharing rows g, g+8)
+#pragma unroll
+  for (int k = 0; k < NOUT; ++k) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      o4[h][k] += __shfl_xor_sync(0xffffffffu, o4[h][k], 1);
+      o4[h][k] += __shfl_xor_sync(0xffffffffu, o4[h][k], 2);
+    }
+  }
+  if ((lane & 3) == 0) {
+#pragma unroll
+    for (int k = 0; k < NOUT; ++k) {
+      Os[(row0 + g) * NOUT + k] = o4[0][k] + P[OB4 + k];
+      Os[(row0 + g + 8) * NOUT + k] = o4[1][k] + P[OB4 + k];
+    }
+  }
+  __syncthreads();
+  if (tid >= FROWS) return;  // warps 0-3 gate the tile (whole warps: ballots stay full)
+  const int pix = my_pix;
+  float4 rgba = make_float4(0.f, 0.f, 0.f, 1.f);
+  double dird[3] = {0, 0, 0};
+  const bool serve = pix >= 0 && gate_pixel(p, f, Os + tid * NOUT, As[tid], Fs[tid], &rgba, dird);
+  const unsigned want = __ballot_sync(0xffffffffu, pix >= 0 && !serve);
   int base = 0;
-  if ((threadIdx.x & 31) == 0 && want) base = atomicAdd(count, __popc(want));
+  if (lane == 0 && want) base = atomicAdd(count, __popc(want));
   base = __shfl_sync(0xffffffffu, base, 0);
-  if (pix >= npix) return;
+  if (pix < 0) return;
   if (serve) {
     p.out[pix] = rgba;
     if (p.diag) {
@@ -558,7 +775,7 @@ __global__ void sur_gate_kernel(const __grid_constant__ TraceParams p, const __g
       p.diag[pix] = d;
     }
   } else {
-    list[base + __popc(want & ((1u << (threadIdx.x & 31)) - 1u))] = pix;
+    list[base + __popc(want & ((1u << lane) - 1u))] = pix;
   }
 }
 
@@ -582,10 +799,6 @@ struct st_surrogate {
   __nv_bfloat16* H[4] = {nullptr, nullptr, nullptr, nullptr};
   __nv_bfloat16 *dZa = nullptr, *dZb = nullptr;
   float *out = nullptr, *dout = nullptr, *T = nullptr, *loss = nullptr;
-  // frame pass buffers (device)
-  float4* aux = nullptr;  // per pixel: initial direction (3), camera shift
-  int* aflags = nullptr;  // per pixel: ST_RAY_* launch flags
-  int aux_cap = 0;
   // training set (device)
   float *DX = nullptr, *DT = nullptr;
   long long ndata = 0;
@@ -748,7 +961,7 @@ void st_surrogate_destroy(st_surrogate* s) {
   for (int l = 0; l < 4; ++l) { cudaFree(s->Z[l]); cudaFree(s->H[l]); }
   cudaFree(s->dZa); cudaFree(s->dZb); cudaFree(s->out); cudaFree(s->dout); cudaFree(s->T);
   cudaFree(s->DX); cudaFree(s->DT);
-  cudaFree(s->aux); cudaFree(s->aflags);
+
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
 }
@@ -823,13 +1036,13 @@ int st_surrogate_generate(st_surrogate* s, long long n, long long offset, double
   if (cudaMalloc(&s->DX, (size_t)n * NIN * 4) != cudaSuccess || cudaMalloc(&s->DT, (size_t)n * NT * 4) != cudaSuccess)
     return ST_ENOMEM;
   float* raw = nullptr;
-  if (host_raw && cudaMalloc(&raw, (size_t)n * 12 * 4) != cudaSuccess) return ST_ENOMEM;
+  if (host_raw && cudaMalloc(&raw, (size_t)n * NRAW * 4) != cudaSuccess) return ST_ENOMEM;
   LabelParams lp{n, offset, s->DX, s->DT, raw, dt};
   label_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s->stream>>>(lp);
   SC(cudaGetLastError());
   if (host_x) SC(cudaMemcpyAsync(host_x, s->DX, (size_t)n * NIN * 4, cudaMemcpyDeviceToHost, s->stream));
   if (host_t) SC(cudaMemcpyAsync(host_t, s->DT, (size_t)n * NT * 4, cudaMemcpyDeviceToHost, s->stream));
-  if (raw) SC(cudaMemcpyAsync(host_raw, raw, (size_t)n * 12 * 4, cudaMemcpyDeviceToHost, s->stream));
+  if (raw) SC(cudaMemcpyAsync(host_raw, raw, (size_t)n * NRAW * 4, cudaMemcpyDeviceToHost, s->stream));
   SC(cudaStreamSynchronize(s->stream));
   cudaFree(raw);
   s->ndata = n;
@@ -877,29 +1090,11 @@ namespace st {
 // Surrogate pass of one frame on `stream` (see st_internal.h).
 int surrogate_frame(st_surrogate* s, const TraceParams& p, const Variant& v, const SurFrame& f, int* list, int* count,
                     cudaStream_t stream) {
-  const int npix = p.width * p.height;
-  const int B = pad128(npix);
-  int rc = ensure_work(s, B);
-  if (rc != ST_OK) return rc;
-  if (s->aux_cap < npix) {
-    cudaFree(s->aux);
-    cudaFree(s->aflags);
-    s->aux = nullptr;
-    s->aflags = nullptr;
-    s->aux_cap = 0;
-    if (cudaMalloc(&s->aux, (size_t)npix * sizeof(float4)) != cudaSuccess ||
-        cudaMalloc(&s->aflags, (size_t)npix * sizeof(int)) != cudaSuccess)
-      return ST_ENOMEM;
-    s->aux_cap = npix;
-  }
-  const unsigned nb = (unsigned)((npix + 127) / 128);
-  if (B > npix) SC(cudaMemsetAsync(s->X + (size_t)npix * sur::NIN, 0, (size_t)(B - npix) * sur::NIN * 4, stream));
-  if (v.kerr) sur::sur_inputs_kernel<1><<<nb, 128, 0, stream>>>(p, f, s->X, s->aux, s->aflags, npix);
-  else sur::sur_inputs_kernel<0><<<nb, 128, 0, stream>>>(p, f, s->X, s->aux, s->aflags, npix);
-  SC(cudaGetLastError());
-  if ((rc = forward(s, s->X, B, false, stream)) != ST_OK) return rc;
+  const unsigned nb = (unsigned)(((p.width + 15) / 16) * ((p.height + 7) / 8));
+  auto k = v.kerr ? sur::sur_frame_kernel<1> : sur::sur_frame_kernel<0>;
+  SC(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sur::F_SMEM));
   SC(cudaMemsetAsync(count, 0, sizeof(int), stream));
-  sur::sur_gate_kernel<<<nb, 128, 0, stream>>>(p, f, s->out, s->aux, s->aflags, list, count, npix);
+  k<<<nb, sur::FTHREADS, sur::F_SMEM, stream>>>(p, f, s->P, s->Wb[0], s->Wb[1], s->Wb[2], list, count);
   SC(cudaGetLastError());
   return ST_OK;
 }

@@ -512,6 +512,45 @@ __device__ void init_ray(const TraceParams& p, const CamView& cam, int i0, int j
   st.g_cross = 0.f;
 }
 
+// Land a step on the sphere |x| = target: the RK4 step of size hc from yp
+// (slope k1) is a polynomial state y(hc); find hc in (0, h) with
+// |y(hc)| = target by false position with the Illinois modification, the
+// bracket [0, h] kept throughout (g(0) = r0 - target and g(h) = rn - target
+// have opposite signs).  A step that crosses the sphere far from linearly in
+// hc (a ray leaving the horizon's neighbourhood within one step) stays
+// bracketed where plain secant iterations can wander off the sphere.
+// Iterates until |g| < tol or the bracket stops shrinking; the first iterate
+// is the linear guess h (target - r0) / (rn - r0).
+template <int KERR, typename R>
+__device__ __forceinline__ void land_on_sphere(const R* yp, R pt, R M, R a, R h, const R* k1, R r0, R rn, R target,
+                                               R* yout) {
+  const R tol = sizeof(R) == 8 ? R(1e-14) : R(1e-6) * target;
+  const R eps = sizeof(R) == 8 ? R(1e-15) : R(1e-7);
+  R ha = R(0), ga = r0 - target, hb = h, gb = rn - target;
+  int side = 0;
+  R inc[6];
+#pragma unroll 1
+  for (int it = 0; it < 60; ++it) {
+    R hc = (ha * gb - hb * ga) / (gb - ga);
+    if (!(hc > ha && hc < hb)) hc = R(0.5) * (ha + hb);
+    rk4_inc<KERR>(yp, pt, M, a, hc, k1, inc);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) yout[k] = yp[k] + inc[k];
+    const R gc = sqrt_(yout[0] * yout[0] + yout[1] * yout[1] + yout[2] * yout[2]) - target;
+    if (gc == R(0) || (hb - ha) < eps * h) break;
+    if ((gc > R(0)) == (gb > R(0))) {
+      hb = hc; gb = gc;
+      if (side == -1) ga *= R(0.5);
+      side = -1;
+    } else {
+      ha = hc; ga = gc;
+      if (side == 1) gb *= R(0.5);
+      side = 1;
+    }
+    if (fabs_(gc) < tol) break;
+  }
+}
+
 // ---- shading pieces applied at interpolated points --------------------------
 
 template <typename R>
@@ -902,21 +941,8 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
     if (p.exit_landing) {
       const R rn = sqrt_(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
       if (rn > st.r_esc) {
-        // two secant iterations on the step size from the saved state
-        const R re = st.r_esc;
-        R ha = h, ra = rn;
-        R hb = (rn > r) ? h * (re - r) / (rn - r) : h;
-        R inc[6], yt[6];
-#pragma unroll 1
-        for (int it = 0; it < 2; ++it) {
-          rk4_inc<KERR>(yp, st.pt, M, a, hb, k1, inc);
-#pragma unroll
-          for (int k = 0; k < 6; ++k) yt[k] = yp[k] + inc[k];
-          const R rb = sqrt_(yt[0] * yt[0] + yt[1] * yt[1] + yt[2] * yt[2]);
-          if (it == 1 || rb == ra) break;
-          const R hn = hb + (re - rb) * (hb - ha) / (rb - ra);
-          ha = hb; ra = rb; hb = hn;
-        }
+        R yt[6];
+        land_on_sphere<KERR>(yp, st.pt, M, a, h, k1, r, rn, st.r_esc, yt);
 #pragma unroll
         for (int k = 0; k < 6; ++k) { y[k] = yt[k]; st.lo[k] = 0.f; }
         st.flags |= ST_RAY_ESCAPED;
@@ -946,19 +972,8 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
     else if (rn <= R(2.00001)) rb = R(2.00001);
     else if (rn >= st.r_esc) rb = st.r_esc;
     if (rb > R(0)) {
-      R ha = h, ra = rn;
-      R hb = (rn != r) ? h * (rb - r) / (rn - r) : h;
-      R inc[6], yt[6];
-#pragma unroll 1
-      for (int it = 0; it < 2; ++it) {
-        rk4_inc<KERR>(yp, st.pt, M, a, hb, k1, inc);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) yt[k] = yp[k] + inc[k];
-        const R rr = sqrt_(yt[0] * yt[0] + yt[1] * yt[1] + yt[2] * yt[2]);
-        if (it == 1 || rr == ra) break;
-        const R hn = hb + (rb - rr) * (hb - ha) / (rr - ra);
-        ha = hb; ra = rr; hb = hn;
-      }
+      R yt[6];
+      land_on_sphere<KERR>(yp, st.pt, M, a, h, k1, r, rn, rb, yt);
 #pragma unroll
       for (int k = 0; k < 6; ++k) { y[k] = yt[k]; st.lo[k] = 0.f; }
       st.flags |= (rb == st.r_esc) ? ST_RAY_ESCAPED : ST_RAY_CAPTURED;

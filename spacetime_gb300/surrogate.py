@@ -10,6 +10,7 @@ import numpy as np
 from . import _abi
 
 NIN, NOUT, NT = 6, 6, 8
+RAW = 15  # label row: r, theta, a, n (3), flags, steps, exit dir (3), r_cross, launch dir d0 (3)
 
 
 def _fp(a):
@@ -63,7 +64,7 @@ class Surrogate:
     def generate(self, n: int, offset: int = 0, dt: float = 0.02, copy: bool = True):
         x = np.empty((n, NIN), np.float32) if copy else None
         t = np.empty((n, NT), np.float32) if copy else None
-        raw = np.empty((n, 12), np.float32) if copy else None
+        raw = np.empty((n, RAW), np.float32) if copy else None
         nul = C.POINTER(C.c_float)()
         _abi.check(self._lib.st_surrogate_generate(self._h, n, offset, dt, _fp(x) if copy else nul,
                                                    _fp(t) if copy else nul, _fp(raw) if copy else nul),
@@ -80,3 +81,29 @@ class Surrogate:
 def raw_to_geometry(raw):
     """(r, theta, a, n[3]) of label rows (raw[:, :6])."""
     return raw[:, 0], raw[:, 1], raw[:, 2], raw[:, 3:6]
+
+
+def label_position_unit(raw):
+    """Unit Cartesian position of each label row's camera, at azimuth 0:
+    pos = (sqrt(r^2 + a^2) sin theta, 0, r cos theta)."""
+    r, th, a = (raw[:, k].astype(np.float64) for k in range(3))
+    pos = np.stack([np.sqrt(r * r + a * a) * np.sin(th), np.zeros_like(r), r * np.cos(th)], 1)
+    return pos / np.linalg.norm(pos, axis=1, keepdims=True)
+
+
+def plane_exit(xh, d0, defl, tilt):
+    """Exit direction from the network's ray-plane angles (the gate's
+    reconstruction): cos E (cos(psi + D) xh + sin(psi + D) et) + sin E en."""
+    xh = np.asarray(xh, np.float64)
+    d0 = np.asarray(d0, np.float64)
+    d0 = d0 / np.linalg.norm(d0, axis=1, keepdims=True)
+    c = (xh * d0).sum(1)
+    t = d0 - c[:, None] * xh
+    sn = np.linalg.norm(t, axis=1)
+    et = t / np.maximum(sn, 1e-300)[:, None]
+    en = np.cross(xh, et)
+    psi = np.arctan2(sn, c)
+    chi = psi + np.asarray(defl, np.float64)
+    e = np.asarray(tilt, np.float64)[:, None]
+    d = np.cos(e) * (np.cos(chi)[:, None] * xh + np.sin(chi)[:, None] * et) + np.sin(e) * en
+    return d / np.linalg.norm(d, axis=1, keepdims=True)

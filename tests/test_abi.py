@@ -129,3 +129,12 @@ def test_host_tetrad_matches_oracle(built_lib, oracle_lib):
         beta = scene.camera_beta(cam)
         ref = oracle_lib.camera_tetrad(cam.pos, cam.fwd, cam.right, cam.up_local, 1.0, a, beta)
         assert np.abs(T - np.stack(ref)).max() < 1e-13
+
+
+def test_surrogate_row_widths_match_header():
+    """The Python handle sizes label rows as the header documents them."""
+    from spacetime_gb300 import surrogate
+    hdr = open(os.path.join(os.path.dirname(__file__), "..", "include", "spacetime_gb300.h")).read()
+    assert f"raw[n][{surrogate.RAW}]" in hdr
+    assert f"t[n][{surrogate.NT}]" in hdr
+    assert f"out[n][{surrogate.NOUT}]" in hdr and f"x[n][{surrogate.NIN}]" in hdr

@@ -14,7 +14,7 @@ import pytest
 from oracle import mlp_oracle as MO
 from oracle import oracle as O
 from spacetime_gb300 import scene
-from spacetime_gb300.surrogate import Surrogate
+from spacetime_gb300.surrogate import Surrogate, label_position_unit, plane_exit
 
 pytestmark = pytest.mark.gpu
 
@@ -117,6 +117,17 @@ def test_labels_match_oracle_integrator(sur):
     # more for the few rays that wind near the photon shell
     assert np.median(errs) < 1e-5, np.sort(errs)[-5:]
     assert (errs < 1e-3).mean() > 0.95
+    # the targets are the exit direction as ray-plane angles: decoding them the
+    # way the render gate does gives back the stored exit direction
+    dec = plane_exit(label_position_unit(raw[ok]), raw[ok, 12:15], t[ok, 0], t[ok, 1])
+    ex = raw[ok, 8:11].astype(np.float64)
+    ang = 2 * np.arcsin(np.clip(np.linalg.norm(dec - ex / np.linalg.norm(ex, axis=1, keepdims=True), axis=1) / 2,
+                                0, 1))
+    assert np.percentile(ang, 99) < 2e-6 and ang.max() < 1e-4, np.sort(ang)[-5:]
+    # 80% of the directions lie in the 75-degree inward cone, all of them on the sphere
+    nr = raw[:, 3]
+    assert abs((nr <= -math.cos(math.radians(75)) + 1e-6).mean() - 0.8) < 0.01
+    assert nr.max() > 0.95 and np.allclose(np.linalg.norm(raw[:, 3:6], axis=1), 1, atol=1e-6)
 
 
 def test_training_reduces_loss(sur):
