@@ -24,6 +24,10 @@
  *                          on the device, no download)
  *   st_camera_tetrad       ks_camera_tetrad + camera_beta, src/preview.jl:93-198,
  *                          src/camera.jl:19-22
+ *   st_context_set_starfield  set_starfield!(ctx; ...), src/metal.jl:257-295, and the
+ *                          CPU renderer's Starfield(...), src/starfield.jl:60-81
+ *   st_render_motion       render_draft_mtl(...; camera_at, per_pixel_shutter),
+ *                          src/metal.jl:2017-2030, 2130-2169, 829-857
  *
  * Output layout: linear HDR RGB float32 in the reference's column-major
  * (3, width, height) order, i.e. out[3*(i + width*j) + c] for 0-based pixel
@@ -119,6 +123,30 @@ typedef struct {
   int march_stride;          /* gas sampled every march_stride*dt of arc, 1..16 */
 } st_volume;
 
+/* Procedural point stars, evaluated per escaping ray in the source sky
+ * (starfield_mtl, src/metal.jl:652-724; starfield_color, src/starfield.jl:83-150).
+ * Stars sit on a density x density lattice of directions (u = atan2(y,x)/2pi +
+ * 1/2, v = (z+1)/2), at most one per cell, placed, thinned and coloured by
+ * the reference's hash; each is a Gaussian of width
+ * psf_pixels * 2 fov_factor / height radians.  The sky image is scaled by
+ * texture_weight under them.  Star colour comes from the stars' own
+ * blackbody table (white point wb_temperature, chroma scaled by saturation
+ * about Rec.709 luminance), never the disc's. */
+typedef struct {
+  double strength;           /* 0 disables */
+  double texture_weight;     /* sky image weight under the stars */
+  int height;                /* render height the PSF is sized for */
+  double fov_factor;         /* the vertical field is 2 fov_factor across height rows */
+  double density, fill, flux, psf_pixels;
+  double galactic[3];        /* galactic-plane normal (need not be unit) */
+  double concentration;      /* occupancy thinning exp(-|n.s| concentration) */
+  double temp_min, temp_max; /* star temperatures, uniform */
+  int seed;
+  double wb_temperature;     /* star white point */
+  double saturation;         /* chroma scale of the star table */
+  int table_size;            /* star table entries */
+} st_starfield;
+
 typedef struct {
   int width, height;
   int samples;               /* samples^2 stratified passes per pixel */
@@ -198,6 +226,15 @@ int st_context_create(st_context** out, const float* sky_rgb, int sky_w, int sky
 int st_context_set_disc(st_context* ctx, const st_disc* disc);
 /* NULL disables the volume; the density grid is copied to HBM. */
 int st_context_set_volume(st_context* ctx, const st_volume* vol);
+/* set_starfield! defaults: strength 1, texture_weight 0, height 1080,
+ * fov_factor 0.55, density 384, fill 0.5, flux 0.011, psf_pixels 0.5,
+ * galactic (0,0,1), concentration 3, temperatures 3000-16000 K, seed 12345,
+ * white point 10000 K, saturation 1, 1024 entries. */
+void st_starfield_default(st_starfield* sf);
+/* NULL or strength <= 0 disables the stars (the context default).  Rejects a
+ * zero galactic normal (ArgumentError in the reference), height < 1,
+ * density < 1, psf_pixels <= 0 or table_size < 2 with ST_EINVAL. */
+int st_context_set_starfield(st_context* ctx, const st_starfield* sf);
 void st_context_destroy(st_context* ctx);
 
 /* Render one frame into caller-owned host memory out_rgb[3*width*height]. */
@@ -213,6 +250,25 @@ int st_render_diag(st_context* ctx, const st_camera* cam, const st_spacetime* st
  * the context's float4 [height][width] framebuffer (valid until the next call). */
 int st_render_device(st_context* ctx, const st_camera* cam, const st_spacetime* st,
                      const st_render_params* p, const float** dev_rgba, st_stats* stats);
+
+/* Motion blur, render_draft_mtl(...; camera_at, per_pixel_shutter)
+ * (src/metal.jl:2130-2169).  Each of the samples^2 passes owns one shutter
+ * stratum m (shuffled, like the pixel and lens strata).  The caller evaluates
+ * its camera_at(s) at the fractions the passes need and passes the poses:
+ *   per_pixel_shutter = 0: poses[m] = camera_at((m + 0.5) / samples^2),
+ *                          m < samples^2: each pass renders from the
+ *                          midpoint of its stratum (nposes = samples^2);
+ *   per_pixel_shutter = 1: poses[m] = camera_at(m / samples^2), m <= samples^2:
+ *                          each pixel moves the pose from poses[m] toward
+ *                          poses[m + 1] by a hashed fraction
+ *                          (src/metal.jl:843-857; nposes = samples^2 + 1).
+ * A pose supplies position, axes, fov_factor and velocity; projection and lens
+ * come from cam, which also sets the escape radius and the step budget, as
+ * the reference's render call does.  diag (may be NULL) receives the last
+ * pass's per-ray records.  No surrogate (ST_EUNSUPPORTED). */
+int st_render_motion(st_context* ctx, const st_camera* cam, const st_camera* poses, int nposes,
+                     int per_pixel_shutter, const st_spacetime* st, const st_render_params* p,
+                     float* out_rgb, st_ray_diag* diag, st_stats* stats);
 
 /* Render `nframes` camera poses (a camera track) in one persistent launch;
  * out_rgb holds nframes frames back to back. */

@@ -45,6 +45,12 @@ class OrcScene(C.Structure):
         ("r_escape", C.c_double), ("tspan", C.c_double), ("hstep_coef", C.c_double),
         ("hstep_cap", C.c_double), ("rtol", C.c_double), ("atol", C.c_double), ("relativistic", C.c_int),
         ("exit_landing", C.c_int), ("tol", C.c_double),
+        ("shutter_seed", C.c_int), ("pos_end", D3), ("u_end", C.c_double * 4), ("Ef_end", C.c_double * 4),
+        ("Er_end", C.c_double * 4), ("Eu_end", C.c_double * 4),
+        ("star_strength", C.c_double), ("star_tw", C.c_double), ("star_N", C.c_double), ("star_fill", C.c_double),
+        ("star_sigma", C.c_double), ("star_flux", C.c_double), ("star_g", D3), ("star_conc", C.c_double),
+        ("star_tmin", C.c_double), ("star_tspan", C.c_double), ("star_lut", FP), ("star_lut_size", C.c_int),
+        ("star_seed", C.c_int), ("star_lut_tmin", C.c_double), ("star_lut_tmax", C.c_double),
     ]
 
 
@@ -162,6 +168,28 @@ def blackbody_lut(wb=6500.0, tmin=500.0, tmax=30000.0, n=1024):
     return out
 
 
+STAR_WB_TEMPERATURE = 10000.0  # src/metal.jl:75
+
+
+def star_lut(wb=STAR_WB_TEMPERATURE, saturation=1.0, n=1024):
+    """The stars' colour table (_star_lut_cpu, src/metal.jl:86-104): the
+    white-balanced blackbody table over [500, 30000] K in float32, chroma
+    scaled by `saturation` about Rec.709 luminance.  Shape (n, 3)."""
+    lut = blackbody_lut(wb, 500.0, 30000.0, n).astype(np.float32)
+    if saturation != 1.0:
+        s = np.float32(saturation)
+        L = (np.float32(0.2126) * lut[:, 0] + np.float32(0.7152) * lut[:, 1]
+             + np.float32(0.0722) * lut[:, 2])[:, None]
+        lut = (L + s * (lut - L)).astype(np.float32)
+    return lut
+
+
+def camera_beta_of(cam):
+    """camera_beta (src/camera.jl:19-22): world velocity on the camera axes."""
+    v = np.asarray(cam.velocity, dtype=np.float64)
+    return (float(v @ cam.fwd), float(v @ cam.right), float(v @ cam.up_local))
+
+
 def sim_hash(x, y, z):
     return lib().orc_sim_hash(x, y, z)
 
@@ -182,7 +210,7 @@ class Scene:
     def __init__(self, *, cam, M, a, sky, width, height, semantics, integrator, dt=0.02, nmax=0,
                  r_escape=0.0, tspan=0.0, disc=None, emitter=EMIT_KEPLER, lut=None, volume=None,
                  relativistic=False, exit_landing=None, ju=None, jv=None, rtol=1e-10, atol=1e-12,
-                 rect=None, tol=1e-4):
+                 rect=None, tol=1e-4, starfield=None, shutter=None):
         s = OrcScene()
         s.pos[:] = list(map(float, cam.pos))
         s.fwd[:] = list(map(float, cam.fwd))
@@ -252,7 +280,42 @@ class Scene:
         s.rtol, s.atol = rtol, atol
         s.tol = tol
         s.relativistic = int(relativistic)
+        if starfield is not None:
+            self._set_starfield(s, starfield)
+        if shutter is not None:
+            # (seed, end camera): the end pose's tetrad, as the host computes it
+            seed, end = shutter
+            u, Ef, Er, Eu = camera_tetrad(end.pos, end.fwd, end.right, end.up_local, M, a,
+                                          camera_beta_of(end))
+            s.shutter_seed = int(seed)
+            s.pos_end[:] = list(map(float, end.pos))
+            s.u_end[:], s.Ef_end[:], s.Er_end[:], s.Eu_end[:] = list(u), list(Ef), list(Er), list(Eu)
         self.s = s
+
+    def _set_starfield(self, s, sf):
+        """sf: dict of st_starfield's fields (set_starfield! packing,
+        src/metal.jl:268-290; star table per _star_lut_cpu, :86-104)."""
+        g = np.asarray(sf.get("galactic", (0.0, 0.0, 1.0)), dtype=np.float64)
+        gn = float(np.linalg.norm(g))
+        n = int(sf.get("table_size", 1024))
+        lut = np.ascontiguousarray(star_lut(sf.get("wb_temperature", STAR_WB_TEMPERATURE),
+                                            sf.get("saturation", 1.0), n), dtype=np.float32)
+        self._keep.append(lut)
+        s.star_strength = float(sf.get("strength", 1.0))
+        s.star_tw = float(sf.get("texture_weight", 0.0))
+        s.star_N = float(sf.get("density", 384.0))
+        s.star_fill = float(sf.get("fill", 0.5))
+        s.star_sigma = float(sf.get("psf_pixels", 0.5)) * 2.0 * float(sf.get("fov_factor", 0.55)) / int(
+            sf.get("height", 1080))
+        s.star_flux = float(sf.get("flux", 0.011))
+        s.star_g[:] = list(g / gn)
+        s.star_conc = float(sf.get("concentration", 3.0))
+        s.star_tmin = float(sf.get("temp_min", 3000.0))
+        s.star_tspan = float(sf.get("temp_max", 16000.0)) - s.star_tmin
+        s.star_lut = lut.ctypes.data_as(FP)
+        s.star_lut_size = n
+        s.star_seed = int(sf.get("seed", 12345))
+        s.star_lut_tmin, s.star_lut_tmax = 500.0, 30000.0
 
     def render(self, nthreads: int = 0, records: bool = True):
         s = self.s

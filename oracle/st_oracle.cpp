@@ -657,6 +657,56 @@ void locate(StepFn step, G g, double g0, double g1, double h1, double* yout) {
   }
 }
 
+// Procedural stars along unit direction d (starfield_mtl, src/metal.jl:652-724;
+// starfield_color, src/starfield.jl:83-150): the direction's lattice cell on a
+// star_N x star_N grid of (u = atan2(y,x)/2pi + 1/2, v = (z+1)/2) and its eight
+// neighbours; a star per cell at a hashed point, kept with probability
+// fill exp(-|n.s| concentration), flux xi^(-2/3), Gaussian PSF, colour from the
+// star table (DRAFT index rounds half up, RENDER to nearest even).
+void star_light(const orc_scene* s, bool draft, double dx, double dy, double dz, double* rgb) {
+  const double N = s->star_N;
+  const int Ni = (int)s->star_N;
+  const double two_pi = 2.0 * kPi;
+  const double u = std::atan2(dy, dx) / two_pi + 0.5;
+  const double v = (dz + 1.0) * 0.5;
+  const int i0 = (int)std::floor(u * N), j0 = (int)std::floor(v * N);
+  const double sig = s->star_sigma;
+  const double inv2s2 = 1.0 / (2.0 * sig * sig), cut = 25.0 * sig * sig;
+  const int n = s->star_lut_size, seed = s->star_seed;
+  double ar = 0.0, ag = 0.0, ab = 0.0;
+  for (int dj = -1; dj <= 1; ++dj) {
+    const int jj = j0 + dj;
+    if (jj < 0 || jj >= Ni) continue;
+    for (int di = -1; di <= 1; ++di) {
+      int ii = (i0 + di) % Ni;
+      if (ii < 0) ii += Ni;
+      const double su = sim_hash(ii, jj, seed + 1), sv = sim_hash(ii, jj, seed + 2);
+      const double phs = ((ii + su) / N - 0.5) * two_pi;
+      const double sz = 2.0 * (jj + sv) / N - 1.0;
+      const double sr = std::sqrt(std::max(1.0 - sz * sz, 0.0));
+      const double sx = sr * std::cos(phs), sy = sr * std::sin(phs);
+      const double ex = dx - sx, ey = dy - sy, ez = dz - sz;
+      const double d2 = ex * ex + ey * ey + ez * ez;
+      if (d2 > cut) continue;
+      double occ = s->star_fill;
+      if (s->star_conc > 0.0)
+        occ *= std::exp(-std::fabs(sx * s->star_g[0] + sy * s->star_g[1] + sz * s->star_g[2]) * s->star_conc);
+      if (!((double)sim_hash(ii, jj, seed) < occ)) continue;
+      const double xi = std::max((double)sim_hash(ii, jj, seed + 3), (double)1e-4f);
+      const double w = s->star_flux * std::exp((double)-0.6666667f * std::log(xi)) * std::exp(-d2 * inv2s2);
+      const double T = s->star_tmin + s->star_tspan * (double)sim_hash(ii, jj, seed + 4);
+      const double lt0 = s->star_lut_tmin, lt1 = s->star_lut_tmax;
+      const double frac = (clampd(T, lt0, lt1) - lt0) / std::max(lt1 - lt0, 1e-6);
+      int li = draft ? (int)(frac * (n - 1) + 0.5) : (int)std::nearbyint(frac * (n - 1));
+      li = std::min(std::max(li, 0), n - 1);
+      ar += w * s->star_lut[3 * li];
+      ag += w * s->star_lut[3 * li + 1];
+      ab += w * s->star_lut[3 * li + 2];
+    }
+  }
+  rgb[0] = ar; rgb[1] = ag; rgb[2] = ab;
+}
+
 void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
   const orc_scene* s = S.s;
   const Phys& P = S.P;
@@ -708,9 +758,22 @@ void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
     }
     cr = dxl / nu; cu = dyl / nu; cf = 1.0 / nu;
   }
-  const Tetrad& T = S.T;
+  // Per-pixel shutter: the pose moves toward the stratum's end pose by a
+  // hashed fraction of the way (src/metal.jl:843-857).
+  Tetrad T = S.T;
+  double cpos[3] = {s->pos[0], s->pos[1], s->pos[2]};
+  if (s->shutter_seed > 0) {
+    const double tau = (double)sim_hash(i1, j1, s->shutter_seed);
+    for (int k = 0; k < 3; ++k) cpos[k] += tau * (s->pos_end[k] - cpos[k]);
+    for (int k = 0; k < 4; ++k) {
+      T.Ef[k] += tau * (s->Ef_end[k] - T.Ef[k]);
+      T.Er[k] += tau * (s->Er_end[k] - T.Er[k]);
+      T.Eu[k] += tau * (s->Eu_end[k] - T.Eu[k]);
+      T.u[k] += tau * (s->u_end[k] - T.u[k]);
+    }
+  }
   double origin[3], q[4];
-  for (int k = 0; k < 3; ++k) origin[k] = s->pos[k] + offr * T.Er[k + 1] + offu * T.Eu[k + 1];
+  for (int k = 0; k < 3; ++k) origin[k] = cpos[k] + offr * T.Er[k + 1] + offu * T.Eu[k + 1];
   for (int k = 0; k < 4; ++k) q[k] = cf * T.Ef[k] + cr * T.Er[k] + cu * T.Eu[k] - T.u[k];
   double y[6], pt;
   lower_photon(origin, q, P, y, &pt);
@@ -935,6 +998,11 @@ void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
     const double ph = std::atan2(rec.dir[1], rec.dir[0]);
     double sky[3];
     sample_sky(s, th, ph, sky);
+    if (s->star_strength > 0.0) {
+      double sl[3];
+      star_light(s, S.draft, rec.dir[0], rec.dir[1], rec.dir[2], sl);
+      for (int c = 0; c < 3; ++c) sky[c] = sky[c] * s->star_tw + s->star_strength * sl[c];
+    }
     sky_tint(scam, sky);
     for (int c = 0; c < 3; ++c) rgb[c] += alpha * sky[c];
   }

@@ -98,6 +98,17 @@ typedef struct {
   int relativistic;
   int exit_landing;        /* land exactly on r_escape (DRAFT) */
   double tol;              /* kernel-twin adaptive tolerance */
+  /* per-pixel shutter (src/metal.jl:829-857): seed 0 = off; the pose at the
+   * far end of the stratum, interpolated per pixel at tau = hash(i, j, seed) */
+  int shutter_seed;
+  double pos_end[3], u_end[4], Ef_end[4], Er_end[4], Eu_end[4];
+  /* procedural stars (src/metal.jl:652-724, src/starfield.jl:83-150); strength 0 = off */
+  double star_strength, star_tw;
+  double star_N, star_fill, star_sigma, star_flux;
+  double star_g[3], star_conc, star_tmin, star_tspan;
+  const float* star_lut;   /* (3, star_lut_size) */
+  int star_lut_size, star_seed;
+  double star_lut_tmin, star_lut_tmax;
 } orc_scene;
 
 typedef struct {

@@ -61,6 +61,16 @@ class StVolume(C.Structure):
     ]
 
 
+class StStarfield(C.Structure):
+    _fields_ = [
+        ("strength", C.c_double), ("texture_weight", C.c_double), ("height", C.c_int),
+        ("fov_factor", C.c_double), ("density", C.c_double), ("fill", C.c_double), ("flux", C.c_double),
+        ("psf_pixels", C.c_double), ("galactic", C.c_double * 3), ("concentration", C.c_double),
+        ("temp_min", C.c_double), ("temp_max", C.c_double), ("seed", C.c_int),
+        ("wb_temperature", C.c_double), ("saturation", C.c_double), ("table_size", C.c_int),
+    ]
+
+
 class StRenderParams(C.Structure):
     _fields_ = [
         ("width", C.c_int), ("height", C.c_int), ("samples", C.c_int),
@@ -111,6 +121,7 @@ EXPORTS = [
     "st_surrogate_create", "st_surrogate_destroy", "st_surrogate_num_params", "st_surrogate_get_params",
     "st_surrogate_set_params", "st_surrogate_forward", "st_surrogate_loss_grad", "st_surrogate_generate",
     "st_surrogate_train", "st_render_frames_noalloc", "st_context_set_surrogate",
+    "st_starfield_default", "st_context_set_starfield", "st_render_motion",
 ]
 
 _lib = None
@@ -170,6 +181,13 @@ def load(path: str | None = None) -> C.CDLL:
     lib.st_render_frames_noalloc.restype = C.c_int
     lib.st_context_set_surrogate.argtypes = [C.c_void_p, C.c_void_p]
     lib.st_context_set_surrogate.restype = C.c_int
+    lib.st_starfield_default.argtypes = [P(StStarfield)]
+    lib.st_starfield_default.restype = None
+    lib.st_context_set_starfield.argtypes = [C.c_void_p, P(StStarfield)]
+    lib.st_context_set_starfield.restype = C.c_int
+    lib.st_render_motion.argtypes = [C.c_void_p, P(StCamera), P(StCamera), C.c_int, C.c_int, P(StSpacetime),
+                                     P(StRenderParams), P(C.c_float), C.c_void_p, P(StStats)]
+    lib.st_render_motion.restype = C.c_int
     for name in ("st_context_create", "st_context_set_disc", "st_context_set_volume", "st_render",
                  "st_render_diag", "st_render_device", "st_render_frames", "st_camera_tetrad",
                  "st_surrogate_create", "st_surrogate_num_params", "st_surrogate_get_params",

@@ -74,6 +74,39 @@ class Lens:
         return lens_fov(self.focal_length)
 
 
+@dataclass(frozen=True)
+class Starfield:
+    """Procedural point stars, Starfield(...) of the CPU renderer
+    (src/starfield.jl:60-81) and set_starfield!(ctx; ...) of the GPU one
+    (src/metal.jl:257-295), argument for argument."""
+    strength: float = 1.0
+    texture_weight: float = 0.0
+    height: int = 1080
+    fov_factor: float = 0.55
+    density: float = 384.0
+    fill: float = 0.5
+    flux: float = 0.011
+    psf_pixels: float = 0.5
+    galactic: tuple = (0.0, 0.0, 1.0)
+    concentration: float = 3.0
+    temp_min: float = 3000.0
+    temp_max: float = 16000.0
+    seed: int = 12345
+    wb_temperature: float = 10000.0
+    saturation: float = 1.0
+    table_size: int = 1024
+
+    def as_c(self) -> "_abi.StStarfield":
+        c = _abi.StStarfield()
+        for name, _ in _abi.StStarfield._fields_:
+            v = getattr(self, name)
+            if name == "galactic":
+                c.galactic[:] = [float(x) for x in v]
+            else:
+                setattr(c, name, v)
+        return c
+
+
 @dataclass
 class RenderResult:
     image: np.ndarray
@@ -155,6 +188,18 @@ class Context:
         _abi.check(self._lib.st_context_set_volume(self._h, C.byref(v)), "st_context_set_volume")
         self.volume = vol
 
+    def set_starfield(self, sf: Starfield | None = None, **kw):
+        """set_starfield!(ctx; strength, texture_weight, height, fov_factor,
+        density, fill, flux, psf_pixels, galactic, concentration, temp_min,
+        temp_max, seed, wb_temperature, saturation): a Starfield, or its
+        fields as keywords; None (or strength 0) turns the stars off."""
+        if sf is None and kw:
+            sf = Starfield(**kw)
+        c = sf.as_c() if sf is not None else None
+        _abi.check(self._lib.st_context_set_starfield(self._h, C.byref(c) if c is not None else None),
+                   "st_context_set_starfield")
+        self.starfield = sf
+
     def set_surrogate(self, sur):
         """Attach a trained surrogate (spacetime_gb300.surrogate.Surrogate) for
         renders with surrogate=1; None detaches it."""
@@ -214,6 +259,23 @@ class Context:
         _abi.check(rc, "st_render_device")
         return ptr.value, stats.as_dict()
 
+    def render_motion_raw(self, cam: Camera, poses, bh, p: _abi.StRenderParams, per_pixel_shutter: bool = False,
+                          diag: bool = False) -> RenderResult:
+        """Motion-blurred render (st_render_motion): poses are camera_at
+        sampled at (m + 1/2)/samples^2 (midpoint) or m/samples^2, m <=
+        samples^2 (per-pixel shutter)."""
+        n = len(poses)
+        arr = (_abi.StCamera * n)(*[_st_camera(c) for c in poses])
+        img = np.empty((p.height, p.width, 3), dtype=np.float32)
+        d = np.empty(p.height * p.width, dtype=_abi.DIAG_DTYPE) if diag else None
+        stats = _abi.StStats()
+        rc = self._lib.st_render_motion(self._h, C.byref(_st_camera(cam)), arr, n, int(per_pixel_shutter),
+                                        C.byref(_st_spacetime(bh)), C.byref(p),
+                                        img.ctypes.data_as(C.POINTER(C.c_float)),
+                                        C.c_void_p(d.ctypes.data) if diag else None, C.byref(stats))
+        _abi.check(rc, "st_render_motion")
+        return RenderResult(img, stats.as_dict(), d.reshape(p.height, p.width) if diag else None)
+
     def render_frames_raw(self, cams, bh, p: _abi.StRenderParams) -> RenderResult:
         n = len(cams)
         arr = (_abi.StCamera * n)(*[_st_camera(c) for c in cams])
@@ -236,7 +298,7 @@ def _prec(x):
 def render(cam: Camera, bh, sky: np.ndarray, *, disc: AccretionDisc | None = AccretionDisc(),
            width: int = 400, height: int = 200, samples: int = 1, relativistic: bool = False,
            precision="fp64", dt: float = 0.02, jittered: bool = False, seed: int = 0,
-           context: Context | None = None, **kw) -> np.ndarray:
+           starfield: Starfield | None = None, context: Context | None = None, **kw) -> np.ndarray:
     """The CPU renderer's call, `render(cam, bh, sky; disc, width, height,
     samples, relativistic)` (src/raytrace.jl:339-428), on the GPU: horizon at
     r = 2.00001, escape at r_max = max(5|pos|, 100), affine budget
@@ -248,6 +310,8 @@ def render(cam: Camera, bh, sky: np.ndarray, *, disc: AccretionDisc | None = Acc
         # the reference has no render(cam, ::Kerr, ...) method
         raise TypeError("render: the CPU-renderer semantics are Schwarzschild-only; use render_draft")
     ctx = context or Context(sky, disc=disc, emitter=_abi.ST_EMIT_KEPLER)
+    if starfield is not None or context is None:
+        ctx.set_starfield(starfield)
     try:
         p = ctx.params(_abi.ST_SEM_RENDER, width=width, height=height, samples=samples,
                        relativistic=int(relativistic), precision=_prec(precision), dt=dt,
@@ -261,15 +325,23 @@ def render(cam: Camera, bh, sky: np.ndarray, *, disc: AccretionDisc | None = Acc
 def render_draft(ctx: Context, cam: Camera, bh, *, width: int = 1920, height: int = 1080, samples: int = 2,
                  dt: float = 0.02, fisheye_deg: float = 0.0, aperture_world: float = 0.0,
                  focus_dist: float = 1.0, relativistic: bool = False, precision="fp32",
-                 pixel_jitter: bool = True, seed: int = 0, **kw) -> np.ndarray:
+                 pixel_jitter: bool = True, seed: int = 0, camera_at=None, per_pixel_shutter: bool = False,
+                 **kw) -> np.ndarray:
     """render_draft_mtl(ctx, cam, st; width, height, samples, dt, fisheye_deg,
-    aperture_world, focus_dist, relativistic) (src/metal.jl:2040-2242)."""
+    aperture_world, focus_dist, relativistic, camera_at, per_pixel_shutter)
+    (src/metal.jl:2040-2242).  camera_at(s) -> Camera for the shutter
+    fraction s in [0, 1) turns on motion blur."""
     cam2 = Camera(cam.pos, cam.fwd, cam.right, cam.up_local, cam.fov_factor, cam.velocity,
                   _abi.ST_PROJ_FISHEYE if fisheye_deg > 0 else _abi.ST_PROJ_PINHOLE, fisheye_deg,
                   aperture_world, focus_dist)
     p = ctx.params(_abi.ST_SEM_DRAFT, width=width, height=height, samples=samples, dt=dt,
                    relativistic=int(relativistic), precision=_prec(precision),
                    pixel_jitter=int(pixel_jitter), seed=seed, **kw)
+    if camera_at is not None:
+        n = samples * samples
+        poses = ([camera_at(m / n) for m in range(n + 1)] if per_pixel_shutter
+                 else [camera_at((m + 0.5) / n) for m in range(n)])
+        return ctx.render_motion_raw(cam2, poses, bh, p, per_pixel_shutter=per_pixel_shutter).image
     return ctx.render_raw(cam2, bh, p).image
 
 

@@ -308,6 +308,12 @@ struct st_context {
   st::TraceParams gkey{};
   st::Variant gvar{};
   size_t gbytes = 0;
+  // procedural stars: host parameters and the stars' own colour table
+  st_starfield star{};
+  bool star_on = false;
+  float4* d_star_lut = nullptr;
+  int star_lut_size = 0;
+  double star_lut_tmin = 500.0, star_lut_tmax = 30000.0;
   st_surrogate* sur = nullptr;  // attached surrogate (not owned)
   int* d_list = nullptr;        // surrogate fallback pixels
   size_t list_cap = 0;
@@ -449,6 +455,30 @@ int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, 
   p->sky = ctx->d_sky;
   p->sky_w = ctx->sky_w;
   p->sky_h = ctx->sky_h;
+  if (ctx->star_on) {
+    // set_starfield! packing (src/metal.jl:268-290): sigma from the PSF in
+    // pixels and the vertical field, unit galactic normal, temperature span
+    const st_starfield& sf = ctx->star;
+    const double gn = std::sqrt(sf.galactic[0] * sf.galactic[0] + sf.galactic[1] * sf.galactic[1] +
+                                sf.galactic[2] * sf.galactic[2]);
+    p->star_strength = sf.strength;
+    p->star_tw = sf.texture_weight;
+    p->star_N = sf.density;
+    p->star_fill = sf.fill;
+    p->star_sigma = sf.psf_pixels * 2.0 * sf.fov_factor / sf.height;
+    p->star_flux = sf.flux;
+    for (int k = 0; k < 3; ++k) p->star_g[k] = sf.galactic[k] / gn;
+    p->star_conc = sf.concentration;
+    p->star_tmin = sf.temp_min;
+    p->star_tspan = sf.temp_max - sf.temp_min;
+    p->star_lut = ctx->d_star_lut;
+    p->star_lut_size = ctx->star_lut_size;
+    p->star_lut_tmin = ctx->star_lut_tmin;
+    p->star_lut_tmax = ctx->star_lut_tmax;
+    p->star_seed = sf.seed;
+  } else {
+    p->star_strength = 0.0;
+  }
   p->counters = ctx->d_counters;
   p->queue = ctx->d_queue;
   p->chunk_steps = rp->chunk_steps > 0 ? rp->chunk_steps : 32;
@@ -465,6 +495,16 @@ struct PassPlan {
   int jseed;
   double lens_u0, lens_v0, lens_w;
   int lens_seed;
+  int time_m;        // shutter stratum of this pass (motion blur)
+  int shutter_seed;  // per-pixel shutter hash seed of this pass
+};
+
+// Motion blur of one render (st_render_motion): the caller's camera_at
+// evaluated at the fractions the passes use.
+struct Motion {
+  const st_camera* poses;
+  int nposes;
+  int per_pixel;
 };
 
 // The samples^2 passes of render_draft_mtl (src/metal.jl:2091-2168) or of
@@ -474,10 +514,11 @@ std::vector<PassPlan> plan_passes(const st_render_params* rp, const st_camera* c
   const int S = rp->samples;
   const int n = S * S;
   st::Rng rng{rp->seed ^ 0x5eed5eedull};
-  std::vector<int> order(n), lens(n);
-  for (int k = 0; k < n; ++k) { order[k] = k; lens[k] = k; }
+  std::vector<int> order(n), lens(n), tperm(n);
+  for (int k = 0; k < n; ++k) { order[k] = k; lens[k] = k; tperm[k] = k; }
   if (rp->pixel_jitter) st::shuffle(order, rng);
   st::shuffle(lens, rng);
+  st::shuffle(tperm, rng);  // time strata pair randomly with the others (src/metal.jl:2124-2130)
   const bool dof = cam->aperture_world > 0.0 && cam->projection == ST_PROJ_PINHOLE;
   std::vector<PassPlan> out(n);
   for (int k = 0; k < n; ++k) {
@@ -502,13 +543,31 @@ std::vector<PassPlan> plan_passes(const st_render_params* rp, const st_camera* c
       pp.lens_w = 1.0 / S;
       pp.lens_seed = k + 1;
     }
+    pp.time_m = tperm[k];
+    pp.shutter_seed = 104729 + (k + 1);  // clear of the lens seeds (src/metal.jl:2148-2150)
     out[k] = pp;
   }
   return out;
 }
 
+// The tetrad of a motion pose: the pose's position, axes, field and velocity
+// with the render's own projection and lens settings (_ks_cam_params of
+// camera_at(s) with the call's fisheye_deg / focus_dist, src/metal.jl:2141-2158).
+int pose_params(st_context* ctx, const st_camera* cam, const st_camera* pose, const st_spacetime* stp,
+                const st_render_params* rp, TraceParams* out) {
+  st_camera pc = *cam;
+  for (int k = 0; k < 3; ++k) {
+    pc.pos[k] = pose->pos[k]; pc.fwd[k] = pose->fwd[k]; pc.right[k] = pose->right[k];
+    pc.up[k] = pose->up[k]; pc.velocity[k] = pose->velocity[k];
+  }
+  pc.fov_factor = pose->fov_factor;
+  st::Variant w;
+  return fill_params(ctx, &pc, stp, rp, out, &w);
+}
+
 int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
-              float* host_rgb, st_ray_diag* host_diag, const float** dev_rgba, st_stats* stats) {
+              float* host_rgb, st_ray_diag* host_diag, const float** dev_rgba, st_stats* stats,
+              const Motion* mo = nullptr) {
   const auto t0 = std::chrono::steady_clock::now();
   TraceParams p;
   st::Variant v;
@@ -545,6 +604,28 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
     p.ju = pp.ju; p.jv = pp.jv; p.jw = pp.jw; p.jseed = pp.jseed;
     p.lens_u0 = pp.lens_u0; p.lens_v0 = pp.lens_v0; p.lens_w = pp.lens_w; p.lens_seed = pp.lens_seed;
     p.first_pass = (k == 0) ? 1 : 0;
+    if (mo) {
+      // this pass's pose: the stratum midpoint, or its start with the end
+      // pose for the per-pixel shutter
+      TraceParams q;
+      if ((rc = pose_params(ctx, cam, &mo->poses[pp.time_m], stp, rp, &q)) != ST_OK) return rc;
+      std::memcpy(p.pos, q.pos, sizeof p.pos);
+      std::memcpy(p.Ef, q.Ef, sizeof p.Ef);
+      std::memcpy(p.Er, q.Er, sizeof p.Er);
+      std::memcpy(p.Eu, q.Eu, sizeof p.Eu);
+      std::memcpy(p.U, q.U, sizeof p.U);
+      p.fov = q.fov;
+      p.shutter_seed = 0;
+      if (mo->per_pixel) {
+        if ((rc = pose_params(ctx, cam, &mo->poses[pp.time_m + 1], stp, rp, &q)) != ST_OK) return rc;
+        std::memcpy(p.pos_end, q.pos, sizeof p.pos_end);
+        std::memcpy(p.Ef_end, q.Ef, sizeof p.Ef_end);
+        std::memcpy(p.Er_end, q.Er, sizeof p.Er_end);
+        std::memcpy(p.Eu_end, q.Eu, sizeof p.Eu_end);
+        std::memcpy(p.U_end, q.U, sizeof p.U_end);
+        p.shutter_seed = pp.shutter_seed;
+      }
+    }
     if (rp->surrogate) {
       const PassPlan& pp0 = passes[0];
       (void)pp0;
@@ -744,12 +825,79 @@ int st_context_set_volume(st_context* ctx, const st_volume* v) {
   return ST_OK;
 }
 
+void st_starfield_default(st_starfield* sf) {
+  if (!sf) return;
+  std::memset(sf, 0, sizeof(*sf));
+  sf->strength = 1.0;
+  sf->texture_weight = 0.0;
+  sf->height = 1080;
+  sf->fov_factor = 0.55;
+  sf->density = 384.0;
+  sf->fill = 0.5;
+  sf->flux = 0.011;
+  sf->psf_pixels = 0.5;
+  sf->galactic[2] = 1.0;
+  sf->concentration = 3.0;
+  sf->temp_min = 3000.0;
+  sf->temp_max = 16000.0;
+  sf->seed = 12345;
+  sf->wb_temperature = 10000.0;  // STAR_WB_TEMPERATURE, src/metal.jl:75
+  sf->saturation = 1.0;
+  sf->table_size = 1024;
+}
+
+// Star colour table (_star_lut_cpu, src/metal.jl:86-104): Blackbody(wb) entries
+// over [500, 30000] K in single precision, chroma scaled by `saturation`
+// about Rec.709 luminance.
+int st_context_set_starfield(st_context* ctx, const st_starfield* sf) {
+  if (!ctx) return ST_EINVAL;
+  if (!sf || !(sf->strength > 0.0)) { ctx->star_on = false; return ST_OK; }
+  const double gn = std::sqrt(sf->galactic[0] * sf->galactic[0] + sf->galactic[1] * sf->galactic[1] +
+                              sf->galactic[2] * sf->galactic[2]);
+  if (!(gn > 0.0) || sf->height < 1 || !(sf->density >= 1.0) || !(sf->psf_pixels > 0.0) ||
+      sf->table_size < 2 || sf->table_size > (1 << 20) || !(sf->wb_temperature > 0.0))
+    return ST_EINVAL;
+  const int n = sf->table_size;
+  const double tmin = 500.0, tmax = 30000.0;
+  double ref[3];
+  st::host_blackbody(sf->wb_temperature, ref);
+  std::vector<float4> lut(n);
+  const float sat = (float)sf->saturation;
+  for (int i = 0; i < n; ++i) {
+    const double T = tmin + (tmax - tmin) * i / (n - 1);
+    double c[3];
+    st::host_blackbody(std::max(T, 1.0), c);
+    float r = (float)(c[0] / ref[0]), g = (float)(c[1] / ref[1]), b = (float)(c[2] / ref[2]);
+    if (sf->saturation != 1.0) {
+      const float L = 0.2126f * r + 0.7152f * g + 0.0722f * b;
+      r = L + sat * (r - L); g = L + sat * (g - L); b = L + sat * (b - L);
+    }
+    lut[i] = make_float4(r, g, b, 0.f);
+  }
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
+  if (ctx->d_star_lut && ctx->star_lut_size != n) {
+    cudaFree(ctx->d_star_lut);
+    ctx->d_star_lut = nullptr;
+    ctx->star_lut_size = 0;
+  }
+  if (!ctx->d_star_lut && cudaMalloc(&ctx->d_star_lut, n * sizeof(float4)) != cudaSuccess) return ST_ENOMEM;
+  if (cudaMemcpy(ctx->d_star_lut, lut.data(), n * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess)
+    return ST_ECUDA;
+  ctx->star_lut_size = n;
+  ctx->star_lut_tmin = tmin;
+  ctx->star_lut_tmax = tmax;
+  ctx->star = *sf;
+  ctx->star_on = true;
+  return ST_OK;
+}
+
 void st_context_destroy(st_context* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   cudaFree(ctx->d_sky);
   cudaFree(ctx->d_lut);
+  cudaFree(ctx->d_star_lut);
   cudaFree(ctx->d_vol);
   cudaFree(ctx->d_fb);
   cudaFree(ctx->d_rgb);
@@ -778,6 +926,17 @@ int st_render_diag(st_context* ctx, const st_camera* cam, const st_spacetime* st
                    float* out_rgb, st_ray_diag* diag, st_stats* stats) {
   if (!out_rgb || !diag) return ST_EINVAL;
   return do_render(ctx, cam, st, p, out_rgb, diag, nullptr, stats);
+}
+
+int st_render_motion(st_context* ctx, const st_camera* cam, const st_camera* poses, int nposes,
+                     int per_pixel_shutter, const st_spacetime* st, const st_render_params* p, float* out_rgb,
+                     st_ray_diag* diag, st_stats* stats) {
+  if (!out_rgb || !cam || !poses || !p || p->samples <= 0) return ST_EINVAL;
+  const int n = p->samples * p->samples;
+  if (nposes != (per_pixel_shutter ? n + 1 : n)) return ST_EINVAL;
+  if (p->surrogate) return ST_EUNSUPPORTED;
+  const Motion mo{poses, nposes, per_pixel_shutter ? 1 : 0};
+  return do_render(ctx, cam, st, p, out_rgb, diag, nullptr, stats, &mo);
 }
 
 int st_render_device(st_context* ctx, const st_camera* cam, const st_spacetime* st, const st_render_params* p,

@@ -23,7 +23,7 @@ struct FrameCam {
 };
 
 // Everything a trace launch needs, passed by value as a __grid_constant__
-// kernel parameter (well under the 4 KB limit).
+// kernel parameter (about 1.2 KB, under the 4 KB limit).
 struct TraceParams {
   // camera tetrad (FP64 host computation, src/preview.jl:93-198)
   double pos[3];
@@ -67,6 +67,17 @@ struct TraceParams {
   // sky
   const float4* sky;         // [sky_h][sky_w] RGB_
   int sky_w, sky_h;
+  // procedural stars (starfield_mtl, src/metal.jl:652-724); strength 0 = off
+  double star_strength, star_tw;  // star weight, sky-image weight under them
+  double star_N, star_fill, star_sigma, star_flux;
+  double star_g[3], star_conc, star_tmin, star_tspan;
+  const float4* star_lut;    // [star_lut_size] RGB_, the stars' own white point
+  int star_lut_size, star_seed;
+  double star_lut_tmin, star_lut_tmax;
+  // per-pixel shutter (src/metal.jl:829-857): seed 0 = off; the camera pose
+  // at the far end of this pass's shutter stratum
+  int shutter_seed;
+  double pos_end[3], Ef_end[4], Er_end[4], Eu_end[4], U_end[4];
   // outputs
   float4* out;               // [height][width] (x frames)
   st_ray_diag* diag;         // optional

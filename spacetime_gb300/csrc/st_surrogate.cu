@@ -587,6 +587,12 @@ __device__ __forceinline__ bool gate_pixel(const TraceParams& p, const SurFrame&
   dird[0] = d0; dird[1] = d1; dird[2] = d2;
   float sky[3];
   sample_sky(p, acosf(fminf(fmaxf(d2, -1.f), 1.f)), atan2f(d1, d0), sky);
+  if (p.star_strength > 0.0) {
+    float sl[3];
+    star_light<ST_SEM_DRAFT>(p, d0, d1, d2, sl);
+    const float tw = (float)p.star_tw, ss = (float)p.star_strength;
+    for (int c = 0; c < 3; ++c) sky[c] = sky[c] * tw + ss * sl[c];
+  }
   const float g = a4.w;
   if (g != 1.f) {
     sky[0] *= 57.4f / (__expf(4.067f / g) - 1.f);

@@ -457,11 +457,30 @@ __device__ void init_ray(const TraceParams& p, const CamView& cam, int i0, int j
     }
     cr = dxl / nu; cu = dyl / nu; cf = D(1) / nu;
   }
+  // the pose; with the per-pixel shutter on, moved toward the stratum's end
+  // pose by a hashed fraction (src/metal.jl:843-857)
+  D cpos[3], cEf[4], cEr[4], cEu[4], cU[4];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) cpos[k] = D(cam.pos[k]);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) { cEf[k] = D(cam.Ef[k]); cEr[k] = D(cam.Er[k]); cEu[k] = D(cam.Eu[k]); cU[k] = D(cam.U[k]); }
+  if (p.shutter_seed > 0) {
+    const D tau = D(sim_hash(i1, j1, p.shutter_seed));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) cpos[k] += tau * (D(p.pos_end[k]) - cpos[k]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      cEf[k] += tau * (D(p.Ef_end[k]) - cEf[k]);
+      cEr[k] += tau * (D(p.Er_end[k]) - cEr[k]);
+      cEu[k] += tau * (D(p.Eu_end[k]) - cEu[k]);
+      cU[k] += tau * (D(p.U_end[k]) - cU[k]);
+    }
+  }
   D x[3], q[4];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) x[k] = D(cam.pos[k]) + offr * D(cam.Er[k + 1]) + offu * D(cam.Eu[k + 1]);
+  for (int k = 0; k < 3; ++k) x[k] = cpos[k] + offr * cEr[k + 1] + offu * cEu[k + 1];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) q[k] = cf * D(cam.Ef[k]) + cr * D(cam.Er[k]) + cu * D(cam.Eu[k]) - D(cam.U[k]);
+  for (int k = 0; k < 4; ++k) q[k] = cf * cEf[k] + cr * cEr[k] + cu * cEu[k] - cU[k];
   D s[6], pt;
   lower_photon<KERR>(x, q, D(p.M), D(p.a), s, &pt);
 
@@ -983,6 +1002,64 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
   return false;
 }
 
+// Procedural stars along unit direction d (starfield_mtl, src/metal.jl:652-724;
+// the CPU renderer's starfield_color, src/starfield.jl:83-150): the ray's own
+// lattice cell and its eight neighbours, each holding at most one star placed
+// by the hash; Gaussian PSF of width sigma, cut at 5 sigma; occupancy thinned
+// away from the galactic plane; flux xi^(-2/3); colour from the stars' table,
+// indexed as the disc's (DRAFT rounds half up, RENDER to nearest even).
+template <int SEM, typename R>
+__device__ __forceinline__ void star_light(const TraceParams& p, R dx, R dy, R dz, R* rgb) {
+  const R N = R(p.star_N);
+  const int Ni = (int)p.star_N;
+  const R two_pi = R(6.283185307179586);
+  const R u = atan2_(dy, dx) / two_pi + R(0.5);
+  const R v = (dz + R(1)) * R(0.5);
+  const int i0 = (int)floor_(u * N), j0 = (int)floor_(v * N);
+  const R sig = R(p.star_sigma);
+  const R inv2s2 = R(1) / (R(2) * sig * sig);
+  const R cut = R(25) * sig * sig;
+  const R fill = R(p.star_fill), conc = R(p.star_conc), flux0 = R(p.star_flux);
+  const R gx = R(p.star_g[0]), gy = R(p.star_g[1]), gz = R(p.star_g[2]);
+  const R tmin = R(p.star_tmin), tspan = R(p.star_tspan);
+  const R lt0 = R(p.star_lut_tmin), lt1 = R(p.star_lut_tmax);
+  const int n = p.star_lut_size;
+  const int seed = p.star_seed;
+  R ar = R(0), ag = R(0), ab = R(0);
+#pragma unroll 1
+  for (int dj = -1; dj <= 1; ++dj) {
+    const int jj = j0 + dj;
+    if (jj < 0 || jj >= Ni) continue;
+#pragma unroll 1
+    for (int di = -1; di <= 1; ++di) {
+      int ii = (i0 + di) % Ni;
+      if (ii < 0) ii += Ni;
+      const R su = R(sim_hash(ii, jj, seed + 1)), sv = R(sim_hash(ii, jj, seed + 2));
+      const R phs = ((R(ii) + su) / N - R(0.5)) * two_pi;
+      const R sz = R(2) * (R(jj) + sv) / N - R(1);
+      const R sr = sqrt_(max_(R(1) - sz * sz, R(0)));
+      const R sx = sr * cos_(phs), sy = sr * sin_(phs);
+      const R ex = dx - sx, ey = dy - sy, ez = dz - sz;
+      const R d2 = ex * ex + ey * ey + ez * ez;
+      if (d2 > cut) continue;
+      R occ = fill;
+      if (conc > R(0)) occ *= exp_(-fabs_(sx * gx + sy * gy + sz * gz) * conc);
+      if (!(R(sim_hash(ii, jj, seed)) < occ)) continue;
+      const R xi = max_(R(sim_hash(ii, jj, seed + 3)), R(1e-4f));
+      const R w = flux0 * exp_(R(-0.6666667f) * log_(xi)) * exp_(-d2 * inv2s2);
+      const R T = tmin + tspan * R(sim_hash(ii, jj, seed + 4));
+      const R frac = (clamp_(T, lt0, lt1) - lt0) / max_(lt1 - lt0, R(1e-6));
+      int li;
+      if constexpr (SEM == ST_SEM_DRAFT) li = (int)(frac * R(n - 1) + R(0.5));
+      else li = (int)rint(frac * R(n - 1));
+      li = min(max(li, 0), n - 1);
+      const float4 c = p.star_lut[li];
+      ar += w * R(c.x); ag += w * R(c.y); ab += w * R(c.z);
+    }
+  }
+  rgb[0] = ar; rgb[1] = ag; rgb[2] = ab;
+}
+
 // Classification, sky and output (src/metal.jl:1629-1704, src/raytrace.jl:267-298).
 template <int PREC, int KERR, int SEM>
 __device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typename RealOf<PREC>::T>& st, int out_index,
@@ -1006,6 +1083,16 @@ __device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typena
     const R ph = atan2_(d1, d0);
     R sky[3];
     sample_sky(p, th, ph, sky);
+    if (p.star_strength > 0.0) {
+      // the image under the stars, then the stars (src/metal.jl:1668-1677;
+      // src/starfield.jl:157-164), both before the relativistic tint
+      R sl[3];
+      star_light<SEM>(p, d0, d1, d2, sl);
+      const R tw = R(p.star_tw), ss = R(p.star_strength);
+      sky[0] = sky[0] * tw + ss * sl[0];
+      sky[1] = sky[1] * tw + ss * sl[1];
+      sky[2] = sky[2] * tw + ss * sl[2];
+    }
     const R g = st.scam;
     if (g != R(1)) {
       sky[0] *= R(57.4) / (exp_(R(4.067) / g) - R(1));
