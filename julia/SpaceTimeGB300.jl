@@ -46,10 +46,17 @@ mutable struct StRenderParams
     semantics::Cint; precision::Cint; schedule::Cint
     r_escape::Float64; tspan::Float64
     relativistic::Cint; exit_landing::Cint; pixel_jitter::Cint; seed::UInt64
-    r_guard::Float64; crit_band::Float64; renorm_every::Cint
+    r_guard::Float64; crit_band::Float64; crit_r::Float64; renorm_every::Cint
     surrogate::Cint; surrogate_sigma::Float64
-    block_x::Cint; block_y::Cint; chunk_steps::Cint
+    block_x::Cint; block_y::Cint; chunk_steps::Cint; graph::Cint
+    order::Cint; tol::Float64
     StRenderParams() = new()
+end
+struct StStarfield
+    strength::Float64; texture_weight::Float64; height::Cint; fov_factor::Float64
+    density::Float64; fill::Float64; flux::Float64; psf_pixels::Float64
+    galactic::NTuple{3,Float64}; concentration::Float64; temp_min::Float64; temp_max::Float64
+    seed::Cint; wb_temperature::Float64; saturation::Float64; table_size::Cint
 end
 
 check(rc, where) = rc == ST_OK ||
@@ -138,15 +145,45 @@ function render_gb300(cam::Camera, bh::Schwarzschild, sky; disc=AccretionDisc(),
     st_render!(ctx, st_camera(cam), bh, p)
 end
 
-"""`render_draft_mtl(ctx, cam, st; ...)` on the GPU with the Metal kernel's rules."""
+"""`set_starfield!(ctx; ...)` (src/metal.jl:257-295), same keywords and defaults."""
+function set_starfield_gb300!(ctx::GB300Context; strength::Real=1.0, texture_weight::Real=0.0,
+                              height::Union{Int,Nothing}=nothing, fov_factor::Real=0.55, density::Real=384,
+                              fill::Real=0.5, flux::Real=0.011, psf_pixels::Real=0.5,
+                              galactic::NTuple{3,Real}=(0.0, 0.0, 1.0), concentration::Real=3.0,
+                              temp_min::Real=3000, temp_max::Real=16000, seed::Integer=12345,
+                              wb_temperature::Real=10000.0, saturation::Real=1.0)
+    sf = Ref(StStarfield(strength, texture_weight, something(height, ctx.height), fov_factor, density, fill,
+                         flux, psf_pixels, Float64.(galactic), concentration, temp_min, temp_max, seed,
+                         wb_temperature, saturation, 1024))
+    check(ccall((:st_context_set_starfield, libst), Cint, (Ptr{Cvoid}, Ref{StStarfield}), ctx.handle, sf),
+          "st_context_set_starfield")
+end
+
+"""`render_draft_mtl(ctx, cam, st; ...)` on the GPU with the Metal kernel's rules; with
+`camera_at` (a function of the shutter fraction s in [0, 1) returning a Camera) it renders
+motion blur, midpoint or per-pixel shutter, through st_render_motion."""
 function render_draft_gb300(ctx::GB300Context, cam::Camera, bh; width::Int=1920, height::Int=1080,
                             samples::Int=2, dt::Real=0.02, fisheye_deg::Real=0.0, aperture_world::Real=0.0,
                             focus_dist::Real=1.0, relativistic::Bool=false, precision::Int=ST_PREC_FP32,
-                            pixel_jitter::Bool=true)
+                            pixel_jitter::Bool=true, camera_at::Union{Function,Nothing}=nothing,
+                            per_pixel_shutter::Bool=false, order::Int=4, tol::Real=1e-4)
     p = default_params(ST_SEM_DRAFT)
     p.width = width; p.height = height; p.samples = samples; p.dt = dt
     p.relativistic = relativistic; p.precision = precision; p.pixel_jitter = pixel_jitter
-    st_render!(ctx, st_camera(cam; fisheye_deg, aperture_world, focus_dist), bh, p)
+    p.order = order; p.tol = tol
+    c = st_camera(cam; fisheye_deg, aperture_world, focus_dist)
+    camera_at === nothing && return st_render!(ctx, c, bh, p)
+    n = samples^2
+    fracs = per_pixel_shutter ? [m / n for m in 0:n] : [(m + 0.5) / n for m in 0:(n - 1)]
+    poses = [st_camera(camera_at(s); fisheye_deg, aperture_world, focus_dist) for s in fracs]
+    out = Array{Float32,3}(undef, 3, width, height)
+    st = Ref(StSpacetime(bh.M, spin(bh)))
+    check(ccall((:st_render_motion, libst), Cint,
+                (Ptr{Cvoid}, Ref{StCamera}, Ptr{StCamera}, Cint, Cint, Ref{StSpacetime}, Ref{StRenderParams},
+                 Ptr{Float32}, Ptr{Cvoid}, Ptr{Cvoid}),
+                ctx.handle, Ref(c), poses, length(poses), per_pixel_shutter, st, p, out, C_NULL, C_NULL),
+          "st_render_motion")
+    [RGBf(out[1, i, j], out[2, i, j], out[3, i, j]) for i in 1:width, j in 1:height]
 end
 
 end # module

@@ -138,3 +138,18 @@ def test_surrogate_row_widths_match_header():
     assert f"raw[n][{surrogate.RAW}]" in hdr
     assert f"t[n][{surrogate.NT}]" in hdr
     assert f"out[n][{surrogate.NOUT}]" in hdr and f"x[n][{surrogate.NIN}]" in hdr
+
+
+def _julia_fields(src, name):
+    m = re.search(r"struct " + name + r"\n(.*?)\n(?:    " + name + r"\(\) = new\(\)\n)?end", src, re.S)
+    assert m, name
+    body = re.sub(r"#.*", "", m.group(1))
+    return [f.split("::")[0].strip() for f in re.split(r"[;\n]", body) if "::" in f]
+
+
+def test_julia_binding_structs_follow_the_c_layout():
+    """The Julia module's ccall structs list the C structs' fields in order."""
+    src = open(os.path.join(os.path.dirname(__file__), "..", "julia", "SpaceTimeGB300.jl")).read()
+    for jname, cstruct in (("StRenderParams", _abi.StRenderParams), ("StStarfield", _abi.StStarfield),
+                           ("StCamera", _abi.StCamera), ("StDisc", _abi.StDisc), ("StVolume", _abi.StVolume)):
+        assert _julia_fields(src, jname) == [f for f, _ in cstruct._fields_], jname

@@ -21,9 +21,11 @@ from .helpers import angle
 pytestmark = pytest.mark.gpu
 
 
-def _scene():
+def _scene(disc=True):
     w = workloads.config1_thin().scaled(192, 108)
     w.params = dict(samples=1, pixel_jitter=0, exit_landing=1)
+    if not disc:
+        w.disc = None
     return w
 
 
@@ -45,31 +47,34 @@ def test_untrained_surrogate_falls_back_everywhere(built_lib):
 
 
 def test_trained_surrogate_gain(built_lib):
-    w = _scene()
+    """Config1's camera and hole with no disc: every ray either escapes or
+    falls in, so the gate is set by the network's confidence alone."""
+    w = _scene(disc=False)
     sky = workloads.sky(512, 256)
     sur = Surrogate(0, seed=1)
-    sur.generate(1 << 20, offset=0, copy=False)
-    for k in range(10):
-        lr = 1e-5 + 0.5 * (2e-3 - 1e-5) * (1 + np.cos(np.pi * k / 9))
-        sur.train(1000, batch=16384, lr=lr, weight_decay=1e-6)
-    with Context(sky, disc=w.disc, emitter=w.emitter) as ctx:
+    sur.generate(1 << 21, offset=0, copy=False)
+    for k in range(12):
+        lr = 1e-5 + 0.5 * (2e-3 - 1e-5) * (1 + np.cos(np.pi * k / 11))
+        sur.train(2000, batch=16384, lr=lr, weight_decay=1e-6)
+    with Context(sky, disc=None, emitter=w.emitter) as ctx:
         ctx.set_surrogate(sur)
         p0 = ctx.params(w.semantics, width=w.width, height=w.height, precision=_abi.ST_PREC_FP32, **w.params)
         a = ctx.render_raw(w.cam, w.bh, p0, diag=True)
         p1 = ctx.params(w.semantics, width=w.width, height=w.height, precision=_abi.ST_PREC_FP32, surrogate=1,
-                        surrogate_sigma=3e-4, **w.params)
+                        surrogate_sigma=1e-3, **w.params)
         b = ctx.render_raw(w.cam, w.bh, p1, diag=True)
     served = (b.diag["flags"] & _abi.ST_RAY_SURROGATE) > 0
     print("served fraction", served.mean(), "steps", a.stats["steps"], "->", b.stats["steps"],
           "kernel ms", a.stats["kernel_ms"], "->", b.stats["kernel_ms"])
-    assert served.mean() > 0.05
-    assert b.stats["steps"] < a.stats["steps"]
+    assert served.mean() > 0.2
+    assert b.stats["steps"] < (1.0 - 0.5 * served.mean()) * a.stats["steps"]
+    assert b.stats["surrogate_rays"] == served.sum()
     assert np.isfinite(b.image).all()
     ref, rays = O.scene_for(w, sky, O.INT_TSIT5).render()
     ok = served & ((rays["flags"] & O.RAY_ESCAPED) > 0)
     d = angle(b.diag["dir"][ok], rays["dir"][ok])
     print("served dir error median", np.median(d), "p99", np.percentile(d, 99))
-    assert np.median(d) < 3e-4
+    assert np.median(d) < 1e-3
     # unserved pixels are the integrator's, bit for bit
     np.testing.assert_array_equal(a.image[~served], b.image[~served])
     sur.close()
