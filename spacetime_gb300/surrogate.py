@@ -4,6 +4,7 @@ AdamW, and inference."""
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -76,6 +77,17 @@ class Surrogate:
         _abi.check(self._lib.st_surrogate_train(self._h, steps, batch, lr, weight_decay, _fp(hist)),
                    "st_surrogate_train")
         return hist
+
+
+TRAINED = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "surrogate_kerr.npy")
+
+
+def load_trained(device: int = 0) -> "Surrogate":
+    """The shipped network (spacetime_gb300/data/surrogate_kerr.npy, made by
+    spacetime_gb300/train_surrogate.py)."""
+    s = Surrogate(device)
+    s.set_params(np.load(TRAINED))
+    return s
 
 
 def raw_to_geometry(raw):
