@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -37,6 +38,7 @@
 
 #include "st_internal.h"
 #include "st_mlp.cuh"
+#include "st_tc.cuh"
 #include "st_trace.cuh"
 
 namespace st {
@@ -785,6 +787,240 @@ __global__ void __launch_bounds__(FTHREADS, 1)
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same frame pass on the 5th-generation tensor cores (tcgen05 + TMEM)
+// ---------------------------------------------------------------------------
+//
+// One CTA = one 16 x 8 pixel tile = 128 network rows; 8 warps.  Hidden layer
+// l: its weights (a 128 KB K-major 128-byte-swizzled bf16 image, packed once
+// per parameter update by pack_sw128) arrive by bulk copy into shared memory;
+// one thread issues 16 tcgen05.mma (M = 128, N = 256, K = 16) reading the
+// activation tile and the weights straight from shared memory into a 128-lane
+// x 256-column FP32 accumulator in TMEM, and commits to an mbarrier; the
+// epilogue reads the accumulator back (tcgen05.ld, warp w: TMEM lanes
+// 32 (w mod 4).., columns 128 (w / 4)..), adds the bias, applies SiLU and
+// writes bf16 activations back into the swizzled tile for the next layer.
+// The next layer's weights are copied while the epilogue runs.  Layer 0
+// (6 -> 256) and layer 4 (256 -> 6, from the last accumulator, rounded to bf16
+// as the unfused forward stores it) run in FP32.
+//
+// Every wait on an mbarrier is bounded; a wait that runs out marks the tile
+// failed (its pixels all go to the integrator, so the frame stays exact), sets
+// the status word, and the CTA still frees its TMEM.
+constexpr uint32_t TC_ROWS = 128, TC_THREADS = 256;
+constexpr uint32_t TC_A_BYTES = TC_ROWS * NH * 2;  // 64 KB activation tile
+constexpr uint32_t TC_B_BYTES = NH * NH * 2;       // 128 KB weight tile
+constexpr uint32_t TC_TMEM_COLS = 256;
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 22;
+constexpr uint32_t TC_IDESC = tc::idesc_bf16_f32(128, 256);
+
+struct TcSmall {
+  float4 aux[TC_ROWS];
+  float X[TC_ROWS * NIN];
+  float Opart[2][TC_ROWS * NOUT];
+  float W0[NH * NIN];
+  float b0[NH];
+  float bh[3][NH];
+  float W4[NOUT * NH];
+  float b4[8];
+  int fl[TC_ROWS];
+  uint64_t bar_w, bar_mma;
+  uint32_t tmem;
+  int fail;
+};
+constexpr size_t TC_SMEM = 1024 + TC_A_BYTES + TC_B_BYTES + sizeof(TcSmall);
+static_assert(TC_SMEM <= 227 * 1024, "tensor-core surrogate tile exceeds shared memory");
+
+// P (FP32 master weights) -> the three hidden layers' swizzled bf16 images.
+__global__ void pack_sw128(const float* __restrict__ P, unsigned char* __restrict__ Wsw) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 3 * NH * NH) return;
+  const int l = idx / (NH * NH), rem = idx - l * NH * NH;
+  const int n = rem / NH, k = rem - n * NH;
+  const size_t off = l == 0 ? OW1 : l == 1 ? OW2 : OW3;
+  *reinterpret_cast<__nv_bfloat16*>(Wsw + (size_t)l * TC_B_BYTES + tc::sw128_off(n, k, NH)) =
+      __float2bfloat16_rn(P[off + (size_t)n * NH + k]);
+}
+
+template <int KERR>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    sur_frame_tc_kernel(const __grid_constant__ TraceParams p, const __grid_constant__ SurFrame f,
+                        const float* __restrict__ P, const unsigned char* __restrict__ Wsw, int* list, int* count) {
+  extern __shared__ unsigned char tsm_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(tsm_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  unsigned char* As = base;
+  unsigned char* Bs = base + TC_A_BYTES;
+  TcSmall& S = *reinterpret_cast<TcSmall*>(Bs + TC_B_BYTES);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tiles_x = (p.width + 15) >> 4;
+  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  int my_pix = -1;
+  if (tid < (int)TC_ROWS) {
+    const int wq = tid >> 5, l = tid & 31;
+    const int i = tx * 16 + (wq & 1) * 8 + (l & 7), j = ty * 8 + (wq >> 1) * 4 + (l >> 3);
+    if (i < p.width && j < p.height) my_pix = j * p.width + i;
+  }
+  if (tid == 0) {
+    tc::mbar_init(&S.bar_w, 1);
+    tc::mbar_init(&S.bar_mma, 1);
+    S.fail = 0;
+    tc::mbar_fence_init();
+  }
+  if (warp == 0) tc::tmem_alloc(&S.tmem, TC_TMEM_COLS);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = S.tmem;
+  if (tid == 0) {
+    tc::mbar_expect_tx(&S.bar_w, TC_B_BYTES);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) tc::bulk_g2s(Bs + c * 32768, Wsw + c * 32768, 32768, &S.bar_w);
+  }
+  // small FP32 operands, and this tile's network inputs
+  for (int c = tid; c < NH * NIN; c += TC_THREADS) S.W0[c] = P[OW0 + c];
+  for (int c = tid; c < NH; c += TC_THREADS) {
+    S.b0[c] = P[OB0 + c];
+    S.bh[0][c] = P[OB1 + c];
+    S.bh[1][c] = P[OB2 + c];
+    S.bh[2][c] = P[OB3 + c];
+  }
+  for (int c = tid; c < NOUT * NH; c += TC_THREADS) S.W4[c] = P[OW4 + c];
+  if (tid < NOUT) S.b4[tid] = P[OB4 + tid];
+  if (tid < (int)TC_ROWS) {
+    float x[NIN] = {0, 0, 0, 0, 0, 0};
+    float4 a4 = make_float4(0.f, 0.f, 1.f, 1.f);
+    int fl = ST_RAY_GRAZE;
+    if (my_pix >= 0) pixel_inputs<KERR>(p, f, my_pix, x, &a4, &fl);
+#pragma unroll
+    for (int k = 0; k < NIN; ++k) S.X[tid * NIN + k] = x[k];
+    S.aux[tid] = a4;
+    S.fl[tid] = fl;
+  }
+  __syncthreads();
+  // layer 0 (FP32): thread = hidden unit n, all 128 rows, into the swizzled tile
+  {
+    const int n = tid;
+    float w0[NIN];
+#pragma unroll
+    for (int i = 0; i < NIN; ++i) w0[i] = S.W0[n * NIN + i];
+    const float bb = S.b0[n];
+    for (int r = 0; r < (int)TC_ROWS; ++r) {
+      float z = bb;
+#pragma unroll
+      for (int i = 0; i < NIN; ++i) z += S.X[r * NIN + i] * w0[i];
+      *reinterpret_cast<__nv_bfloat16*>(As + tc::sw128_off(r, n, TC_ROWS)) = __float2bfloat16_rn(mlp::silu(z));
+    }
+  }
+  tc::fence_proxy_async();
+  __syncthreads();
+  const uint32_t a_addr = tc::smem_u32(As), b_addr = tc::smem_u32(Bs);
+  const uint32_t q = warp & 3, half = warp >> 2;
+  const int row = (int)(q * 32 + lane);
+  float part[NOUT] = {0, 0, 0, 0, 0, 0};
+  uint32_t ph = 0;
+  for (int l = 0; l < 3; ++l) {
+    if (tid == 0) {
+      if (tc::mbar_wait(&S.bar_w, ph, TC_WAIT_LIMIT)) {
+        tc::fence_after_sync();
+#pragma unroll
+        for (int s = 0; s < NH / 16; ++s) {
+          const uint64_t ad = tc::sw128_desc(a_addr + (s >> 2) * (TC_ROWS * 128) + (s & 3) * 32);
+          const uint64_t bd = tc::sw128_desc(b_addr + (s >> 2) * (NH * 128) + (s & 3) * 32);
+          tc::mma_bf16(tmem, ad, bd, TC_IDESC, s > 0 ? 1u : 0u);
+        }
+        tc::mma_commit(&S.bar_mma);
+      } else {
+        S.fail = 1;
+      }
+    }
+    __syncthreads();
+    if (S.fail) break;
+    if (!tc::mbar_wait(&S.bar_mma, ph, TC_WAIT_LIMIT)) S.fail = 1;
+    ph ^= 1u;
+    __syncthreads();
+    if (S.fail) break;
+    tc::fence_after_sync();
+    if (tid == 0 && l < 2) {
+      // the MMAs are done with the weight tile: fetch the next layer's
+      tc::mbar_expect_tx(&S.bar_w, TC_B_BYTES);
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        tc::bulk_g2s(Bs + c * 32768, Wsw + (size_t)(l + 1) * TC_B_BYTES + c * 32768, 32768, &S.bar_w);
+    }
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+      const int col0 = (int)half * 128 + c * 32;
+      float v[32];
+      tc::tmem_ld32(tmem + ((q * 32u) << 16) + (uint32_t)col0, v);
+      if (l < 2) {
+#pragma unroll
+        for (int ch = 0; ch < 4; ++ch) {
+          uint32_t pk[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int k = col0 + ch * 8 + 2 * e;
+            const __nv_bfloat162 h2 = __floats2bfloat162_rn(mlp::silu(v[ch * 8 + 2 * e] + S.bh[l][k]),
+                                                            mlp::silu(v[ch * 8 + 2 * e + 1] + S.bh[l][k + 1]));
+            pk[e] = *reinterpret_cast<const uint32_t*>(&h2);
+          }
+          *reinterpret_cast<uint4*>(As + tc::sw128_off(row, col0 + ch * 8, TC_ROWS)) =
+              make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < 32; ++e) {
+          const int k = col0 + e;
+          const float h = __bfloat162float(__float2bfloat16_rn(mlp::silu(v[e] + S.bh[2][k])));
+#pragma unroll
+          for (int o = 0; o < NOUT; ++o) part[o] += h * S.W4[o * NH + k];
+        }
+      }
+    }
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  const bool failed = S.fail != 0;
+  if (!failed) {
+#pragma unroll
+    for (int o = 0; o < NOUT; ++o) S.Opart[half][row * NOUT + o] = part[o];
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, TC_TMEM_COLS);
+  }
+  if (failed && tid == 0 && p.counters) atomicMax(p.counters + CNT_STATUS, (unsigned long long)ST_ECUDA);
+  if (tid >= (int)TC_ROWS) return;  // warps 0-3 gate the tile (whole warps: ballots stay full)
+  const int pix = my_pix;
+  float o[NOUT];
+#pragma unroll
+  for (int k = 0; k < NOUT; ++k) o[k] = S.Opart[0][tid * NOUT + k] + S.Opart[1][tid * NOUT + k] + S.b4[k];
+  float4 rgba = make_float4(0.f, 0.f, 0.f, 1.f);
+  double dird[3] = {0, 0, 0};
+  const bool serve = !failed && pix >= 0 && gate_pixel(p, f, o, S.aux[tid], S.fl[tid], &rgba, dird);
+  const unsigned want = __ballot_sync(0xffffffffu, pix >= 0 && !serve);
+  int base_i = 0;
+  if (lane == 0 && want) base_i = atomicAdd(count, __popc(want));
+  base_i = __shfl_sync(0xffffffffu, base_i, 0);
+  if (pix < 0) return;
+  if (serve) {
+    p.out[pix] = rgba;
+    if (p.diag) {
+      st_ray_diag d;
+      d.dir[0] = dird[0]; d.dir[1] = dird[1]; d.dir[2] = dird[2];
+      d.r_final = 0.f; d.alpha = 1.f; d.r_cross = -1.f; d.g_cross = 0.f; d.lambda = 0.f;
+      d.flags = ST_RAY_SURROGATE | ST_RAY_ESCAPED;
+      d.steps = 0; d.fp64_steps = 0; d.pad[0] = d.pad[1] = 0;
+      p.diag[pix] = d;
+    }
+  } else {
+    list[base_i + __popc(want & ((1u << lane) - 1u))] = pix;
+  }
+}
+
 }  // namespace sur
 }  // namespace st
 
@@ -799,6 +1035,7 @@ struct st_surrogate {
   cudaStream_t stream = nullptr;
   float *P = nullptr, *G = nullptr, *Mm = nullptr, *Vv = nullptr;
   __nv_bfloat16* Wb[3] = {nullptr, nullptr, nullptr};
+  unsigned char* Wsw = nullptr;  // hidden layers as swizzled bf16 images for the tcgen05 frame kernel
   int cap = 0;  // rows of the work buffers
   float* X = nullptr;
   float* Z[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -847,6 +1084,8 @@ int sync_bf16(st_surrogate* s) {
     to_bf16<<<(NH * NH + 255) / 256, 256, 0, s->stream>>>(s->P + OWH[l], s->Wb[l], NH * NH);
     SC(cudaGetLastError());
   }
+  pack_sw128<<<(3 * NH * NH + 255) / 256, 256, 0, s->stream>>>(s->P, s->Wsw);
+  SC(cudaGetLastError());
   return ST_OK;
 }
 
@@ -925,6 +1164,7 @@ int st_surrogate_create(st_surrogate** out, int device, unsigned long long seed)
     return fail(ST_ENOMEM);
   for (int l = 0; l < 3; ++l)
     if (cudaMalloc(&s->Wb[l], NH * NH * 2) != cudaSuccess) return fail(ST_ENOMEM);
+  if (cudaMalloc(&s->Wsw, 3 * (size_t)TC_B_BYTES) != cudaSuccess) return fail(ST_ENOMEM);
   // He-style uniform initialisation from a splitmix64 stream (host)
   std::vector<float> P(NPARAM, 0.f);
   uint64_t z = seed * 0x9e3779b97f4a7c15ull + 12345;
@@ -963,6 +1203,7 @@ void st_surrogate_destroy(st_surrogate* s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   cudaFree(s->P); cudaFree(s->G); cudaFree(s->Mm); cudaFree(s->Vv); cudaFree(s->loss);
   for (int l = 0; l < 3; ++l) cudaFree(s->Wb[l]);
+  cudaFree(s->Wsw);
   cudaFree(s->X);
   for (int l = 0; l < 4; ++l) { cudaFree(s->Z[l]); cudaFree(s->H[l]); }
   cudaFree(s->dZa); cudaFree(s->dZb); cudaFree(s->out); cudaFree(s->dout); cudaFree(s->T);
@@ -1097,10 +1338,19 @@ namespace st {
 int surrogate_frame(st_surrogate* s, const TraceParams& p, const Variant& v, const SurFrame& f, int* list, int* count,
                     cudaStream_t stream) {
   const unsigned nb = (unsigned)(((p.width + 15) / 16) * ((p.height + 7) / 8));
-  auto k = v.kerr ? sur::sur_frame_kernel<1> : sur::sur_frame_kernel<0>;
-  SC(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sur::F_SMEM));
   SC(cudaMemsetAsync(count, 0, sizeof(int), stream));
-  k<<<nb, sur::FTHREADS, sur::F_SMEM, stream>>>(p, f, s->P, s->Wb[0], s->Wb[1], s->Wb[2], list, count);
+  // tcgen05 / TMEM kernel by default; SPACETIME_GB300_SURROGATE_MMA=sync runs
+  // the mma.sync kernel (the same computation on the warp-level tensor-core path)
+  const char* mode = std::getenv("SPACETIME_GB300_SURROGATE_MMA");
+  if (mode && std::strcmp(mode, "sync") == 0) {
+    auto k = v.kerr ? sur::sur_frame_kernel<1> : sur::sur_frame_kernel<0>;
+    SC(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sur::F_SMEM));
+    k<<<nb, sur::FTHREADS, sur::F_SMEM, stream>>>(p, f, s->P, s->Wb[0], s->Wb[1], s->Wb[2], list, count);
+  } else {
+    auto k = v.kerr ? sur::sur_frame_tc_kernel<1> : sur::sur_frame_tc_kernel<0>;
+    SC(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sur::TC_SMEM));
+    k<<<nb, sur::TC_THREADS, sur::TC_SMEM, stream>>>(p, f, s->P, s->Wsw, list, count);
+  }
   SC(cudaGetLastError());
   return ST_OK;
 }

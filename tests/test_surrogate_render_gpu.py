@@ -78,3 +78,33 @@ def test_trained_surrogate_gain(built_lib):
     # unserved pixels are the integrator's, bit for bit
     np.testing.assert_array_equal(a.image[~served], b.image[~served])
     sur.close()
+
+
+def test_tcgen05_frame_kernel_matches_mma_sync(built_lib, monkeypatch):
+    """The frame pass on tcgen05 / TMEM and on mma.sync computes the same
+    network on the same inputs (FP32 accumulation in a different order):
+    the same pixels are served, with the same exit directions."""
+    from spacetime_gb300.surrogate import load_trained
+    w = _scene(disc=False)
+    sky = workloads.sky(512, 256)
+    sur = load_trained()
+    out = {}
+    with Context(sky, disc=None, emitter=w.emitter) as ctx:
+        ctx.set_surrogate(sur)
+        p = ctx.params(w.semantics, width=w.width, height=w.height, precision=_abi.ST_PREC_FP32, surrogate=1,
+                       surrogate_sigma=4e-4, **w.params)
+        for mode in ("sync", "tc"):
+            monkeypatch.setenv("SPACETIME_GB300_SURROGATE_MMA", mode)
+            out[mode] = ctx.render_raw(w.cam, w.bh, p, diag=True)
+    a, b = out["sync"], out["tc"]
+    assert a.stats["status"] == _abi.ST_OK and b.stats["status"] == _abi.ST_OK
+    sa = (a.diag["flags"] & _abi.ST_RAY_SURROGATE) > 0
+    sb = (b.diag["flags"] & _abi.ST_RAY_SURROGATE) > 0
+    print("served", sa.mean(), sb.mean(), "disagree", (sa != sb).mean())
+    assert sa.mean() > 0.2
+    assert (sa != sb).mean() <= 0.005
+    both = sa & sb
+    d = angle(a.diag["dir"][both], b.diag["dir"][both])
+    print("direction difference median", np.median(d), "max", d.max())
+    assert np.percentile(d, 99) <= 1e-5
+    sur.close()
