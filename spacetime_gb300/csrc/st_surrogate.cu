@@ -815,7 +815,6 @@ constexpr uint32_t TC_WAIT_LIMIT = 1u << 22;
 constexpr uint32_t TC_IDESC = tc::idesc_bf16_f32(128, 256);
 
 struct TcSmall {
-  float4 aux[TC_ROWS];
   float X[TC_ROWS * NIN];
   float Opart[2][TC_ROWS * NOUT];
   float W0[NH * NIN];
@@ -823,7 +822,6 @@ struct TcSmall {
   float bh[3][NH];
   float W4[NOUT * NH];
   float b4[8];
-  int fl[TC_ROWS];
   uint64_t bar_w, bar_mma;
   uint32_t tmem;
   int fail;
@@ -842,10 +840,76 @@ __global__ void pack_sw128(const float* __restrict__ P, unsigned char* __restric
       __float2bfloat16_rn(P[off + (size_t)n * NH + k]);
 }
 
+// Pixel of row `r` (0..127) of tile `t`: each 32-row group is an 8 x 4 block
+// of the 16 x 8 tile, the warp shape of the trace kernel; -1 off the frame.
+__device__ __forceinline__ int tile_pixel(const TraceParams& p, int t, int r) {
+  const int tiles_x = (p.width + 15) >> 4;
+  const int tx = t % tiles_x, ty = t / tiles_x;
+  const int wq = r >> 5, l = r & 31;
+  const int i = tx * 16 + (wq & 1) * 8 + (l & 7), j = ty * 8 + (wq >> 1) * 4 + (l >> 3);
+  return (i < p.width && j < p.height) ? j * p.width + i : -1;
+}
+
+// Network inputs of every pixel, row-ordered by tile (one thread per pixel).
 template <int KERR>
+__global__ void __launch_bounds__(128) sur_inputs_kernel(const __grid_constant__ TraceParams p,
+                                                          const __grid_constant__ SurFrame f, float* __restrict__ X,
+                                                          float4* __restrict__ aux, int* __restrict__ fl) {
+  const int row = blockIdx.x * 128 + threadIdx.x;
+  const int pix = tile_pixel(p, blockIdx.x, threadIdx.x);
+  float x[NIN] = {0, 0, 0, 0, 0, 0};
+  float4 a4 = make_float4(0.f, 0.f, 1.f, 1.f);
+  int flags = ST_RAY_GRAZE;
+  if (pix >= 0) pixel_inputs<KERR>(p, f, pix, x, &a4, &flags);
+#pragma unroll
+  for (int k = 0; k < NIN; ++k) X[(size_t)row * NIN + k] = x[k];
+  aux[row] = a4;
+  fl[row] = flags;
+}
+
+// Gate of every pixel from the network's outputs (one thread per pixel,
+// warp-ordered append of the pixels left to integrate).
+__global__ void __launch_bounds__(128) sur_gate_kernel(const __grid_constant__ TraceParams p,
+                                                        const __grid_constant__ SurFrame f,
+                                                        const float* __restrict__ O, const float4* __restrict__ aux,
+                                                        const int* __restrict__ fl, const int* __restrict__ status,
+                                                        int* list, int* count) {
+  const int row = blockIdx.x * 128 + threadIdx.x, lane = threadIdx.x & 31;
+  const int pix = tile_pixel(p, blockIdx.x, threadIdx.x);
+  float o[NOUT];
+#pragma unroll
+  for (int k = 0; k < NOUT; ++k) o[k] = O[(size_t)row * NOUT + k];
+  float4 rgba = make_float4(0.f, 0.f, 0.f, 1.f);
+  double dird[3] = {0, 0, 0};
+  // a tile whose network pass failed (status[t] != 0) is integrated whole
+  const bool serve = pix >= 0 && status[blockIdx.x] == 0 && gate_pixel(p, f, o, aux[row], fl[row], &rgba, dird);
+  const unsigned want = __ballot_sync(0xffffffffu, pix >= 0 && !serve);
+  int base_i = 0;
+  if (lane == 0 && want) base_i = atomicAdd(count, __popc(want));
+  base_i = __shfl_sync(0xffffffffu, base_i, 0);
+  if (pix < 0) return;
+  if (serve) {
+    p.out[pix] = rgba;
+    if (p.diag) {
+      st_ray_diag d;
+      d.dir[0] = dird[0]; d.dir[1] = dird[1]; d.dir[2] = dird[2];
+      d.r_final = 0.f; d.alpha = 1.f; d.r_cross = -1.f; d.g_cross = 0.f; d.lambda = 0.f;
+      d.flags = ST_RAY_SURROGATE | ST_RAY_ESCAPED;
+      d.steps = 0; d.fp64_steps = 0; d.pad[0] = d.pad[1] = 0;
+      p.diag[pix] = d;
+    }
+  } else {
+    list[base_i + __popc(want & ((1u << lane) - 1u))] = pix;
+  }
+}
+
+// The network on the tensor cores: X[tiles*128][6] -> O[tiles*128][6]; one
+// CTA per 128 rows.  tile_status[t] = 0, or 1 when a bounded wait ran out
+// (the gate then integrates the tile's pixels, and the status word is set).
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    sur_frame_tc_kernel(const __grid_constant__ TraceParams p, const __grid_constant__ SurFrame f,
-                        const float* __restrict__ P, const unsigned char* __restrict__ Wsw, int* list, int* count) {
+    sur_mlp_tc_kernel(const float* __restrict__ P, const unsigned char* __restrict__ Wsw,
+                      const float* __restrict__ X, float* __restrict__ O, int* __restrict__ tile_status,
+                      unsigned long long* counters) {
   extern __shared__ unsigned char tsm_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(tsm_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -853,14 +917,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   unsigned char* Bs = base + TC_A_BYTES;
   TcSmall& S = *reinterpret_cast<TcSmall*>(Bs + TC_B_BYTES);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int tiles_x = (p.width + 15) >> 4;
-  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
-  int my_pix = -1;
-  if (tid < (int)TC_ROWS) {
-    const int wq = tid >> 5, l = tid & 31;
-    const int i = tx * 16 + (wq & 1) * 8 + (l & 7), j = ty * 8 + (wq >> 1) * 4 + (l >> 3);
-    if (i < p.width && j < p.height) my_pix = j * p.width + i;
-  }
+  const size_t row0 = (size_t)blockIdx.x * TC_ROWS;
   if (tid == 0) {
     tc::mbar_init(&S.bar_w, 1);
     tc::mbar_init(&S.bar_mma, 1);
@@ -877,7 +934,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
     for (int c = 0; c < 4; ++c) tc::bulk_g2s(Bs + c * 32768, Wsw + c * 32768, 32768, &S.bar_w);
   }
-  // small FP32 operands, and this tile's network inputs
+  // small FP32 operands, and this tile's inputs (coalesced)
   for (int c = tid; c < NH * NIN; c += TC_THREADS) S.W0[c] = P[OW0 + c];
   for (int c = tid; c < NH; c += TC_THREADS) {
     S.b0[c] = P[OB0 + c];
@@ -887,16 +944,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
   for (int c = tid; c < NOUT * NH; c += TC_THREADS) S.W4[c] = P[OW4 + c];
   if (tid < NOUT) S.b4[tid] = P[OB4 + tid];
-  if (tid < (int)TC_ROWS) {
-    float x[NIN] = {0, 0, 0, 0, 0, 0};
-    float4 a4 = make_float4(0.f, 0.f, 1.f, 1.f);
-    int fl = ST_RAY_GRAZE;
-    if (my_pix >= 0) pixel_inputs<KERR>(p, f, my_pix, x, &a4, &fl);
-#pragma unroll
-    for (int k = 0; k < NIN; ++k) S.X[tid * NIN + k] = x[k];
-    S.aux[tid] = a4;
-    S.fl[tid] = fl;
-  }
+  for (int c = tid; c < (int)(TC_ROWS * NIN); c += TC_THREADS) S.X[c] = X[row0 * NIN + c];
   __syncthreads();
   // layer 0 (FP32): thread = hidden unit n, all 128 rows, into the swizzled tile
   {
@@ -992,32 +1040,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     tc::fence_after_sync();
     tc::tmem_dealloc(tmem, TC_TMEM_COLS);
   }
-  if (failed && tid == 0 && p.counters) atomicMax(p.counters + CNT_STATUS, (unsigned long long)ST_ECUDA);
-  if (tid >= (int)TC_ROWS) return;  // warps 0-3 gate the tile (whole warps: ballots stay full)
-  const int pix = my_pix;
-  float o[NOUT];
-#pragma unroll
-  for (int k = 0; k < NOUT; ++k) o[k] = S.Opart[0][tid * NOUT + k] + S.Opart[1][tid * NOUT + k] + S.b4[k];
-  float4 rgba = make_float4(0.f, 0.f, 0.f, 1.f);
-  double dird[3] = {0, 0, 0};
-  const bool serve = !failed && pix >= 0 && gate_pixel(p, f, o, S.aux[tid], S.fl[tid], &rgba, dird);
-  const unsigned want = __ballot_sync(0xffffffffu, pix >= 0 && !serve);
-  int base_i = 0;
-  if (lane == 0 && want) base_i = atomicAdd(count, __popc(want));
-  base_i = __shfl_sync(0xffffffffu, base_i, 0);
-  if (pix < 0) return;
-  if (serve) {
-    p.out[pix] = rgba;
-    if (p.diag) {
-      st_ray_diag d;
-      d.dir[0] = dird[0]; d.dir[1] = dird[1]; d.dir[2] = dird[2];
-      d.r_final = 0.f; d.alpha = 1.f; d.r_cross = -1.f; d.g_cross = 0.f; d.lambda = 0.f;
-      d.flags = ST_RAY_SURROGATE | ST_RAY_ESCAPED;
-      d.steps = 0; d.fp64_steps = 0; d.pad[0] = d.pad[1] = 0;
-      p.diag[pix] = d;
-    }
-  } else {
-    list[base_i + __popc(want & ((1u << lane) - 1u))] = pix;
+  if (tid == 0) {
+    tile_status[blockIdx.x] = failed ? 1 : 0;
+    if (failed && counters) atomicMax(counters + CNT_STATUS, (unsigned long long)ST_ECUDA);
+  }
+  if (failed) return;
+  for (int c = tid; c < (int)(TC_ROWS * NOUT); c += TC_THREADS) {
+    const int r = c / NOUT, k = c - r * NOUT;
+    O[row0 * NOUT + c] = S.Opart[0][r * NOUT + k] + S.Opart[1][r * NOUT + k] + S.b4[k];
   }
 }
 
@@ -1036,6 +1066,13 @@ struct st_surrogate {
   float *P = nullptr, *G = nullptr, *Mm = nullptr, *Vv = nullptr;
   __nv_bfloat16* Wb[3] = {nullptr, nullptr, nullptr};
   unsigned char* Wsw = nullptr;  // hidden layers as swizzled bf16 images for the tcgen05 frame kernel
+  // frame-pass buffers, rows in tile order: inputs, launch data, outputs, per-tile status
+  float* fX = nullptr;
+  float4* fAux = nullptr;
+  int* fFl = nullptr;
+  float* fO = nullptr;
+  int* fStatus = nullptr;
+  long long frows = 0;
   int cap = 0;  // rows of the work buffers
   float* X = nullptr;
   float* Z[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -1204,6 +1241,7 @@ void st_surrogate_destroy(st_surrogate* s) {
   cudaFree(s->P); cudaFree(s->G); cudaFree(s->Mm); cudaFree(s->Vv); cudaFree(s->loss);
   for (int l = 0; l < 3; ++l) cudaFree(s->Wb[l]);
   cudaFree(s->Wsw);
+  cudaFree(s->fX); cudaFree(s->fAux); cudaFree(s->fFl); cudaFree(s->fO); cudaFree(s->fStatus);
   cudaFree(s->X);
   for (int l = 0; l < 4; ++l) { cudaFree(s->Z[l]); cudaFree(s->H[l]); }
   cudaFree(s->dZa); cudaFree(s->dZb); cudaFree(s->out); cudaFree(s->dout); cudaFree(s->T);
@@ -1347,9 +1385,28 @@ int surrogate_frame(st_surrogate* s, const TraceParams& p, const Variant& v, con
     SC(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sur::F_SMEM));
     k<<<nb, sur::FTHREADS, sur::F_SMEM, stream>>>(p, f, s->P, s->Wb[0], s->Wb[1], s->Wb[2], list, count);
   } else {
-    auto k = v.kerr ? sur::sur_frame_tc_kernel<1> : sur::sur_frame_tc_kernel<0>;
-    SC(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sur::TC_SMEM));
-    k<<<nb, sur::TC_THREADS, sur::TC_SMEM, stream>>>(p, f, s->P, s->Wsw, list, count);
+    const long long rows = (long long)nb * sur::TC_ROWS;
+    if (s->frows < rows) {
+      cudaFree(s->fX); cudaFree(s->fAux); cudaFree(s->fFl); cudaFree(s->fO); cudaFree(s->fStatus);
+      s->fX = nullptr; s->fAux = nullptr; s->fFl = nullptr; s->fO = nullptr; s->fStatus = nullptr;
+      s->frows = 0;
+      if (cudaMalloc(&s->fX, rows * sur::NIN * sizeof(float)) != cudaSuccess ||
+          cudaMalloc(&s->fAux, rows * sizeof(float4)) != cudaSuccess ||
+          cudaMalloc(&s->fFl, rows * sizeof(int)) != cudaSuccess ||
+          cudaMalloc(&s->fO, rows * sur::NOUT * sizeof(float)) != cudaSuccess ||
+          cudaMalloc(&s->fStatus, (size_t)nb * sizeof(int)) != cudaSuccess)
+        return ST_ENOMEM;
+      s->frows = rows;
+    }
+    if (v.kerr) sur::sur_inputs_kernel<1><<<nb, 128, 0, stream>>>(p, f, s->fX, s->fAux, s->fFl);
+    else sur::sur_inputs_kernel<0><<<nb, 128, 0, stream>>>(p, f, s->fX, s->fAux, s->fFl);
+    SC(cudaGetLastError());
+    SC(cudaFuncSetAttribute(sur::sur_mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)sur::TC_SMEM));
+    sur::sur_mlp_tc_kernel<<<nb, sur::TC_THREADS, sur::TC_SMEM, stream>>>(s->P, s->Wsw, s->fX, s->fO, s->fStatus,
+                                                                          p.counters);
+    SC(cudaGetLastError());
+    sur::sur_gate_kernel<<<nb, 128, 0, stream>>>(p, f, s->fO, s->fAux, s->fFl, s->fStatus, list, count);
   }
   SC(cudaGetLastError());
   return ST_OK;
