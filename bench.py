@@ -171,6 +171,63 @@ def cpu_baseline(seconds_target: float = 15.0, threads: int | None = None, gpu_f
     return out
 
 
+def surrogate_variant(ctx_cls, device: int, flush, sigma: float, reps: int = 3) -> dict:
+    """The learned surrogate on the frame it serves: config 1's camera and
+    hole (Kerr a=0.9, r=15 M, i=80 deg, 1920x1080, kernel rules) with no disc
+    or gas, so every ray either escapes or falls in.  Times the same frame
+    three ways -- plain FP32 RK4, FP32 RK4 with FP64 guards, surrogate + FP32
+    (shipped network, gate sigma) -- and scores each against the FP64 oracle
+    (Tsit5 rtol 1e-10) on a 480x270 rendering of the frame."""
+    import numpy as np
+    import torch
+    from oracle import oracle as O
+    from spacetime_gb300 import _abi, workloads
+    from spacetime_gb300.surrogate import load_trained
+    w = workloads.config1_thin()
+    w.disc = None
+    w.params = dict(samples=1, pixel_jitter=0, exit_landing=1)
+    sky = workloads.sky()
+    sur = load_trained(device)
+    ctx = ctx_cls(sky, disc=None, emitter=w.emitter, device=device)
+    ctx.set_surrogate(sur)
+    small = w.scaled(480, 270)
+    ref, rays = O.scene_for(small, sky, O.INT_TSIT5).render()
+    arms = {"plain_fp32": dict(precision=_abi.ST_PREC_FP32),
+            "fp32_fp64_guarded": dict(precision=_abi.ST_PREC_FP32_GUARDED, r_guard=3.0, crit_band=0.05,
+                                      crit_r=4.0, renorm_every=256),
+            "surrogate_fp32": dict(precision=_abi.ST_PREC_FP32, surrogate=1, surrogate_sigma=sigma)}
+    out = {"workload": "config1 camera and hole (Kerr a=0.9, r=15 M, i=80 deg, Lens(24)), 1920x1080, "
+                       "no disc or gas; kernel rules; the shipped surrogate network",
+           "sigma_gate_rad": sigma}
+    for name, kw in arms.items():
+        p = ctx.params(w.semantics, width=1920, height=1080, **w.params, **kw)
+        ctx.render_device(w.cam, w.bh, p)
+        ts = []
+        for _ in range(reps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            _, st = ctx.render_device(w.cam, w.bh, p)
+            ts.append(st["kernel_ms"])
+        ms = float(np.mean(ts))
+        ps = ctx.params(w.semantics, width=480, height=270, **w.params, **kw)
+        r = ctx.render_raw(w.cam, w.bh, ps, diag=True)
+        both = ((r.diag["flags"] & 1) > 0) & ((rays["flags"] & O.RAY_ESCAPED) > 0)
+        d = np.zeros(both.shape)
+        a, b = r.diag["dir"][both], rays["dir"][both]
+        d[both] = 2 * np.arcsin(np.clip(np.linalg.norm(a - b, axis=-1) / 2, 0, 1))
+        rel = np.abs(r.image.astype(np.float64) - ref).sum(-1) / np.maximum(ref.sum(-1), 1e-6)
+        out[name] = {"value": 1920 * 1080 / (ms * 1e-3) / 1e6, "ms_per_step": ms,
+                     "served_fraction": st["surrogate_rays"] / (1920 * 1080),
+                     "dir_median_rad": float(np.median(d)), "dir_p99_rad": float(np.percentile(d, 99)),
+                     "radiance_rel_median": float(np.median(rel)),
+                     "radiance_rel_p99": float(np.percentile(rel, 99))}
+    out["speedup_vs_plain_fp32"] = out["surrogate_fp32"]["value"] / out["plain_fp32"]["value"]
+    out["speedup_vs_fp32_fp64_guarded"] = out["surrogate_fp32"]["value"] / out["fp32_fp64_guarded"]["value"]
+    ctx.close()
+    sur.close()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -284,7 +341,7 @@ def main(argv=None):
     ap.add_argument("--workload", default="config1", choices=["config1", "config1_thin", "config2", "config4"],
                     help="config1 is the headline; the others are the remaining benchmark configurations")
     ap.add_argument("--surrogate", default=None, help="trained surrogate parameters (.npy) for config1_thin")
-    ap.add_argument("--sigma", type=float, default=1e-4, help="surrogate gate: max predicted std-dev (rad)")
+    ap.add_argument("--sigma", type=float, default=4e-4, help="surrogate gate: max predicted std-dev (rad)")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -400,6 +457,10 @@ def main(argv=None):
                               "fp64_steps_per_frame": stv["fp64_steps"]}
         for name in variants:
             variants[name]["speedup_of_value"] = value / variants[name]["value"]
+        try:
+            variants["surrogate_no_gas"] = surrogate_variant(Context, local, flush, args.sigma)
+        except Exception as e:  # report, do not fail the bench
+            variants["surrogate_no_gas"] = {"failed": str(e)}
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         try:
@@ -421,8 +482,9 @@ def main(argv=None):
             "precision": {"fp64": "FP64", "fp32": "FP32 (MUFU sqrt/rcp/exp/log)",
                           "fp32g": "FP32 RHS, float-float state, FP64 guards"}[args.precision],
             "guards": {"r_guard": args.r_guard, "crit_band": args.crit_band, "renorm_every": args.renorm},
-            "surrogate": ("not applied: every ray of this frame starts inside the gas slab, and the gas "
-                          "line integral needs the integrated path (the surrogate serves gas-free rays)")
+            "surrogate": ("not applied to this frame: every ray starts inside the gas slab, and the gas "
+                          "line integral needs the integrated path; measured on the same camera and hole "
+                          "without gas in variants.surrogate_no_gas")
                          if args.workload == "config1" else
                          ({"params": os.path.basename(args.surrogate), "sigma_gate_rad": args.sigma,
                            "served_fraction": served / (W * H)} if args.surrogate else False),

@@ -487,6 +487,7 @@ int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, 
   v->vol = p->vol_on;
   v->sem = rp->semantics;
   v->sched = rp->schedule == ST_SCHED_PERSISTENT ? ST_SCHED_PERSISTENT : ST_SCHED_PIXEL;
+  st::fill_float_copies(p);
   return ST_OK;
 }
 

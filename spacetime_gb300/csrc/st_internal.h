@@ -92,7 +92,42 @@ struct TraceParams {
   int chunk_steps;
   unsigned int* queue;       // queue head (device)
   long long budget_iters;    // per-warp loop bound of the persistent kernel
+  // single-precision copies of the parameters the per-step code reads, so a
+  // float variant never converts from double inside its loop (on GB300 every
+  // double -> float conversion issues on the FP64 pipe)
+  struct Flt {
+    float M, a, rkill2, vol_rb2, hcap, dt, hcoef, tspan, ds_gas, zmax, r_isco, E_isco, L_isco, opac, emis, disc_inner, disc_outer, disc_falloff, lut_tmin, lut_tmax, ls_in, ls_out, crit_r2, r_guard2, tol;
+  } f;
 };
+
+// Fill TraceParams::f from the double fields (host, after they are set).
+inline void fill_float_copies(TraceParams* p) {
+  p->f.M = (float)p->M;
+  p->f.a = (float)p->a;
+  p->f.rkill2 = (float)p->rkill2;
+  p->f.vol_rb2 = (float)p->vol_rb2;
+  p->f.hcap = (float)p->hcap;
+  p->f.dt = (float)p->dt;
+  p->f.hcoef = (float)p->hcoef;
+  p->f.tspan = (float)p->tspan;
+  p->f.ds_gas = (float)p->ds_gas;
+  p->f.zmax = (float)p->zmax;
+  p->f.r_isco = (float)p->r_isco;
+  p->f.E_isco = (float)p->E_isco;
+  p->f.L_isco = (float)p->L_isco;
+  p->f.opac = (float)p->opac;
+  p->f.emis = (float)p->emis;
+  p->f.disc_inner = (float)p->disc_inner;
+  p->f.disc_outer = (float)p->disc_outer;
+  p->f.disc_falloff = (float)p->disc_falloff;
+  p->f.lut_tmin = (float)p->lut_tmin;
+  p->f.lut_tmax = (float)p->lut_tmax;
+  p->f.ls_in = (float)p->ls_in;
+  p->f.ls_out = (float)p->ls_out;
+  p->f.crit_r2 = (float)p->crit_r2;
+  p->f.r_guard2 = (float)p->r_guard2;
+  p->f.tol = (float)p->tol;
+}
 
 // Variant key of the compiled kernels (the reference's Val{...} switches,
 // src/metal.jl:759-763, plus precision and schedule).

@@ -149,9 +149,11 @@ __global__ void __launch_bounds__(GEMM_THREADS) gemm_bf16_kernel(const __nv_bflo
     }
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+// SiLU and its derivative with the fast exponential and division (two MUFU
+// operations each); where exp(-z) overflows, the quotient is 0 as it should be.
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.f + __expf(-z)); }
 __device__ __forceinline__ float dsilu(float z) {
-  const float s = 1.f / (1.f + __expf(-z));
+  const float s = __fdividef(1.f, 1.f + __expf(-z));
   return s * (1.f + z * (1.f - s));
 }
 

@@ -200,6 +200,7 @@ extern "C" int st_render_frames_noalloc(const float* dev_sky_rgba, int sky_w, in
   v.sched = ST_SCHED_PERSISTENT;
   int nsm = 0;
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return ST_ECUDA;
+  st::fill_float_copies(&p);
   if (st::launch_trace(v, p, 0, 0, nsm, s) != cudaSuccess) return ST_ECUDA;
   unsigned long long cnt[st::CNT_N];
   if (cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, s) != cudaSuccess) return ST_ECUDA;

@@ -867,13 +867,14 @@ __global__ void __launch_bounds__(128) sur_inputs_kernel(const __grid_constant__
   fl[row] = flags;
 }
 
-// Gate of every pixel from the network's outputs (one thread per pixel,
-// warp-ordered append of the pixels left to integrate).
+// Gate of every pixel from the network's outputs (one thread per pixel).
+// Served pixels are written; each warp records which of its pixels are left
+// to integrate (mask, count) for the ordered compaction below.
 __global__ void __launch_bounds__(128) sur_gate_kernel(const __grid_constant__ TraceParams p,
                                                         const __grid_constant__ SurFrame f,
                                                         const float* __restrict__ O, const float4* __restrict__ aux,
                                                         const int* __restrict__ fl, const int* __restrict__ status,
-                                                        int* list, int* count) {
+                                                        unsigned* __restrict__ wmask, int* __restrict__ wcount) {
   const int row = blockIdx.x * 128 + threadIdx.x, lane = threadIdx.x & 31;
   const int pix = tile_pixel(p, blockIdx.x, threadIdx.x);
   float o[NOUT];
@@ -884,23 +885,56 @@ __global__ void __launch_bounds__(128) sur_gate_kernel(const __grid_constant__ T
   // a tile whose network pass failed (status[t] != 0) is integrated whole
   const bool serve = pix >= 0 && status[blockIdx.x] == 0 && gate_pixel(p, f, o, aux[row], fl[row], &rgba, dird);
   const unsigned want = __ballot_sync(0xffffffffu, pix >= 0 && !serve);
-  int base_i = 0;
-  if (lane == 0 && want) base_i = atomicAdd(count, __popc(want));
-  base_i = __shfl_sync(0xffffffffu, base_i, 0);
-  if (pix < 0) return;
-  if (serve) {
-    p.out[pix] = rgba;
-    if (p.diag) {
-      st_ray_diag d;
-      d.dir[0] = dird[0]; d.dir[1] = dird[1]; d.dir[2] = dird[2];
-      d.r_final = 0.f; d.alpha = 1.f; d.r_cross = -1.f; d.g_cross = 0.f; d.lambda = 0.f;
-      d.flags = ST_RAY_SURROGATE | ST_RAY_ESCAPED;
-      d.steps = 0; d.fp64_steps = 0; d.pad[0] = d.pad[1] = 0;
-      p.diag[pix] = d;
-    }
-  } else {
-    list[base_i + __popc(want & ((1u << lane) - 1u))] = pix;
+  if (lane == 0) {
+    wmask[row >> 5] = want;
+    wcount[row >> 5] = __popc(want);
   }
+  if (pix < 0 || !serve) return;
+  p.out[pix] = rgba;
+  if (p.diag) {
+    st_ray_diag d;
+    d.dir[0] = dird[0]; d.dir[1] = dird[1]; d.dir[2] = dird[2];
+    d.r_final = 0.f; d.alpha = 1.f; d.r_cross = -1.f; d.g_cross = 0.f; d.lambda = 0.f;
+    d.flags = ST_RAY_SURROGATE | ST_RAY_ESCAPED;
+    d.steps = 0; d.fp64_steps = 0; d.pad[0] = d.pad[1] = 0;
+    p.diag[pix] = d;
+  }
+}
+
+// Exclusive prefix sum of the per-warp counts in one CTA of 1024 threads
+// (each thread a contiguous run), and the total into *count.
+__global__ void __launch_bounds__(1024) sur_scan_kernel(const int* __restrict__ wcount, int* __restrict__ woff,
+                                                         int nwarps, int* count) {
+  __shared__ int part[1024];
+  const int t = threadIdx.x;
+  const int per = (nwarps + 1023) / 1024;
+  const int b = t * per, e = min(b + per, nwarps);
+  int sum = 0;
+  for (int i = b; i < e; ++i) sum += wcount[i];
+  part[t] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const int v = t >= off ? part[t - off] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  int run = part[t] - sum;  // exclusive prefix of this thread's run
+  for (int i = b; i < e; ++i) {
+    woff[i] = run;
+    run += wcount[i];
+  }
+  if (t == 1023) *count = part[1023];
+}
+
+// Pixels left to integrate, in tile raster order (warp by warp).
+__global__ void __launch_bounds__(128) sur_scatter_kernel(const __grid_constant__ TraceParams p,
+                                                           const unsigned* __restrict__ wmask,
+                                                           const int* __restrict__ woff, int* __restrict__ list) {
+  const int row = blockIdx.x * 128 + threadIdx.x, lane = threadIdx.x & 31;
+  const unsigned m = wmask[row >> 5];
+  if (!((m >> lane) & 1u)) return;
+  list[woff[row >> 5] + __popc(m & ((1u << lane) - 1u))] = tile_pixel(p, blockIdx.x, threadIdx.x);
 }
 
 // The network on the tensor cores: X[tiles*128][6] -> O[tiles*128][6]; one
@@ -1072,6 +1106,9 @@ struct st_surrogate {
   int* fFl = nullptr;
   float* fO = nullptr;
   int* fStatus = nullptr;
+  unsigned* fMask = nullptr;  // per warp of rows: pixels left to integrate
+  int* fCount = nullptr;      // per warp: their number
+  int* fOff = nullptr;        // per warp: offset in the list
   long long frows = 0;
   int cap = 0;  // rows of the work buffers
   float* X = nullptr;
@@ -1388,13 +1425,19 @@ int surrogate_frame(st_surrogate* s, const TraceParams& p, const Variant& v, con
     const long long rows = (long long)nb * sur::TC_ROWS;
     if (s->frows < rows) {
       cudaFree(s->fX); cudaFree(s->fAux); cudaFree(s->fFl); cudaFree(s->fO); cudaFree(s->fStatus);
+      cudaFree(s->fMask); cudaFree(s->fCount); cudaFree(s->fOff);
       s->fX = nullptr; s->fAux = nullptr; s->fFl = nullptr; s->fO = nullptr; s->fStatus = nullptr;
+      s->fMask = nullptr; s->fCount = nullptr; s->fOff = nullptr;
       s->frows = 0;
+      const size_t nw = (size_t)rows / 32;
       if (cudaMalloc(&s->fX, rows * sur::NIN * sizeof(float)) != cudaSuccess ||
           cudaMalloc(&s->fAux, rows * sizeof(float4)) != cudaSuccess ||
           cudaMalloc(&s->fFl, rows * sizeof(int)) != cudaSuccess ||
           cudaMalloc(&s->fO, rows * sur::NOUT * sizeof(float)) != cudaSuccess ||
-          cudaMalloc(&s->fStatus, (size_t)nb * sizeof(int)) != cudaSuccess)
+          cudaMalloc(&s->fStatus, (size_t)nb * sizeof(int)) != cudaSuccess ||
+          cudaMalloc(&s->fMask, nw * sizeof(unsigned)) != cudaSuccess ||
+          cudaMalloc(&s->fCount, nw * sizeof(int)) != cudaSuccess ||
+          cudaMalloc(&s->fOff, nw * sizeof(int)) != cudaSuccess)
         return ST_ENOMEM;
       s->frows = rows;
     }
@@ -1406,7 +1449,11 @@ int surrogate_frame(st_surrogate* s, const TraceParams& p, const Variant& v, con
     sur::sur_mlp_tc_kernel<<<nb, sur::TC_THREADS, sur::TC_SMEM, stream>>>(s->P, s->Wsw, s->fX, s->fO, s->fStatus,
                                                                           p.counters);
     SC(cudaGetLastError());
-    sur::sur_gate_kernel<<<nb, 128, 0, stream>>>(p, f, s->fO, s->fAux, s->fFl, s->fStatus, list, count);
+    sur::sur_gate_kernel<<<nb, 128, 0, stream>>>(p, f, s->fO, s->fAux, s->fFl, s->fStatus, s->fMask, s->fCount);
+    SC(cudaGetLastError());
+    sur::sur_scan_kernel<<<1, 1024, 0, stream>>>(s->fCount, s->fOff, (int)(rows / 32), count);
+    SC(cudaGetLastError());
+    sur::sur_scatter_kernel<<<nb, 128, 0, stream>>>(p, s->fMask, s->fOff, list);
   }
   SC(cudaGetLastError());
   return ST_OK;

@@ -47,6 +47,12 @@ __device__ __forceinline__ float fabs_(float x) { return fabsf(x); }
 __device__ __forceinline__ double fabs_(double x) { return fabs(x); }
 __device__ __forceinline__ float floor_(float x) { return floorf(x); }
 __device__ __forceinline__ double floor_(double x) { return floor(x); }
+// A parameter in the variant's precision: the float copy for float code, the
+// double for double code (no conversion either way).
+template <typename R> __device__ __forceinline__ R pr(double d, float f);
+template <> __device__ __forceinline__ float pr<float>(double, float f) { return f; }
+template <> __device__ __forceinline__ double pr<double>(double d, float) { return d; }
+#define PR(x) pr<R>(p.x, p.f.x)
 template <typename R> __device__ __forceinline__ R min_(R a, R b) { return a < b ? a : b; }
 template <typename R> __device__ __forceinline__ R max_(R a, R b) { return a > b ? a : b; }
 template <typename R> __device__ __forceinline__ R clamp_(R x, R lo, R hi) { return x < lo ? lo : (x > hi ? hi : x); }
@@ -211,7 +217,7 @@ __device__ __forceinline__ R emitter_opz(R sx, R sy, R psx, R psy, R E, R M, R a
 // LUT colour; RENDER rounds half to even (Julia round), DRAFT truncates x+0.5.
 template <typename R>
 __device__ __forceinline__ float4 lut_color(const TraceParams& p, R T, bool render_rule) {
-  const R tmin = R(p.lut_tmin), tmax = R(p.lut_tmax);
+  const R tmin = PR(lut_tmin), tmax = PR(lut_tmax);
   const R fr = (clamp_(T, tmin, tmax) - tmin) / (tmax - tmin);
   int idx;
   if (render_rule) idx = (int)rint(fr * R(p.lut_size - 1));
@@ -223,10 +229,10 @@ __device__ __forceinline__ float4 lut_color(const TraceParams& p, R T, bool rend
 // Trilinear gas density, src/metal.jl:569-610.
 template <typename R>
 __device__ __forceinline__ R sample_volume(const TraceParams& p, R sc, R phi, R z) {
-  const R zmax = R(p.zmax);
+  const R zmax = PR(zmax);
   if (sc <= R(0) || fabs_(z) >= zmax) return R(0);
   const R ls = log_(sc);
-  const R lin = R(p.ls_in), lout = R(p.ls_out);
+  const R lin = PR(ls_in), lout = PR(ls_out);
   if (ls <= lin || ls >= lout) return R(0);
   const int nr = p.nr, nphi = p.nphi, nz = p.nz;
   const R two_pi = R(6.283185307179586);
@@ -517,7 +523,7 @@ __device__ void init_ray(const TraceParams& p, const CamView& cam, int i0, int j
   st.alpha = R(1);
   st.r_prev = R(-1);
   const D r0 = sqrt_(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
-  st.r_floor = r0 > D(2.05) * D(p.M) ? R(2) * R(p.M) : R(0.3) * R(p.M);
+  st.r_floor = r0 > D(2.05) * D(p.M) ? R(2) * PR(M) : R(0.3) * PR(M);
   st.inside0 = r0 < D(2.00001);
   st.march_acc = R(0);
   st.lambda = R(0);
@@ -574,9 +580,9 @@ __device__ __forceinline__ void land_on_sphere(const R* yp, R pt, R M, R a, R h,
 
 template <typename R>
 __device__ __forceinline__ R disc_kepler(const TraceParams& p, R X0, R X1, const R* Pm, R pt, R gcam, R* acc, R* alpha) {
-  const R M = R(p.M);
+  const R M = PR(M);
   const R r = sqrt_(X0 * X0 + X1 * X1);
-  if (!(R(p.disc_inner) < r && r < R(p.disc_outer))) return R(0);
+  if (!(PR(disc_inner) < r && r < PR(disc_outer))) return R(0);
   const R f = R(2) * M / r;
   const R kap = (X0 * Pm[0] + X1 * Pm[1]) / r;
   const R c1 = f * (-pt + kap) / r;
@@ -595,11 +601,11 @@ __device__ __forceinline__ R disc_kepler(const TraceParams& p, R X0, R X1, const
   const R T_obs = T_emit * gcam / max_(opz_d * opz_g, R(0.1));
   const R inten = R(100) / (exp_(R(29622.4) / max_(T_obs, R(1))) - R(1));
   const float4 col = lut_color(p, T_obs, true);
-  const R R_in = R(p.disc_inner) / (R(2) * M), R_out = R(p.disc_outer) / (R(2) * M);
+  const R R_in = PR(disc_inner) / (R(2) * M), R_out = PR(disc_outer) / (R(2) * M);
   const R iscotaper = clamp_((R_ * R_ - R_in * R_in) * R(0.3), R(0), R(1));
   const R outertaper = clamp_(T_emit / R(1000), R(0), R(1));
   const R dens = clamp_((R_out - R_) / (R_out - R_in), R(0), R(1));
-  const R fall = R(p.disc_falloff);
+  const R fall = PR(disc_falloff);
   const R dpow = (fall == R(0)) ? R(1) : (dens <= R(0) ? R(0) : exp_(fall * log_(dens)));
   const R op = iscotaper * outertaper * dpow;
   const R w = inten * (*alpha * op);
@@ -610,24 +616,24 @@ __device__ __forceinline__ R disc_kepler(const TraceParams& p, R X0, R X1, const
 
 template <typename R>
 __device__ __forceinline__ R disc_exact(const TraceParams& p, R xh, R yh, R pxh, R pyh, R pt, R scam, R* acc, R* alpha) {
-  const R M = R(p.M);
+  const R M = PR(M);
   const R sc = sqrt_(xh * xh + yh * yh);
-  if (!(R(p.disc_inner) < sc && sc < R(p.disc_outer))) return R(0);
-  const R r_isco = R(p.r_isco);
+  if (!(PR(disc_inner) < sc && sc < PR(disc_outer))) return R(0);
+  const R r_isco = PR(r_isco);
   const R R_ = sc / (R(2) * M);
   const R RT = max_(sc, r_isco) / (R(2) * M);
   const R T_emit = exp_(R(10.034259) - R(0.375) * log_(RT * RT));
   const R t3 = sc / r_isco;
   const R plunge = sc < r_isco ? t3 * t3 * t3 : R(1);
-  const R opz = emitter_opz(xh, yh, pxh, pyh, -pt, M, R(p.a), r_isco, R(p.E_isco), R(p.L_isco));
+  const R opz = emitter_opz(xh, yh, pxh, pyh, -pt, M, PR(a), r_isco, PR(E_isco), PR(L_isco));
   const R T_obs = T_emit * scam / opz;
   const R inten = R(100) / (exp_(R(29622.4) / max_(T_obs, R(1))) - R(1));
   const float4 col = lut_color(p, T_obs, false);
-  const R R_in = R(p.disc_inner) / (R(2) * M), R_out = R(p.disc_outer) / (R(2) * M);
+  const R R_in = PR(disc_inner) / (R(2) * M), R_out = PR(disc_outer) / (R(2) * M);
   const R iscotaper = clamp_((R_ * R_ - R_in * R_in) * R(0.3), R(0), R(1));
   const R outertaper = clamp_(T_emit / R(1000), R(0), R(1));
   const R dens = clamp_((R_out - R_) / (R_out - R_in), R(0), R(1));
-  const R fall = R(p.disc_falloff);
+  const R fall = PR(disc_falloff);
   const R dpow = dens <= R(1e-6) ? (fall > R(0) ? R(0) : R(1)) : exp_(fall * log_(dens));
   const R op = iscotaper * outertaper * dpow * plunge;
   const R w = *alpha * op * inten;
@@ -642,15 +648,15 @@ template <typename R>
 __device__ __forceinline__ bool march_gas(const TraceParams& p, const R* yp, const R* yn, R r2p, R h_used, R vlen,
                                           RayState<R>& st) {
   const R r2n = yn[0] * yn[0] + yn[1] * yn[1] + yn[2] * yn[2];
-  if (!(st.alpha > R(0.003) && min_(r2p, r2n) < R(p.vol_rb2))) return false;
-  const R ds = R(p.ds_gas);
+  if (!(st.alpha > R(0.003) && min_(r2p, r2n) < PR(vol_rb2))) return false;
+  const R ds = PR(ds_gas);
   const R seg = h_used * vlen;
   // a step spans at most a few M of arc; anything else (overflow, NaN) is not marched
   if (!(seg < R(64))) return false;
   R t_s = ds - st.march_acc;
   if (t_s > seg) { st.march_acc += seg; return false; }
-  const R zmax = R(p.zmax);
-  const R r_isco = R(p.r_isco), M = R(p.M);
+  const R zmax = PR(zmax);
+  const R r_isco = PR(r_isco), M = PR(M);
   const R inv_seg = R(1) / seg;
   // bounded: seg < 64 and ds >= dt, so at most 64/dt + 1 samples (capped at 8192)
   for (int guard = 0; guard < 8192 && t_s <= seg && st.alpha > R(0.003); ++guard) {
@@ -670,13 +676,13 @@ __device__ __forceinline__ bool march_gas(const TraceParams& p, const R* yp, con
           if (scyl < r_isco) { const R t3 = scyl / r_isco; rho *= t3 * t3 * t3; }
           const R psx = yp[3] + fs * (yn[3] - yp[3]);
           const R psy = yp[4] + fs * (yn[4] - yp[4]);
-          const R opz = emitter_opz(sx, sy, psx, psy, -st.pt, M, R(p.a), r_isco, R(p.E_isco), R(p.L_isco));
+          const R opz = emitter_opz(sx, sy, psx, psy, -st.pt, M, PR(a), r_isco, PR(E_isco), PR(L_isco));
           const R T_obs = T_emit * st.scam / opz;
           const R inten = R(100) / (exp_(R(29622.4) / max_(T_obs, R(1))) - R(1));
           const float4 col = lut_color(p, T_obs, false);
-          const R tau = R(p.opac) * rho * ds;
+          const R tau = PR(opac) * rho * ds;
           const R aa = R(1) - exp_(-tau);
-          const R w = st.alpha * aa * inten * R(p.emis);
+          const R w = st.alpha * aa * inten * PR(emis);
           st.acc[0] += w * R(col.x); st.acc[1] += w * R(col.y); st.acc[2] += w * R(col.z);
           st.alpha *= (R(1) - aa);
         }
@@ -832,7 +838,7 @@ __device__ __forceinline__ void renorm_fp64(float* y, float* lo, float pt, doubl
 template <int PREC, int KERR, int VOL, int SEM, int ORD = 4>
 __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename RealOf<PREC>::T>& st) {
   using R = typename RealOf<PREC>::T;
-  const R M = R(p.M), a = R(p.a);
+  const R M = PR(M), a = PR(a);
   R* y = st.y;
   const R r2 = y[0] * y[0] + y[1] * y[1] + y[2] * y[2];
   const R r = sqrt_(r2);
@@ -841,7 +847,7 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
   if constexpr (SEM == ST_SEM_DRAFT) {
     if constexpr (KERR) {
       rk2 = ks_r2(y[0], y[1], y[2], a);
-      if (rk2 < R(p.rkill2)) { st.flags |= ST_RAY_CAPTURED; return true; }
+      if (rk2 < PR(rkill2)) { st.flags |= ST_RAY_CAPTURED; return true; }
     } else {
       if (r < R(3.2) * M) {
         if (r < st.r_floor || (r < R(2.95) * M && st.r_prev > R(0) && r < st.r_prev - R(1e-4) * M)) {
@@ -854,7 +860,7 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
     if (r > st.r_esc) { st.flags |= ST_RAY_ESCAPED; return true; }
   } else {
     if (r >= st.r_esc) { st.flags |= ST_RAY_ESCAPED; return true; }
-    if (st.lambda >= R(p.tspan)) { st.flags |= ST_RAY_BUDGET; return true; }
+    if (st.lambda >= PR(tspan)) { st.flags |= ST_RAY_BUDGET; return true; }
     // A ray moving inward below 2.95M never escapes (escaping rays have
     // periapsis > 3M).  In ingoing KS coordinates the backward ray reaches the
     // past horizon only asymptotically, which a fixed step cannot follow, so
@@ -867,14 +873,14 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
     st.r_prev = r;
   }
   // radius-adaptive step, src/metal.jl:1250-1260
-  const R cap = (VOL && r2 < R(p.vol_rb2)) ? R(2) : R(p.hcap);
-  R h = R(p.dt) * min_(max_(R(p.hcoef) * r / M, R(1)), cap);
+  const R cap = (VOL && r2 < PR(vol_rb2)) ? R(2) : PR(hcap);
+  R h = PR(dt) * min_(max_(PR(hcoef) * r / M, R(1)), cap);
   if constexpr (KERR) {
-    const R rk = R(p.rkill2);
+    const R rk = PR(rkill2);
     const R fr = clamp_((rk2 - rk) / max_(rk, R(1e-6)), R(0), R(1));
     h *= R(0.12) + R(0.88) * fr;
   }
-  if constexpr (SEM == ST_SEM_RENDER) h = min_(h, R(p.tspan) - st.lambda);
+  if constexpr (SEM == ST_SEM_RENDER) h = min_(h, PR(tspan) - st.lambda);
 
   R yp[6];
 #pragma unroll
@@ -893,19 +899,19 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
 
   bool fp64_step = false;
   if constexpr (PREC == ST_PREC_FP32_GUARDED) {
-    fp64_step = (st.guard_ray && (p.crit_r2 <= 0.0 || rk2 < R(p.crit_r2))) ||
-                (!(st.flags & ST_RAY_BCAPT) && rk2 < R(p.r_guard2));
+    fp64_step = (st.guard_ray && (PR(crit_r2) <= R(0) || rk2 < PR(crit_r2))) ||
+                (!(st.flags & ST_RAY_BCAPT) && rk2 < PR(r_guard2));
   }
   if constexpr (ORD == 45 || ORD == 46) {
     // adaptive Tsit5 (src/metal.jl:1278-1381); 45 caps the step at the
     // radius-adaptive h, 46 runs free up to 50 dt with the thin-disc approach guard
     R hmax = h;
     if constexpr (ORD == 46) {
-      hmax = R(50) * R(p.dt);
-      if (!VOL && p.disc_on) hmax = min_(hmax, max_(h, R(0.5) * (r - R(p.disc_outer))));
+      hmax = R(50) * PR(dt);
+      if (!VOL && p.disc_on) hmax = min_(hmax, max_(h, R(0.5) * (r - PR(disc_outer))));
     }
     R sn[6], k7[6];
-    h = tsit5_adaptive<KERR>(yp, st.pt, M, a, r, h, hmax, R(p.tol), R(p.dt), k1, sn, k7, st.h_carry, st.err_prev);
+    h = tsit5_adaptive<KERR>(yp, st.pt, M, a, r, h, hmax, PR(tol), PR(dt), k1, sn, k7, st.h_carry, st.err_prev);
 #pragma unroll
     for (int k = 0; k < 6; ++k) { y[k] = sn[k]; st.k1c[k] = k7[k]; }
     st.k1_valid = true;
@@ -1065,7 +1071,7 @@ template <int PREC, int KERR, int SEM>
 __device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typename RealOf<PREC>::T>& st, int out_index,
                                            int diag_index) {
   using R = typename RealOf<PREC>::T;
-  const R M = R(p.M), a = R(p.a);
+  const R M = PR(M), a = PR(a);
   R yv[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) yv[k] = st.y[k];
