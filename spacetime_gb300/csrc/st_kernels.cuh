@@ -9,6 +9,11 @@
 #ifndef ST_MINB
 #define ST_MINB 1
 #endif
+// The adaptive Tsit5 modes (order 45 / 46) hold more state per ray; they keep
+// the budget of at most 5 blocks.
+#ifndef ST_MINB_ADAPTIVE
+#define ST_MINB_ADAPTIVE (ST_MINB < 5 ? ST_MINB : 5)
+#endif
 
 namespace st {
 
@@ -35,7 +40,7 @@ __device__ __forceinline__ void flush_counters(const TraceParams& p, unsigned lo
 // One thread per pixel over a 2-D grid of tiles (blockDim.x * blockDim.y a
 // multiple of 32; threads are linearised so a warp covers a compact tile).
 template <int PREC, int KERR, int VOL, int SEM, int ORD = 4>
-__global__ void __launch_bounds__(128, ST_MINB) trace_pixel_kernel(const __grid_constant__ TraceParams p) {
+__global__ void __launch_bounds__(128, ORD == 4 ? ST_MINB : ST_MINB_ADAPTIVE) trace_pixel_kernel(const __grid_constant__ TraceParams p) {
   using R = typename RealOf<PREC>::T;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int j = blockIdx.y * blockDim.y + threadIdx.y;

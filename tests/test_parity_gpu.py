@@ -87,12 +87,18 @@ def test_kerr_volume_fp32_vs_tsit5(built_lib, sky, prec):
 
 
 def test_persistent_schedule_matches_pixel(built_lib, sky):
+    """Same rays, same steps; the two kernels are separate float compilations
+    (multiply-add contraction may differ), so radiance agrees to 1e-3 relative
+    on all but 1 % of pixels rather than bit for bit."""
     w = workloads.config1().scaled(200, 120)
     a = gpu_render(w, sky, FP32G, schedule=_abi.ST_SCHED_PIXEL)
     b = gpu_render(w, sky, FP32G, schedule=_abi.ST_SCHED_PERSISTENT, chunk_steps=16)
     assert b.stats["status"] == _abi.ST_OK
     assert a.stats["steps"] == b.stats["steps"]
-    np.testing.assert_array_equal(a.image, b.image)
+    rel = np.abs(a.image - b.image).sum(-1) / np.maximum(np.abs(a.image).sum(-1), 1e-6)
+    assert (rel > 1e-3).mean() <= 0.01, (rel > 1e-3).mean()
+    c = compare(b.image, b.diag, a.image.astype(np.float64), a.diag)
+    assert c["class_mismatch"] <= 2 and c["dir_median"] <= 1e-5, c
 
 
 @pytest.mark.parametrize("order,twin", [(45, O.INT_TSIT5_K45), (46, O.INT_TSIT5_K46)])
