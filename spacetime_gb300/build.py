@@ -19,7 +19,7 @@ LIB = os.environ.get("SPACETIME_GB300_LIB", os.path.join(HERE, "libspacetime_gb3
 # exp and log (their double arithmetic is unaffected) and ask ptxas for enough
 # resident blocks per SM to keep FP32 latency hidden
 FAST = os.environ.get("ST_FASTMATH", "1") == "1"
-MINB_FP32 = os.environ.get("ST_MINB_FP32", "5")
+MINB_FP32 = os.environ.get("ST_MINB_FP32", "7")
 MINB_FP32G = os.environ.get("ST_MINB_FP32G", "4")
 UNIT_FLAGS = {
     "st_trace_fp32.cu": (["--use_fast_math"] if FAST else []) + [f"-DST_MINB={MINB_FP32}"],
