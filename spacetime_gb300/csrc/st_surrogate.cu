@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
@@ -807,7 +808,7 @@ __global__ void __launch_bounds__(FTHREADS, 1)
 // Every wait on an mbarrier is bounded; a wait that runs out marks the tile
 // failed (its pixels all go to the integrator, so the frame stays exact), sets
 // the status word, and the CTA still frees its TMEM.
-constexpr uint32_t TC_ROWS = 128, TC_THREADS = 256;
+constexpr uint32_t TC_ROWS = 128, TC_THREADS = 512;
 constexpr uint32_t TC_A_BYTES = TC_ROWS * NH * 2;  // 64 KB activation tile
 constexpr uint32_t TC_B_BYTES = NH * NH * 2;       // 128 KB weight tile
 constexpr uint32_t TC_TMEM_COLS = 256;
@@ -815,8 +816,9 @@ constexpr uint32_t TC_WAIT_LIMIT = 1u << 22;
 constexpr uint32_t TC_IDESC = tc::idesc_bf16_f32(128, 256);
 
 struct TcSmall {
-  float X[TC_ROWS * NIN];
-  float Opart[2][TC_ROWS * NOUT];
+  float X[TC_ROWS * NIN];     // this tile's inputs (bulk copy)
+  // the FP32 edge-layer parameters and hidden biases, in the order of the
+  // packed device image Psmall (bulk copy)
   float W0[NH * NIN];
   float b0[NH];
   float bh[3][NH];
@@ -826,6 +828,10 @@ struct TcSmall {
   uint32_t tmem;
   int fail;
 };
+constexpr uint32_t TC_SMALL_BYTES = (NH * NIN + NH + 3 * NH + NOUT * NH + 8) * 4;
+static_assert(TC_SMALL_BYTES % 16 == 0 && offsetof(TcSmall, W0) % 16 == 0, "bulk-copy alignment");
+static_assert(offsetof(TcSmall, b4) + 8 * 4 - offsetof(TcSmall, W0) == TC_SMALL_BYTES, "packed layout");
+constexpr uint32_t TC_X_BYTES = TC_ROWS * NIN * 4;
 constexpr size_t TC_SMEM = 1024 + TC_A_BYTES + TC_B_BYTES + sizeof(TcSmall);
 static_assert(TC_SMEM <= 227 * 1024, "tensor-core surrogate tile exceeds shared memory");
 
@@ -851,6 +857,22 @@ __device__ __forceinline__ int tile_pixel(const TraceParams& p, int t, int r) {
 }
 
 // Network inputs of every pixel, row-ordered by tile (one thread per pixel).
+// The FP32 edge layers and hidden biases packed as TcSmall holds them.
+__global__ void pack_small(const float* __restrict__ P, float* __restrict__ S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int n0 = NH * NIN, n1 = n0 + NH, n2 = n1 + 3 * NH, n3 = n2 + NOUT * NH, n4 = n3 + 8;
+  if (i >= n4) return;
+  float v;
+  if (i < n0) v = P[OW0 + i];
+  else if (i < n1) v = P[OB0 + (i - n0)];
+  else if (i < n2) {
+    const int l = (i - n1) / NH, k = (i - n1) % NH;
+    v = P[(l == 0 ? OB1 : l == 1 ? OB2 : OB3) + k];
+  } else if (i < n3) v = P[OW4 + (i - n2)];
+  else v = (i - n3) < NOUT ? P[OB4 + (i - n3)] : 0.f;
+  S[i] = v;
+}
+
 template <int KERR>
 __global__ void __launch_bounds__(128) sur_inputs_kernel(const __grid_constant__ TraceParams p,
                                                           const __grid_constant__ SurFrame f, float* __restrict__ X,
@@ -938,10 +960,12 @@ __global__ void __launch_bounds__(128) sur_scatter_kernel(const __grid_constant_
 }
 
 // The network on the tensor cores: X[tiles*128][6] -> O[tiles*128][6]; one
-// CTA per 128 rows.  tile_status[t] = 0, or 1 when a bounded wait ran out
-// (the gate then integrates the tile's pixels, and the status word is set).
+// CTA per 128 rows, 16 warps.  tile_status[t] = 0, or 1 when a bounded wait
+// ran out (the gate then integrates the tile's pixels, and the status word is
+// set).  The weights of hidden layer 1, the packed FP32 parameters and the
+// tile's inputs arrive together on one mbarrier.
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    sur_mlp_tc_kernel(const float* __restrict__ P, const unsigned char* __restrict__ Wsw,
+    sur_mlp_tc_kernel(const float* __restrict__ Psmall, const unsigned char* __restrict__ Wsw,
                       const float* __restrict__ X, float* __restrict__ O, int* __restrict__ tile_status,
                       unsigned long long* counters) {
   extern __shared__ unsigned char tsm_raw[];
@@ -964,30 +988,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   tc::fence_after_sync();
   const uint32_t tmem = S.tmem;
   if (tid == 0) {
-    tc::mbar_expect_tx(&S.bar_w, TC_B_BYTES);
+    tc::mbar_expect_tx(&S.bar_w, TC_B_BYTES + TC_SMALL_BYTES + TC_X_BYTES);
 #pragma unroll
     for (int c = 0; c < 4; ++c) tc::bulk_g2s(Bs + c * 32768, Wsw + c * 32768, 32768, &S.bar_w);
+    tc::bulk_g2s(S.W0, Psmall, TC_SMALL_BYTES, &S.bar_w);
+    tc::bulk_g2s(S.X, X + row0 * NIN, TC_X_BYTES, &S.bar_w);
   }
-  // small FP32 operands, and this tile's inputs (coalesced)
-  for (int c = tid; c < NH * NIN; c += TC_THREADS) S.W0[c] = P[OW0 + c];
-  for (int c = tid; c < NH; c += TC_THREADS) {
-    S.b0[c] = P[OB0 + c];
-    S.bh[0][c] = P[OB1 + c];
-    S.bh[1][c] = P[OB2 + c];
-    S.bh[2][c] = P[OB3 + c];
-  }
-  for (int c = tid; c < NOUT * NH; c += TC_THREADS) S.W4[c] = P[OW4 + c];
-  if (tid < NOUT) S.b4[tid] = P[OB4 + tid];
-  for (int c = tid; c < (int)(TC_ROWS * NIN); c += TC_THREADS) S.X[c] = X[row0 * NIN + c];
+  if (!tc::mbar_wait(&S.bar_w, 0, TC_WAIT_LIMIT)) S.fail = 1;
   __syncthreads();
-  // layer 0 (FP32): thread = hidden unit n, all 128 rows, into the swizzled tile
-  {
-    const int n = tid;
+  const bool start_ok = S.fail == 0;
+  // layer 0 (FP32): thread = hidden unit n over one half of the rows
+  if (start_ok) {
+    const int n = tid & (NH - 1), r0 = (tid >> 8) * (TC_ROWS / 2);
     float w0[NIN];
 #pragma unroll
     for (int i = 0; i < NIN; ++i) w0[i] = S.W0[n * NIN + i];
     const float bb = S.b0[n];
-    for (int r = 0; r < (int)TC_ROWS; ++r) {
+#pragma unroll 4
+    for (int r = r0; r < r0 + (int)TC_ROWS / 2; ++r) {
       float z = bb;
 #pragma unroll
       for (int i = 0; i < NIN; ++i) z += S.X[r * NIN + i] * w0[i];
@@ -997,11 +1015,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   tc::fence_proxy_async();
   __syncthreads();
   const uint32_t a_addr = tc::smem_u32(As), b_addr = tc::smem_u32(Bs);
-  const uint32_t q = warp & 3, half = warp >> 2;
+  // warp w: TMEM lanes (rows) 32 (w mod 4).., columns 64 (w div 4)..
+  const uint32_t q = warp & 3, cq = warp >> 2;
   const int row = (int)(q * 32 + lane);
   float part[NOUT] = {0, 0, 0, 0, 0, 0};
   uint32_t ph = 0;
-  for (int l = 0; l < 3; ++l) {
+  for (int l = 0; l < 3 && start_ok; ++l) {
     if (tid == 0) {
       if (tc::mbar_wait(&S.bar_w, ph, TC_WAIT_LIMIT)) {
         tc::fence_after_sync();
@@ -1031,8 +1050,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tc::bulk_g2s(Bs + c * 32768, Wsw + (size_t)(l + 1) * TC_B_BYTES + c * 32768, 32768, &S.bar_w);
     }
 #pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-      const int col0 = (int)half * 128 + c * 32;
+    for (int c = 0; c < 2; ++c) {
+      const int col0 = (int)cq * 64 + c * 32;
       float v[32];
       tc::tmem_ld32(tmem + ((q * 32u) << 16) + (uint32_t)col0, v);
       if (l < 2) {
@@ -1064,9 +1083,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
   }
   const bool failed = S.fail != 0;
+  // layer-4 partial sums over each warp's 64 columns, in the weight tile
+  // (free: the last MMA has completed and no copy targets it)
+  float* Opart = reinterpret_cast<float*>(Bs);
   if (!failed) {
 #pragma unroll
-    for (int o = 0; o < NOUT; ++o) S.Opart[half][row * NOUT + o] = part[o];
+    for (int o = 0; o < NOUT; ++o) Opart[(cq * TC_ROWS + row) * NOUT + o] = part[o];
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -1081,7 +1103,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (failed) return;
   for (int c = tid; c < (int)(TC_ROWS * NOUT); c += TC_THREADS) {
     const int r = c / NOUT, k = c - r * NOUT;
-    O[row0 * NOUT + c] = S.Opart[0][r * NOUT + k] + S.Opart[1][r * NOUT + k] + S.b4[k];
+    float acc = S.b4[k];
+#pragma unroll
+    for (int g = 0; g < 4; ++g) acc += Opart[(g * TC_ROWS + r) * NOUT + k];
+    O[row0 * NOUT + c] = acc;
   }
 }
 
@@ -1100,6 +1125,7 @@ struct st_surrogate {
   float *P = nullptr, *G = nullptr, *Mm = nullptr, *Vv = nullptr;
   __nv_bfloat16* Wb[3] = {nullptr, nullptr, nullptr};
   unsigned char* Wsw = nullptr;  // hidden layers as swizzled bf16 images for the tcgen05 frame kernel
+  float* Psmall = nullptr;       // FP32 edge layers and biases packed for the same kernel
   // frame-pass buffers, rows in tile order: inputs, launch data, outputs, per-tile status
   float* fX = nullptr;
   float4* fAux = nullptr;
@@ -1159,6 +1185,8 @@ int sync_bf16(st_surrogate* s) {
     SC(cudaGetLastError());
   }
   pack_sw128<<<(3 * NH * NH + 255) / 256, 256, 0, s->stream>>>(s->P, s->Wsw);
+  SC(cudaGetLastError());
+  pack_small<<<(TC_SMALL_BYTES / 4 + 255) / 256, 256, 0, s->stream>>>(s->P, s->Psmall);
   SC(cudaGetLastError());
   return ST_OK;
 }
@@ -1239,6 +1267,7 @@ int st_surrogate_create(st_surrogate** out, int device, unsigned long long seed)
   for (int l = 0; l < 3; ++l)
     if (cudaMalloc(&s->Wb[l], NH * NH * 2) != cudaSuccess) return fail(ST_ENOMEM);
   if (cudaMalloc(&s->Wsw, 3 * (size_t)TC_B_BYTES) != cudaSuccess) return fail(ST_ENOMEM);
+  if (cudaMalloc(&s->Psmall, TC_SMALL_BYTES) != cudaSuccess) return fail(ST_ENOMEM);
   // He-style uniform initialisation from a splitmix64 stream (host)
   std::vector<float> P(NPARAM, 0.f);
   uint64_t z = seed * 0x9e3779b97f4a7c15ull + 12345;
@@ -1278,6 +1307,7 @@ void st_surrogate_destroy(st_surrogate* s) {
   cudaFree(s->P); cudaFree(s->G); cudaFree(s->Mm); cudaFree(s->Vv); cudaFree(s->loss);
   for (int l = 0; l < 3; ++l) cudaFree(s->Wb[l]);
   cudaFree(s->Wsw);
+  cudaFree(s->Psmall);
   cudaFree(s->fX); cudaFree(s->fAux); cudaFree(s->fFl); cudaFree(s->fO); cudaFree(s->fStatus);
   cudaFree(s->X);
   for (int l = 0; l < 4; ++l) { cudaFree(s->Z[l]); cudaFree(s->H[l]); }
@@ -1446,8 +1476,8 @@ int surrogate_frame(st_surrogate* s, const TraceParams& p, const Variant& v, con
     SC(cudaGetLastError());
     SC(cudaFuncSetAttribute(sur::sur_mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)sur::TC_SMEM));
-    sur::sur_mlp_tc_kernel<<<nb, sur::TC_THREADS, sur::TC_SMEM, stream>>>(s->P, s->Wsw, s->fX, s->fO, s->fStatus,
-                                                                          p.counters);
+    sur::sur_mlp_tc_kernel<<<nb, sur::TC_THREADS, sur::TC_SMEM, stream>>>(s->Psmall, s->Wsw, s->fX, s->fO,
+                                                                          s->fStatus, p.counters);
     SC(cudaGetLastError());
     sur::sur_gate_kernel<<<nb, 128, 0, stream>>>(p, f, s->fO, s->fAux, s->fFl, s->fStatus, s->fMask, s->fCount);
     SC(cudaGetLastError());
