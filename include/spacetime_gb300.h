@@ -28,6 +28,7 @@
  *                          CPU renderer's Starfield(...), src/starfield.jl:60-81
  *   st_render_motion       render_draft_mtl(...; camera_at, per_pixel_shutter),
  *                          src/metal.jl:2017-2030, 2130-2169, 829-857
+ *   st_save_raw / st_load_raw  save_raw / load_raw, src/rawio.jl:18-42 (host only)
  *
  * Output layout: linear HDR RGB float32 in the reference's column-major
  * (3, width, height) order, i.e. out[3*(i + width*j) + c] for 0-based pixel
@@ -269,6 +270,18 @@ int st_render_device(st_context* ctx, const st_camera* cam, const st_spacetime* 
 int st_render_motion(st_context* ctx, const st_camera* cam, const st_camera* poses, int nposes,
                      int per_pixel_shutter, const st_spacetime* st, const st_render_params* p,
                      float* out_rgb, st_ray_diag* diag, st_stats* stats);
+
+/* Raw HDR frame files, save_raw / load_raw (src/rawio.jl:18-42): a linear,
+ * unclamped 32-bit float RGB TIFF in display orientation (the reference's
+ * rotr90 of the frame: TIFF pixel (row r, column c) = frame pixel
+ * (width - 1 - c, r)) and a TOML sidecar <path>.toml holding metadata_toml
+ * (may be NULL) followed by the keys `format` and `saved_at`.  rgb is the
+ * frame in this ABI's output layout.  Host only (no GPU). */
+int st_save_raw(const char* path, const float* rgb, int width, int height, const char* metadata_toml);
+/* Frame size of a raw file (float32 RGB chunky TIFF, uncompressed). */
+int st_load_raw_size(const char* path, int* width, int* height);
+/* The frame back in the output layout; width and height must match. */
+int st_load_raw(const char* path, float* rgb, int width, int height);
 
 /* Render `nframes` camera poses (a camera track) in one persistent launch;
  * out_rgb holds nframes frames back to back. */

@@ -26,7 +26,8 @@ UNIT_FLAGS = {
     "st_trace_fp32_guarded.cu": (["--use_fast_math"] if FAST else []) + [f"-DST_MINB={MINB_FP32G}"],
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["st_trace_fp64.cu", "st_trace_fp32.cu", "st_trace_fp32_guarded.cu", "st_api.cu", "st_surrogate.cu", "st_noalloc.cu"]
+SOURCES = ["st_trace_fp64.cu", "st_trace_fp32.cu", "st_trace_fp32_guarded.cu", "st_api.cu", "st_surrogate.cu", "st_noalloc.cu",
+           "st_rawio.cpp"]
 
 
 def nvcc() -> str:
@@ -54,7 +55,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
 
     def one(src: str) -> str:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OBJ, src.replace(".cu", ".o"))
+        o = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
         stamp = o + ".flags"
         want = " ".join(flags + UNIT_FLAGS.get(src, []))
         same = os.path.exists(stamp) and open(stamp).read() == want
