@@ -134,6 +134,7 @@ def cpu_baseline(seconds_target: float = 15.0, threads: int | None = None, gpu_f
     from spacetime_gb300 import workloads
     FW, FH = frame_size
     w = {"config1": workloads.config1, "config1_thin": workloads.config1_thin,
+         "config1_nogas": workloads.config1_nogas,
          "config2": lambda: workloads.config2(nframes=240), "config4": workloads.config4}[workload]()
     w = w.scaled(FW, FH)
     threads = threads or os.cpu_count() or 1
@@ -338,9 +339,12 @@ def main(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--clocks-csv", default=None)
-    ap.add_argument("--workload", default="config1", choices=["config1", "config1_thin", "config2", "config4"],
+    ap.add_argument("--workload", default="config1",
+                    choices=["config1", "config1_thin", "config1_nogas", "config2", "config4"],
                     help="config1 is the headline; the others are the remaining benchmark configurations")
-    ap.add_argument("--surrogate", default=None, help="trained surrogate parameters (.npy) for config1_thin")
+    ap.add_argument("--surrogate", default=None,
+                    help="trained surrogate parameters (.npy; 'shipped' = spacetime_gb300/data/surrogate_kerr.npy) "
+                         "for config1_thin / config1_nogas")
     ap.add_argument("--sigma", type=float, default=4e-4, help="surrogate gate: max predicted std-dev (rad)")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
@@ -360,7 +364,8 @@ def main(argv=None):
     from spacetime_gb300 import _abi, workloads
     from spacetime_gb300.api import Context
 
-    w = workloads.config1() if args.workload == "config1" else workloads.config1_thin()
+    w = {"config1": workloads.config1, "config1_thin": workloads.config1_thin,
+         "config1_nogas": workloads.config1_nogas}[args.workload]()
     W, H = (int(x) for x in args.size.lower().split("x"))
     w = w.scaled(W, H)
     prec = {"fp64": _abi.ST_PREC_FP64, "fp32": _abi.ST_PREC_FP32, "fp32g": _abi.ST_PREC_FP32_GUARDED}[args.precision]
@@ -371,7 +376,8 @@ def main(argv=None):
     if args.surrogate:
         from spacetime_gb300.surrogate import Surrogate
         sur = Surrogate(local)
-        sur.set_params(np.load(args.surrogate))
+        from spacetime_gb300.surrogate import TRAINED
+        sur.set_params(np.load(TRAINED if args.surrogate == "shipped" else args.surrogate))
         ctx.set_surrogate(sur)
         extra = dict(surrogate=1, surrogate_sigma=args.sigma)
     p = ctx.params(w.semantics, width=w.width, height=w.height, precision=prec, schedule=sched,
@@ -477,8 +483,10 @@ def main(argv=None):
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if args.precision != "fp64" else "f64", "data": "synthetic",
         "config": {
-            "workload": f"config1: Kerr a=0.9 M=1, static camera r=15 M i=80 deg, Lens(24), {W}x{H}, "
-                        "gas 256x64x32 ISCO-25M h=0.05r, sky 2048x1024, kernel rules, samples=1",
+            "workload": (f"config1: Kerr a=0.9 M=1, static camera r=15 M i=80 deg, Lens(24), {W}x{H}, "
+                         "gas 256x64x32 ISCO-25M h=0.05r, sky 2048x1024, kernel rules, samples=1")
+                        if args.workload == "config1" else
+                        f"{w.name}: config1's camera and hole, {W}x{H}, sky 2048x1024, kernel rules, samples=1",
             "precision": {"fp64": "FP64", "fp32": "FP32 (MUFU sqrt/rcp/exp/log)",
                           "fp32g": "FP32 RHS, float-float state, FP64 guards"}[args.precision],
             "guards": {"r_guard": args.r_guard, "crit_band": args.crit_band, "renorm_every": args.renorm},

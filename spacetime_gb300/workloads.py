@@ -94,6 +94,16 @@ def config1_thin() -> Workload:
     return w
 
 
+def config1_nogas() -> Workload:
+    """config1's camera and hole with neither disc nor gas: every ray escapes or
+    falls in (the frame the learned surrogate serves)."""
+    w = config1()
+    w.name = "config1-kerr0.9-no-disc-no-gas"
+    w.vol = None
+    w.disc = None
+    return w
+
+
 def config2(nframes=240, width=1280, height=720) -> Workload:
     cams = free_fall_track(30.0, 1.5, nframes, M=1.0, incl_deg=85.0, fov=lens_fov(24.0))
     return Workload("config2-freefall-240x1280x720", Schwarzschild(1.0), cams[0], width, height,
