@@ -29,6 +29,10 @@
  *   st_render_motion       render_draft_mtl(...; camera_at, per_pixel_shutter),
  *                          src/metal.jl:2017-2030, 2130-2169, 829-857
  *   st_save_raw / st_load_raw  save_raw / load_raw, src/rawio.jl:18-42 (host only)
+ *   st_sky_fan             update_sky_fan!, src/metal.jl:2978-3036 (sky_fan_kernel!,
+ *                          fan_band_kernel!, src/metal.jl:2416-2517, 2888-2898)
+ *   st_render_layered      render_layered_gpu!, src/metal.jl:3040-3147 (layer pass of
+ *                          trace_kernel_mtl!, sky_composite_kernel!, :2707-2880)
  *
  * Output layout: linear HDR RGB float32 in the reference's column-major
  * (3, width, height) order, i.e. out[3*(i + width*j) + c] for 0-based pixel
@@ -282,6 +286,29 @@ int st_save_raw(const char* path, const float* rgb, int width, int height, const
 int st_load_raw_size(const char* path, int* width, int* height);
 /* The frame back in the output layout; width and height must match. */
 int st_load_raw(const char* path, float* rgb, int width, int height);
+
+/* ---- layered engine (Schwarzschild) ----------------------------------------
+ * By spherical symmetry the sky a static observer at radius r sees depends on
+ * one angle, psi, between the ray and the outward radial axis.  A fan of 4096
+ * geodesics over psi in [0, pi] (plus 1024 across the escape/capture
+ * transition, padded by 3 coarse spacings) replaces per-pixel sky
+ * integration; only the disc and gas are traced per pixel (at the layer
+ * resolution; rays the fan proves miss them are skipped) and composited over
+ * the fan-driven sky.  Schwarzschild, DRAFT rules, FP64 or FP32, an
+ * unboosted camera at rest with r >= 2.5 M (ST_EUNSUPPORTED otherwise). */
+#define ST_FAN_N 4096
+#define ST_FAN_FINE 1024
+/* The fans for this camera: fan[ST_FAN_N][4] and fine[ST_FAN_FINE][4] =
+ * (escaped 0/1, cos theta_f, sin theta_f, periapsis) with theta_f the exit
+ * direction's angle from the radial axis in the ray's plane; band[2] = the
+ * fine fan's psi range ((0, 0) when the coarse fan has no transition). */
+int st_sky_fan(st_context* ctx, const st_camera* cam, const st_spacetime* st, const st_render_params* p,
+               float* fan, float* fine, float* band);
+/* The layered frame into out_rgb[3*width*height]; layer_width / height <= 0
+ * mean the display size; diag (may be NULL) holds the fan-derived exit
+ * direction per pixel (last pass). */
+int st_render_layered(st_context* ctx, const st_camera* cam, const st_spacetime* st, const st_render_params* p,
+                      int layer_width, int layer_height, float* out_rgb, st_ray_diag* diag, st_stats* stats);
 
 /* Render `nframes` camera poses (a camera track) in one persistent launch;
  * out_rgb holds nframes frames back to back. */

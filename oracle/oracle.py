@@ -80,6 +80,8 @@ def lib() -> C.CDLL:
         dp = P(C.c_double)
         L.orc_render.argtypes = [P(OrcScene), FP, C.c_void_p, C.c_int]
         L.orc_render.restype = C.c_int
+        L.orc_trace_dirs.argtypes = [P(OrcScene), C.c_int, P(C.c_double), C.c_void_p, C.c_int]
+        L.orc_trace_dirs.restype = C.c_int
         L.orc_rhs.argtypes = [C.c_int, dp, C.c_double, C.c_double, C.c_double, dp]
         L.orc_camera_tetrad.argtypes = [dp, dp, dp, dp, C.c_double, C.c_double, dp, dp, dp, dp, dp]
         L.orc_camera_beta.argtypes = [dp, dp, dp, dp, dp]
@@ -316,6 +318,17 @@ class Scene:
         s.star_lut_size = n
         s.star_seed = int(sf.get("seed", 12345))
         s.star_lut_tmin, s.star_lut_tmax = 500.0, 30000.0
+
+    def trace_dirs(self, dirs, nthreads: int = 0):
+        """Per-ray records of rays launched from this scene's camera along
+        camera-frame directions dirs[n][3] = (cf, cr, cu) (orc_trace_dirs)."""
+        d = np.ascontiguousarray(dirs, dtype=np.float64)
+        rays = np.zeros(d.shape[0], dtype=RAY_DTYPE)
+        rc = lib().orc_trace_dirs(C.byref(self.s), d.shape[0], d.ctypes.data_as(C.POINTER(C.c_double)),
+                                  C.c_void_p(rays.ctypes.data), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"orc_trace_dirs failed ({rc})")
+        return rays
 
     def render(self, nthreads: int = 0, records: bool = True):
         s = self.s

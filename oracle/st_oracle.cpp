@@ -312,6 +312,7 @@ struct Scene {
   int ksteps;  // 0, or 45 / 46: the kernel's adaptive twin
   double ds_gas, vol_rb2;
   int nmax;
+  const double* dirs = nullptr;  // orc_trace_dirs: (cf, cr, cu) per ray instead of pixels
 };
 
 // LUT colour. RENDER rounds half to even (Julia `round`, src/blackbody.jl:78);
@@ -758,6 +759,10 @@ void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
     }
     cr = dxl / nu; cu = dyl / nu; cf = 1.0 / nu;
   }
+  if (S.dirs) {  // a given camera-frame direction (orc_trace_dirs), no lens offset
+    cf = S.dirs[3 * (size_t)i0]; cr = S.dirs[3 * (size_t)i0 + 1]; cu = S.dirs[3 * (size_t)i0 + 2];
+    offr = offu = 0.0;
+  }
   // Per-pixel shutter: the pose moves toward the stratum's end pose by a
   // hashed fraction of the way (src/metal.jl:843-857).
   Tetrad T = S.T;
@@ -1020,10 +1025,7 @@ void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
 
 extern "C" {
 
-int orc_render(const orc_scene* s, float* out_rgb, orc_ray* rays, int nthreads) {
-  if (!s || s->width <= 0 || s->height <= 0 || s->cols <= 0 || s->rows <= 0) return 1;
-  if (std::fabs(s->a) > s->M) return 1;
-  Scene S;
+static void setup_scene(const orc_scene* s, Scene& S) {
   S.s = s;
   S.P.M = s->M; S.P.a = s->a; S.P.kerr = (s->a != 0.0);
   double beta[3];
@@ -1048,6 +1050,13 @@ int orc_render(const orc_scene* s, float* out_rgb, orc_ray* rays, int nthreads) 
     S.vol_rb2 = -1.0;
   }
   S.nmax = s->nmax;
+}
+
+int orc_render(const orc_scene* s, float* out_rgb, orc_ray* rays, int nthreads) {
+  if (!s || s->width <= 0 || s->height <= 0 || s->cols <= 0 || s->rows <= 0) return 1;
+  if (std::fabs(s->a) > s->M) return 1;
+  Scene S;
+  setup_scene(s, S);
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
@@ -1062,6 +1071,23 @@ int orc_render(const orc_scene* s, float* out_rgb, orc_ray* rays, int nthreads) 
         for (int c = 0; c < 3; ++c) out_rgb[3 * o + c] = (float)ro.rgb[c];
       if (rays) rays[o] = ro.rec;
     }
+  }
+  return 0;
+}
+
+int orc_trace_dirs(const orc_scene* s, int n, const double* dirs, orc_ray* rays, int nthreads) {
+  if (!s || n <= 0 || !dirs || !rays || std::fabs(s->a) > s->M) return 1;
+  Scene S;
+  setup_scene(s, S);
+  S.dirs = dirs;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int k = 0; k < n; ++k) {
+    RayOut ro;
+    trace_ray(S, k, 0, &ro);
+    rays[k] = ro.rec;
   }
   return 0;
 }

@@ -129,6 +129,12 @@ typedef struct {
  * i.e. [rows][cols][3]) and optionally the per-ray records ([rows][cols]). */
 int orc_render(const orc_scene* sc, float* out_rgb, orc_ray* rays, int nthreads);
 
+/* Trace n rays from the scene's camera along camera-frame directions
+ * dirs[n][3] = (cf, cr, cu) (forward, right, up coefficients of the tetrad,
+ * as a pixel's projection produces them), no lens, jitter or shutter: the
+ * twin of the layered engine's deflection fan.  Pixel fields are unused. */
+int orc_trace_dirs(const orc_scene* sc, int n, const double* dirs, orc_ray* rays, int nthreads);
+
 /* --- unit pieces, for known-answer tests --- */
 void orc_rhs(int kerr, const double s[6], double pt, double M, double a, double d[6]);
 void orc_camera_tetrad(const double pos[3], const double fwd[3], const double right[3],

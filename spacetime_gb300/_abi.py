@@ -122,8 +122,9 @@ EXPORTS = [
     "st_surrogate_set_params", "st_surrogate_forward", "st_surrogate_loss_grad", "st_surrogate_generate",
     "st_surrogate_train", "st_render_frames_noalloc", "st_context_set_surrogate",
     "st_starfield_default", "st_context_set_starfield", "st_render_motion",
-    "st_save_raw", "st_load_raw_size", "st_load_raw",
+    "st_save_raw", "st_load_raw_size", "st_load_raw", "st_sky_fan", "st_render_layered",
 ]
+ST_FAN_N, ST_FAN_FINE = 4096, 1024
 
 _lib = None
 
@@ -195,6 +196,12 @@ def load(path: str | None = None) -> C.CDLL:
     lib.st_load_raw_size.restype = C.c_int
     lib.st_load_raw.argtypes = [C.c_char_p, P(C.c_float), C.c_int, C.c_int]
     lib.st_load_raw.restype = C.c_int
+    lib.st_sky_fan.argtypes = [C.c_void_p, P(StCamera), P(StSpacetime), P(StRenderParams), P(C.c_float),
+                               P(C.c_float), P(C.c_float)]
+    lib.st_sky_fan.restype = C.c_int
+    lib.st_render_layered.argtypes = [C.c_void_p, P(StCamera), P(StSpacetime), P(StRenderParams), C.c_int, C.c_int,
+                                      P(C.c_float), C.c_void_p, P(StStats)]
+    lib.st_render_layered.restype = C.c_int
     for name in ("st_context_create", "st_context_set_disc", "st_context_set_volume", "st_render",
                  "st_render_diag", "st_render_device", "st_render_frames", "st_camera_tetrad",
                  "st_surrogate_create", "st_surrogate_num_params", "st_surrogate_get_params",

@@ -276,6 +276,34 @@ class Context:
         _abi.check(rc, "st_render_motion")
         return RenderResult(img, stats.as_dict(), d.reshape(p.height, p.width) if diag else None)
 
+    def sky_fan(self, cam: Camera, bh, p: _abi.StRenderParams):
+        """(fan (4096, 4), fine (1024, 4), band (2,)) for this camera
+        (update_sky_fan!): columns escaped, cos, sin of the exit angle from the
+        radial axis, periapsis."""
+        fan = np.empty((_abi.ST_FAN_N, 4), np.float32)
+        fine = np.empty((_abi.ST_FAN_FINE, 4), np.float32)
+        band = np.empty(2, np.float32)
+        fp = C.POINTER(C.c_float)
+        _abi.check(self._lib.st_sky_fan(self._h, C.byref(_st_camera(cam)), C.byref(_st_spacetime(bh)), C.byref(p),
+                                        fan.ctypes.data_as(fp), fine.ctypes.data_as(fp), band.ctypes.data_as(fp)),
+                   "st_sky_fan")
+        return fan, fine, band
+
+    def render_layered_raw(self, cam: Camera, bh, p: _abi.StRenderParams, layer_size=None,
+                           diag: bool = False) -> RenderResult:
+        """The layered engine's frame (render_layered_gpu!): fan-driven sky,
+        disc / gas layer at layer_size = (width, height) (default: the display)."""
+        lw, lh = layer_size if layer_size is not None else (0, 0)
+        img = np.empty((p.height, p.width, 3), dtype=np.float32)
+        d = np.empty(p.height * p.width, dtype=_abi.DIAG_DTYPE) if diag else None
+        stats = _abi.StStats()
+        _abi.check(self._lib.st_render_layered(self._h, C.byref(_st_camera(cam)), C.byref(_st_spacetime(bh)),
+                                               C.byref(p), int(lw), int(lh),
+                                               img.ctypes.data_as(C.POINTER(C.c_float)),
+                                               C.c_void_p(d.ctypes.data) if diag else None, C.byref(stats)),
+                   "st_render_layered")
+        return RenderResult(img, stats.as_dict(), d.reshape(p.height, p.width) if diag else None)
+
     def render_frames_raw(self, cams, bh, p: _abi.StRenderParams) -> RenderResult:
         n = len(cams)
         arr = (_abi.StCamera * n)(*[_st_camera(c) for c in cams])

@@ -27,7 +27,7 @@ UNIT_FLAGS = {
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["st_trace_fp64.cu", "st_trace_fp32.cu", "st_trace_fp32_guarded.cu", "st_api.cu", "st_surrogate.cu", "st_noalloc.cu",
-           "st_rawio.cpp"]
+           "st_layered.cu", "st_rawio.cpp"]
 
 
 def nvcc() -> str:

@@ -314,6 +314,12 @@ struct st_context {
   float4* d_star_lut = nullptr;
   int star_lut_size = 0;
   double star_lut_tmin = 500.0, star_lut_tmax = 30000.0;
+  // layered engine: deflection fans, their critical band, the disc / gas layer
+  float4* d_fan = nullptr;
+  float4* d_fine = nullptr;
+  float* d_band = nullptr;
+  float4* d_layer = nullptr;
+  size_t layer_cap = 0;
   st_surrogate* sur = nullptr;  // attached surrogate (not owned)
   int* d_list = nullptr;        // surrogate fallback pixels
   size_t list_cap = 0;
@@ -682,6 +688,74 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
   return status;
 }
 
+constexpr int FAN_N = 4096, FAN_FINE = 1024, FAN_PAD = 3;
+
+// Deflection fans for the camera's radius (update_sky_fan!, src/metal.jl:2978-3036):
+// the coarse fan over psi in [0, pi], its escape/capture band, the fine fan
+// across the band; and the static frame's radial axis at the camera (er).
+int build_fans(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
+               const TraceParams& p, double er[4], cudaStream_t s) {
+  const double r = std::sqrt(st::dot3(cam->pos, cam->pos));
+  // the fan camera: at (r, 0, 0), forward +x, right +y, up +z, at rest
+  st_camera fc{};
+  fc.pos[0] = r;
+  fc.fwd[0] = 1.0; fc.right[1] = 1.0; fc.up[2] = 1.0;
+  fc.fov_factor = 1.0;
+  fc.projection = ST_PROJ_PINHOLE;
+  fc.focus_dist = 1.0;
+  st::lay::FanParams fp{};
+  st::Variant w;
+  int rc = fill_params(ctx, &fc, stp, rp, &fp.p, &w);
+  if (rc != ST_OK) return rc;
+  fp.p.disc_on = 0;
+  fp.p.vol_on = 0;
+  fp.p.vol_rb2 = -1.0;
+  fp.p.layer = 0;
+  fp.p.star_strength = 0.0;
+  fp.p.shutter_seed = 0;
+  fp.p.r_escape = p.r_escape;
+  fp.p.nmax = p.nmax;
+  st::fill_float_copies(&fp.p);
+  if (!ctx->d_fan && cudaMalloc(&ctx->d_fan, FAN_N * sizeof(float4)) != cudaSuccess) return ST_ENOMEM;
+  if (!ctx->d_fine && cudaMalloc(&ctx->d_fine, FAN_FINE * sizeof(float4)) != cudaSuccess) return ST_ENOMEM;
+  if (!ctx->d_band && cudaMalloc(&ctx->d_band, 2 * sizeof(float)) != cudaSuccess) return ST_ENOMEM;
+  ST_CUDA(cudaMemsetAsync(ctx->d_band, 0, 2 * sizeof(float), s));
+  fp.out = ctx->d_fan;
+  fp.n = FAN_N;
+  fp.band = 0;
+  fp.band_lohi = ctx->d_band;
+  ST_CUDA(st::launch_skyfan(rp->precision, fp, s));
+  ST_CUDA(st::launch_fanband(ctx->d_fan, FAN_N, FAN_PAD, ctx->d_band, s));
+  fp.out = ctx->d_fine;
+  fp.n = FAN_FINE;
+  fp.band = 1;
+  ST_CUDA(st::launch_skyfan(rp->precision, fp, s));
+  // the radial axis of the static frame at the camera: the forward vector of
+  // a camera at rest looking straight out (any completion of the basis)
+  double xh[3];
+  for (int k = 0; k < 3; ++k) xh[k] = cam->pos[k] / r;
+  const double ax[3] = {std::fabs(xh[2]) < 0.9 ? 0.0 : 1.0, 0.0, std::fabs(xh[2]) < 0.9 ? 1.0 : 0.0};
+  double b1[3] = {ax[1] * xh[2] - ax[2] * xh[1], ax[2] * xh[0] - ax[0] * xh[2], ax[0] * xh[1] - ax[1] * xh[0]};
+  const double nb = std::sqrt(st::dot3(b1, b1));
+  for (int k = 0; k < 3; ++k) b1[k] /= nb;
+  const double b2[3] = {xh[1] * b1[2] - xh[2] * b1[1], xh[2] * b1[0] - xh[0] * b1[2], xh[0] * b1[1] - xh[1] * b1[0]};
+  const double beta[3] = {0.0, 0.0, 0.0};
+  double U[4], Er[4], Eu[4];
+  st::host_tetrad(cam->pos, xh, b1, b2, stp->M, 0.0, beta, U, er, Er, Eu);
+  return ST_OK;
+}
+
+int layered_check(const st_camera* cam, const st_spacetime* stp, const st_render_params* rp) {
+  if (!cam || !stp || !rp) return ST_EINVAL;
+  if (stp->a != 0.0 || rp->semantics != ST_SEM_DRAFT || rp->surrogate ||
+      (rp->precision != ST_PREC_FP64 && rp->precision != ST_PREC_FP32))
+    return ST_EUNSUPPORTED;
+  // the fan is indexed in the static frame: an unboosted camera at rest, r >= 2.5 M
+  if (st::dot3(cam->velocity, cam->velocity) != 0.0 || std::sqrt(st::dot3(cam->pos, cam->pos)) < 2.5 * stp->M)
+    return ST_EUNSUPPORTED;
+  return ST_OK;
+}
+
 }  // namespace
 
 // Blackbody(wb_temperature, table_min, table_max, table_size), src/blackbody.jl:51-60,
@@ -899,6 +973,10 @@ void st_context_destroy(st_context* ctx) {
   cudaFree(ctx->d_sky);
   cudaFree(ctx->d_lut);
   cudaFree(ctx->d_star_lut);
+  cudaFree(ctx->d_fan);
+  cudaFree(ctx->d_fine);
+  cudaFree(ctx->d_band);
+  cudaFree(ctx->d_layer);
   cudaFree(ctx->d_vol);
   cudaFree(ctx->d_fb);
   cudaFree(ctx->d_rgb);
@@ -938,6 +1016,113 @@ int st_render_motion(st_context* ctx, const st_camera* cam, const st_camera* pos
   if (p->surrogate) return ST_EUNSUPPORTED;
   const Motion mo{poses, nposes, per_pixel_shutter ? 1 : 0};
   return do_render(ctx, cam, st, p, out_rgb, diag, nullptr, stats, &mo);
+}
+
+int st_sky_fan(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
+               float* fan, float* fine, float* band) {
+  if (!ctx || !fan || !fine || !band) return ST_EINVAL;
+  int rc = layered_check(cam, stp, rp);
+  if (rc != ST_OK) return rc;
+  TraceParams p;
+  st::Variant v;
+  if ((rc = fill_params(ctx, cam, stp, rp, &p, &v)) != ST_OK) return rc;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
+  cudaStream_t s = ctx->stream;
+  double er[4];
+  if ((rc = build_fans(ctx, cam, stp, rp, p, er, s)) != ST_OK) return rc;
+  ST_CUDA(cudaMemcpyAsync(fan, ctx->d_fan, FAN_N * sizeof(float4), cudaMemcpyDeviceToHost, s));
+  ST_CUDA(cudaMemcpyAsync(fine, ctx->d_fine, FAN_FINE * sizeof(float4), cudaMemcpyDeviceToHost, s));
+  ST_CUDA(cudaMemcpyAsync(band, ctx->d_band, 2 * sizeof(float), cudaMemcpyDeviceToHost, s));
+  ST_CUDA(cudaStreamSynchronize(s));
+  return ST_OK;
+}
+
+int st_render_layered(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
+                      int layer_width, int layer_height, float* out_rgb, st_ray_diag* host_diag, st_stats* stats) {
+  if (!ctx || !out_rgb) return ST_EINVAL;
+  int rc = layered_check(cam, stp, rp);
+  if (rc != ST_OK) return rc;
+  const auto t0 = std::chrono::steady_clock::now();
+  TraceParams p;
+  st::Variant v;
+  if ((rc = fill_params(ctx, cam, stp, rp, &p, &v)) != ST_OK) return rc;
+  const int lw = layer_width > 0 ? layer_width : rp->width, lh = layer_height > 0 ? layer_height : rp->height;
+  if (lw < 2 || lh < 2 || (long long)lw * lh > (1ll << 30)) return ST_EINVAL;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
+  cudaStream_t s = ctx->stream;
+  const size_t npix = (size_t)rp->width * rp->height;
+  if ((rc = ensure(&ctx->d_fb, &ctx->fb_cap, npix)) != ST_OK) return rc;
+  if ((rc = ensure(&ctx->d_rgb, &ctx->rgb_cap, 3 * npix)) != ST_OK) return rc;
+  if (host_diag && (rc = ensure(&ctx->d_diag, &ctx->diag_cap, npix)) != ST_OK) return rc;
+  const bool matter = ctx->disc_on || ctx->vol_on;
+  if (matter && (rc = ensure(&ctx->d_layer, &ctx->layer_cap, (size_t)lw * lh)) != ST_OK) return rc;
+  ST_CUDA(cudaMemsetAsync(ctx->d_counters, 0, st::CNT_N * sizeof(unsigned long long), s));
+  ST_CUDA(cudaEventRecord(ctx->ev0, s));
+  double er[4];
+  if ((rc = build_fans(ctx, cam, stp, rp, p, er, s)) != ST_OK) return rc;
+  for (int k = 0; k < 4; ++k) p.er[k] = er[k];
+  // the gate: no ray whose periapsis stays beyond it meets the disc or the gas
+  double gate = 0.0;
+  if (ctx->disc_on) gate = std::max(gate, ctx->disc.outer);
+  if (ctx->vol_on && p.vol_rb2 > 0.0) gate = std::max(gate, std::sqrt(p.vol_rb2));
+  const std::vector<PassPlan> passes = plan_passes(rp, cam);
+  int launches = 0;
+  for (size_t k = 0; k < passes.size(); ++k) {
+    const PassPlan& pp = passes[k];
+    p.ju = pp.ju; p.jv = pp.jv; p.jw = pp.jw; p.jseed = pp.jseed;
+    p.lens_u0 = pp.lens_u0; p.lens_v0 = pp.lens_v0; p.lens_w = pp.lens_w; p.lens_seed = pp.lens_seed;
+    st::lay::CompParams cp{ctx->d_fan, FAN_N, ctx->d_fine, FAN_FINE, ctx->d_band, nullptr, lw, lh};
+    if (matter) {
+      // the disc / gas layer of this pass at the layer resolution
+      TraceParams lp = p;
+      lp.width = lw;
+      lp.height = lh;
+      lp.layer = 1;
+      lp.layer_gate = gate;
+      lp.fan = ctx->d_fan;
+      lp.fan_n = FAN_N;
+      lp.out = ctx->d_layer;
+      lp.diag = nullptr;
+      lp.first_pass = 1;
+      lp.weight = 1.0f;
+      st::fill_float_copies(&lp);
+      st::Variant lv = v;
+      lv.sched = ST_SCHED_PIXEL;
+      ST_CUDA(st::launch_trace(lv, lp, rp->block_x, rp->block_y, ctx->num_sms, s));
+      ++launches;
+      cp.layer = ctx->d_layer;
+    }
+    p.out = ctx->d_fb;
+    p.diag = host_diag ? ctx->d_diag : nullptr;
+    p.first_pass = (k == 0) ? 1 : 0;
+    p.weight = (float)(1.0 / passes.size());
+    ST_CUDA(st::launch_composite(rp->precision, p, cp, s));
+    ++launches;
+  }
+  ST_CUDA(cudaEventRecord(ctx->ev1, s));
+  unsigned long long cnt[st::CNT_N];
+  ST_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
+  ST_CUDA(st::launch_pack_rgb(ctx->d_fb, ctx->d_rgb, (int)npix, s));
+  ST_CUDA(cudaMemcpyAsync(out_rgb, ctx->d_rgb, 3 * npix * sizeof(float), cudaMemcpyDeviceToHost, s));
+  if (host_diag)
+    ST_CUDA(cudaMemcpyAsync(host_diag, ctx->d_diag, npix * sizeof(st_ray_diag), cudaMemcpyDeviceToHost, s));
+  ST_CUDA(cudaStreamSynchronize(s));
+  const int status = cnt[st::CNT_STATUS] ? (int)cnt[st::CNT_STATUS] : ST_OK;
+  if (stats) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) != cudaSuccess) { (void)cudaGetLastError(); ms = 0.f; }
+    std::memset(stats, 0, sizeof(*stats));
+    stats->kernel_ms = ms;
+    stats->rays = npix * passes.size();
+    stats->steps = cnt[st::CNT_STEPS];
+    stats->gas_samples = cnt[st::CNT_GAS];
+    stats->launches = launches + 3;
+    stats->status = status;
+    stats->h2d_bytes = sizeof(TraceParams) * (launches + 3);
+    stats->d2h_bytes = 3 * npix * sizeof(float) + sizeof cnt;
+    stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return status;
 }
 
 int st_render_device(st_context* ctx, const st_camera* cam, const st_spacetime* st, const st_render_params* p,

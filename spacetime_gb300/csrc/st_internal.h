@@ -74,6 +74,15 @@ struct TraceParams {
   const float4* star_lut;    // [star_lut_size] RGB_, the stars' own white point
   int star_lut_size, star_seed;
   double star_lut_tmin, star_lut_tmax;
+  // layered engine's disc / gas layer (src/metal.jl:1096-1135, 1204-1212,
+  // 1616-1626; Schwarzschild, DRAFT): layer = 1 traces only emission and
+  // transmittance, culling rays the deflection fan proves stay outside
+  // layer_gate; er = the static frame's radial axis at the camera
+  int layer;
+  double layer_gate;
+  double er[4];
+  const float4* fan;         // [fan_n] (escaped, cos, sin, periapsis)
+  int fan_n;
   // per-pixel shutter (src/metal.jl:829-857): seed 0 = off; the camera pose
   // at the far end of this pass's shutter stratum
   int shutter_seed;
@@ -96,7 +105,7 @@ struct TraceParams {
   // float variant never converts from double inside its loop (on GB300 every
   // double -> float conversion issues on the FP64 pipe)
   struct Flt {
-    float M, a, rkill2, vol_rb2, hcap, dt, hcoef, tspan, ds_gas, zmax, r_isco, E_isco, L_isco, opac, emis, disc_inner, disc_outer, disc_falloff, lut_tmin, lut_tmax, ls_in, ls_out, crit_r2, r_guard2, tol;
+    float M, a, rkill2, vol_rb2, hcap, dt, hcoef, tspan, ds_gas, zmax, r_isco, E_isco, L_isco, opac, emis, disc_inner, disc_outer, disc_falloff, lut_tmin, lut_tmax, ls_in, ls_out, crit_r2, r_guard2, tol, layer_gate;
   } f;
 };
 
@@ -127,6 +136,7 @@ inline void fill_float_copies(TraceParams* p) {
   p->f.crit_r2 = (float)p->crit_r2;
   p->f.r_guard2 = (float)p->r_guard2;
   p->f.tol = (float)p->tol;
+  p->f.layer_gate = (float)p->layer_gate;
 }
 
 // Variant key of the compiled kernels (the reference's Val{...} switches,
@@ -155,6 +165,33 @@ struct SurFrame {
 // the rest into list / *count (device).  Returns an ST_* status.
 int surrogate_frame(struct ::st_surrogate* s, const TraceParams& p, const Variant& v, const SurFrame& f,
                     int* list, int* count, cudaStream_t stream);
+
+// Layered engine (st_layered.cu).
+namespace lay {
+// One deflection fan: a TraceParams with the fan camera's tetrad (at (r,0,0)
+// looking along +x, right +y) and no disc, gas or layer, so each entry is
+// what the trace kernel computes for that ray.
+struct FanParams {
+  TraceParams p;
+  float4* out;       // [n] (escaped, cos theta_f, sin theta_f, periapsis)
+  int n;
+  int band;          // 0: psi = pi k / (n - 1); 1: across band_lohi
+  const float* band_lohi;
+};
+// The composite's fan and layer.
+struct CompParams {
+  const float4* fan;
+  int n;
+  const float4* fine;
+  int nf;
+  const float* band;
+  const float4* layer;  // [lh][lw] premultiplied RGB + transmittance, or null (transparent)
+  int lw, lh;
+};
+}  // namespace lay
+cudaError_t launch_skyfan(int prec, const lay::FanParams& fp, cudaStream_t stream);
+cudaError_t launch_fanband(const float4* fan, int n, int pad, float* band, cudaStream_t stream);
+cudaError_t launch_composite(int prec, const TraceParams& p, const lay::CompParams& cp, cudaStream_t stream);
 
 // Launch one trace pass; returns a cudaError_t.
 cudaError_t launch_trace(const Variant& v, const TraceParams& p, int block_x, int block_y,

@@ -323,7 +323,11 @@ struct RayState {
   R h_carry, err_prev;
   R k1c[6];
   bool k1_valid;
+  R r_layer_prev;  // layer pass: previous radius beyond the gate
 };
+
+// Internal ray flag of the layer pass: the fan proves the ray misses the gate.
+constexpr int ST_RAY_LAYER_CULLED = 1 << 20;
 
 // Camera tetrad for the current ray; per-frame data lives in TraceParams for
 // single frames and in FrameCam for batched tracks (st_render_frames).
@@ -417,6 +421,15 @@ __device__ void bardeen(const D* y, D pt, D M, D a, bool* captured0, bool* graze
   *captured0 = cap;
 }
 
+template <int PREC, int KERR, int SEM>
+__device__ void init_ray_dir(const TraceParams& p, const CamView& cam, int i1, int j1,
+                             typename std::conditional<PREC == ST_PREC_FP32, float, double>::type cf,
+                             typename std::conditional<PREC == ST_PREC_FP32, float, double>::type cr,
+                             typename std::conditional<PREC == ST_PREC_FP32, float, double>::type cu,
+                             typename std::conditional<PREC == ST_PREC_FP32, float, double>::type offr,
+                             typename std::conditional<PREC == ST_PREC_FP32, float, double>::type offu,
+                             RayState<typename RealOf<PREC>::T>& st);
+
 // Build the ray of pixel (i0, j0) (0-based, frame-local).  Ray generation and
 // index lowering run in D (double for FP64 and FP32_GUARDED, float for FP32).
 template <int PREC, int KERR, int SEM>
@@ -463,6 +476,22 @@ __device__ void init_ray(const TraceParams& p, const CamView& cam, int i0, int j
     }
     cr = dxl / nu; cu = dyl / nu; cf = D(1) / nu;
   }
+  init_ray_dir<PREC, KERR, SEM>(p, cam, i1, j1, cf, cr, cu, offr, offu, st);
+}
+
+// The ray along camera-frame direction (cf, cr, cu) from the lens point
+// (offr, offu) of pixel (i1, j1) (1-based, for the shutter hash): pose,
+// photon lowering, launch tests and the initial state.
+template <int PREC, int KERR, int SEM>
+__device__ void init_ray_dir(const TraceParams& p, const CamView& cam, int i1, int j1,
+                             typename std::conditional<PREC == ST_PREC_FP32, float, double>::type cf,
+                             typename std::conditional<PREC == ST_PREC_FP32, float, double>::type cr,
+                             typename std::conditional<PREC == ST_PREC_FP32, float, double>::type cu,
+                             typename std::conditional<PREC == ST_PREC_FP32, float, double>::type offr,
+                             typename std::conditional<PREC == ST_PREC_FP32, float, double>::type offu,
+                             RayState<typename RealOf<PREC>::T>& st) {
+  using R = typename RealOf<PREC>::T;
+  using D = typename std::conditional<PREC == ST_PREC_FP32, float, double>::type;
   // the pose; with the per-pixel shutter on, moved toward the stratum's end
   // pose by a hashed fraction (src/metal.jl:843-857)
   D cpos[3], cEf[4], cEr[4], cEu[4], cU[4];
@@ -535,6 +564,23 @@ __device__ void init_ray(const TraceParams& p, const CamView& cam, int i0, int j
   st.steps = st.fp64_steps = st.gas = 0;
   st.r_cross = -1.f;
   st.g_cross = 0.f;
+  st.r_layer_prev = R(-1);
+  if constexpr (!KERR && SEM == ST_SEM_DRAFT) {
+    // Layer pass: a ray launched beyond the gate whose fan entry (by its
+    // local angle to the radial axis) escapes with periapsis beyond the gate
+    // never meets the disc or gas (src/metal.jl:1103-1133).
+    if (p.layer && r0 > D(p.layer_gate) && p.fan_n > 1) {
+      const D cpsi = clamp_(pt * D(p.er[0]) + s[3] * D(p.er[1]) + s[4] * D(p.er[2]) + s[5] * D(p.er[3]), D(-1), D(1));
+      const D N1 = D(p.fan_n - 1);
+      const D tf = acos_(cpsi) * N1 / D(3.141592653589793);
+      const int k0 = min(max((int)tf, 0), p.fan_n - 2);
+      const D fr = tf - D(k0);
+      const float4 fa = p.fan[k0], fb = p.fan[k0 + 1];
+      const D esc = D(fa.x) + fr * (D(fb.x) - D(fa.x));
+      const D rmin = D(fa.w) + fr * (D(fb.w) - D(fa.w));
+      if (esc > D(0.999) && rmin > D(p.layer_gate)) st.flags |= ST_RAY_LAYER_CULLED;
+    }
+  }
 }
 
 // Land a step on the sphere |x| = target: the RK4 step of size hc from yp
@@ -843,6 +889,19 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
   const R r2 = y[0] * y[0] + y[1] * y[1] + y[2] * y[2];
   const R r = sqrt_(r2);
   R rk2 = r2;
+  if constexpr (!KERR && SEM == ST_SEM_DRAFT) {
+    if (p.layer) {
+      // culled by the fan, or outbound beyond the gate: a null geodesic has
+      // at most one radial turning point, so it cannot come back, and the
+      // sky is the composite's job (src/metal.jl:1204-1212)
+      if (st.flags & ST_RAY_LAYER_CULLED) return true;
+      if (r > PR(layer_gate) && st.r_layer_prev > R(0) && r > st.r_layer_prev) {
+        st.flags |= ST_RAY_ESCAPED;
+        return true;
+      }
+      st.r_layer_prev = r;
+    }
+  }
   if (st.steps >= st.nmax) { st.flags |= ST_RAY_BUDGET; return true; }
   if constexpr (SEM == ST_SEM_DRAFT) {
     if constexpr (KERR) {
@@ -1071,6 +1130,14 @@ template <int PREC, int KERR, int SEM>
 __device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typename RealOf<PREC>::T>& st, int out_index,
                                            int diag_index) {
   using R = typename RealOf<PREC>::T;
+  if constexpr (!KERR && SEM == ST_SEM_DRAFT) {
+    if (p.layer) {
+      // layer output: premultiplied emission and transmittance, by
+      // assignment; capture blackness is the composite's (src/metal.jl:1616-1626)
+      p.out[out_index] = make_float4((float)st.acc[0], (float)st.acc[1], (float)st.acc[2], (float)st.alpha);
+      return;
+    }
+  }
   const R M = PR(M), a = PR(a);
   R yv[6];
 #pragma unroll

@@ -1,0 +1,126 @@
+"""The layered engine on the GPU (update_sky_fan!, render_layered_gpu!,
+src/metal.jl:2394-3147), Schwarzschild, kernel rules.
+
+- Fan: every entry (coarse over psi in [0, pi], fine across the band) against
+  the oracle's FP64 twin of the same ray (orc_trace_dirs): escape flag
+  identical, exit angle within 1e-6 rad (the fan stores float32).
+- Sky: the fan-driven frame against the full per-pixel trace of the same
+  frame: exit directions (interpolated in psi) median <= 1e-6 rad, p99 <= 1e-4.
+- With a disc: the layer pass plus composite against the full trace:
+  radiance median <= 1e-4, and at half layer resolution the frame stays close
+  while tracing fewer steps.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from spacetime_gb300 import _abi, workloads
+from spacetime_gb300.api import Context
+from spacetime_gb300.scene import Camera
+
+from .helpers import angle, gpu_render
+
+pytestmark = pytest.mark.gpu
+
+FP64, FP32 = _abi.ST_PREC_FP64, _abi.ST_PREC_FP32
+
+
+def _scene(disc=False, w=192, h=108):
+    wl = workloads.config0().scaled(w, h)
+    wl.semantics = _abi.ST_SEM_DRAFT
+    wl.emitter = _abi.ST_EMIT_KS_EXACT
+    wl.params = dict(samples=1, pixel_jitter=0, exit_landing=1)
+    if not disc:
+        wl.disc = None
+    return wl
+
+
+def _params(ctx, wl, prec=FP64, **kw):
+    return ctx.params(wl.semantics, width=wl.width, height=wl.height, precision=prec, **wl.params, **kw)
+
+
+def test_fan_fp64_vs_oracle_twin(built_lib):
+    wl = _scene()
+    sky = workloads.sky(512, 256)
+    with Context(sky, disc=None, emitter=wl.emitter) as ctx:
+        fan, fine, band = ctx.sky_fan(wl.cam, wl.bh, _params(ctx, wl))
+    r = float(np.linalg.norm(wl.cam.pos))
+    fcam = Camera(np.array([r, 0.0, 0.0]), np.array([1.0, 0, 0]), np.array([0, 1.0, 0]), np.array([0, 0, 1.0]),
+                  1.0, np.zeros(3))
+    one = workloads.Workload("fan", wl.bh, fcam, 4, 4, _abi.ST_SEM_DRAFT, None, wl.emitter,
+                             params=dict(samples=1, pixel_jitter=0, exit_landing=1))
+    sc = O.scene_for(one, workloads.sky(64, 32), O.INT_RK4)
+    n, nf = fan.shape[0], fine.shape[0]
+    psi = math.pi * np.arange(n) / (n - 1)
+    lo, hi = float(band[0]), float(band[1])
+    assert 0.0 < lo < hi < math.pi
+    psif = lo + (hi - lo) * np.arange(nf) / (nf - 1)
+    for ang, tab in ((psi, fan), (psif, fine)):
+        rays = sc.trace_dirs(np.stack([np.cos(ang), np.sin(ang), np.zeros_like(ang)], 1))
+        esc = (rays["flags"] & O.RAY_BLACK) == 0
+        assert np.array_equal(esc, tab[:, 0] > 0.5)
+        d = rays["dir"][esc][:, :2]
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        g = tab[esc][:, 1:3].astype(np.float64)
+        g /= np.linalg.norm(g, axis=1, keepdims=True)
+        err = np.abs(np.arctan2(d[:, 0] * g[:, 1] - d[:, 1] * g[:, 0], (d * g).sum(1)))
+        assert err.max() <= 1e-6, err.max()
+    # the band brackets the coarse fan's single escape/capture transition
+    flips = np.nonzero(fan[1:, 0] != fan[:-1, 0])[0]
+    assert flips.size == 1 and lo <= psi[flips[0]] and psi[flips[0] + 1] <= hi
+
+
+def test_fan_sky_matches_full_trace(built_lib):
+    wl = _scene()
+    sky = workloads.sky(512, 256)
+    with Context(sky, disc=None, emitter=wl.emitter) as ctx:
+        lay = ctx.render_layered_raw(wl.cam, wl.bh, _params(ctx, wl), diag=True)
+        full = ctx.render_raw(wl.cam, wl.bh, _params(ctx, wl), diag=True)
+    ge = (lay.diag["flags"] & _abi.ST_RAY_ESCAPED) > 0
+    fe = (full.diag["flags"] & _abi.ST_RAY_ESCAPED) > 0
+    assert (ge != fe).mean() <= 0.005
+    both = ge & fe
+    d = angle(lay.diag["dir"][both], full.diag["dir"][both])
+    print("fan sky vs trace: median", np.median(d), "p99", np.percentile(d, 99), "max", d.max(),
+          "ms", lay.stats["kernel_ms"], full.stats["kernel_ms"])
+    assert np.median(d) <= 1e-6 and np.percentile(d, 99) <= 1e-4
+    assert np.isfinite(lay.image).all()
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+def test_layer_and_composite_match_full_trace(built_lib, prec):
+    wl = _scene(disc=True)
+    sky = workloads.sky(512, 256)
+    with Context(sky, disc=wl.disc, emitter=wl.emitter) as ctx:
+        lay = ctx.render_layered_raw(wl.cam, wl.bh, _params(ctx, wl, prec))
+        half = ctx.render_layered_raw(wl.cam, wl.bh, _params(ctx, wl, prec), layer_size=(wl.width // 2, wl.height // 2))
+        full = ctx.render_raw(wl.cam, wl.bh, _params(ctx, wl, prec))
+    lum = full.image.astype(np.float64).sum(-1)
+    rel = np.abs(lay.image - full.image).sum(-1) / np.maximum(lum, 1e-6)
+    relh = np.abs(half.image - full.image).sum(-1) / np.maximum(lum, 1e-6)
+    print("layered vs trace: median", np.median(rel), "p99", np.percentile(rel, 99),
+          "half-res layer median", np.median(relh), "steps", lay.stats["steps"], half.stats["steps"],
+          full.stats["steps"], "ms", lay.stats["kernel_ms"], half.stats["kernel_ms"], full.stats["kernel_ms"])
+    assert lay.stats["status"] == _abi.ST_OK
+    assert np.median(rel) <= 1e-4
+    # rays the fan proves miss the disc are not traced
+    assert lay.stats["steps"] < full.stats["steps"]
+    assert half.stats["steps"] < lay.stats["steps"]
+    assert np.median(relh) <= 0.05 and np.isfinite(half.image).all()
+
+
+def test_layered_rejects_what_the_fan_cannot_index(built_lib):
+    wl = _scene()
+    sky = workloads.sky(64, 32)
+    with Context(sky, disc=None, emitter=wl.emitter) as ctx:
+        p = _params(ctx, wl)
+        with pytest.raises(_abi.StError) as e:
+            ctx.render_layered_raw(wl.cam, workloads.Kerr(1.0, 0.5), p)
+        assert e.value.code == _abi.ST_EUNSUPPORTED
+        moving = Camera(wl.cam.pos, wl.cam.fwd, wl.cam.right, wl.cam.up_local, wl.cam.fov_factor,
+                        np.array([0.0, 0.1, 0.0]))
+        with pytest.raises(_abi.StError) as e:
+            ctx.render_layered_raw(moving, wl.bh, p)
+        assert e.value.code == _abi.ST_EUNSUPPORTED
