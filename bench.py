@@ -229,6 +229,57 @@ def surrogate_variant(ctx_cls, device: int, flush, sigma: float, reps: int = 3) 
     return out
 
 
+def layered_variant(ctx_cls, device: int, flush, reps: int = 3) -> dict:
+    """The layered engine on a Schwarzschild frame: config 0's camera and hole
+    (static camera at r = 30 M, Lens(24)) with the kernel's rules and its thin
+    disc (3-20 M, exact emitter) at 1920x1080, FP32.  The full per-pixel trace
+    against the layered frame (fan-driven sky, disc layer at the display and
+    at half resolution): time per frame with the fans built (first frame at a
+    radius) and cached (every later frame at that radius), and the radiance
+    difference from the full trace."""
+    import numpy as np
+    import torch
+    from spacetime_gb300 import _abi, workloads
+    w = workloads.config0().scaled(1920, 1080)
+    w.semantics = _abi.ST_SEM_DRAFT
+    w.emitter = _abi.ST_EMIT_KS_EXACT
+    w.params = dict(samples=1, pixel_jitter=0, exit_landing=1)
+    ctx = ctx_cls(workloads.sky(), disc=w.disc, emitter=w.emitter, device=device)
+    p = ctx.params(w.semantics, width=w.width, height=w.height, precision=_abi.ST_PREC_FP32, **w.params)
+    out = {"workload": "config0 camera and hole (Schwarzschild, static r=30 M, Lens(24)), 1920x1080, kernel rules, "
+                       "thin disc 3-20 M exact emitter, FP32"}
+
+    def timed(fn):
+        ts = []
+        for _ in range(reps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            r = fn()
+            ts.append(r.stats["kernel_ms"])
+        return r, float(np.mean(ts))
+
+    full, ms_full = timed(lambda: ctx.render_raw(w.cam, w.bh, p))
+    out["full_trace"] = {"ms_per_step": ms_full, "value": 1920 * 1080 / (ms_full * 1e-3) / 1e6,
+                         "steps": full.stats["steps"]}
+    lum = np.maximum(full.image.astype(np.float64).sum(-1), 1e-6)
+    for name, size in (("layered", None), ("layered_half_res_layer", (960, 540))):
+        # a radius not yet seen: the fans are built with the frame
+        from spacetime_gb300.scene import Camera
+        other = Camera.look_at((0.0, -25.0, 3.0), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), w.cam.fov_factor)
+        ctx.render_layered_raw(other, w.bh, p, layer_size=size)
+        torch.cuda.synchronize()
+        cold = ctx.render_layered_raw(w.cam, w.bh, p, layer_size=size)
+        lay, ms = timed(lambda: ctx.render_layered_raw(w.cam, w.bh, p, layer_size=size))
+        rel = np.abs(lay.image.astype(np.float64) - full.image).sum(-1) / lum
+        out[name] = {"ms_per_step": ms, "value": 1920 * 1080 / (ms * 1e-3) / 1e6,
+                     "ms_first_frame_at_radius": cold.stats["kernel_ms"], "steps": lay.stats["steps"],
+                     "speedup_vs_full_trace": ms_full / ms,
+                     "radiance_rel_vs_full_median": float(np.median(rel)),
+                     "radiance_rel_vs_full_p99": float(np.percentile(rel, 99))}
+    ctx.close()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -467,6 +518,10 @@ def main(argv=None):
             variants["surrogate_no_gas"] = surrogate_variant(Context, local, flush, args.sigma)
         except Exception as e:  # report, do not fail the bench
             variants["surrogate_no_gas"] = {"failed": str(e)}
+        try:
+            variants["layered_schwarzschild"] = layered_variant(Context, local, flush)
+        except Exception as e:  # report, do not fail the bench
+            variants["layered_schwarzschild"] = {"failed": str(e)}
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         try:

@@ -320,6 +320,13 @@ struct st_context {
   float* d_band = nullptr;
   float4* d_layer = nullptr;
   size_t layer_cap = 0;
+  // the fans depend only on the camera radius and the integration rules:
+  // the parameters of the last build, and whether the buffers hold them
+  st::lay::FanParams fan_key;
+  int fan_prec = -1;
+  bool fan_valid = false;
+  cudaStream_t side = nullptr;  // the fine fan runs here, beside the layer pass
+  cudaEvent_t ev_coarse = nullptr, ev_fine = nullptr;
   st_surrogate* sur = nullptr;  // attached surrogate (not owned)
   int* d_list = nullptr;        // surrogate fallback pixels
   size_t list_cap = 0;
@@ -703,7 +710,8 @@ int build_fans(st_context* ctx, const st_camera* cam, const st_spacetime* stp, c
   fc.fov_factor = 1.0;
   fc.projection = ST_PROJ_PINHOLE;
   fc.focus_dist = 1.0;
-  st::lay::FanParams fp{};
+  st::lay::FanParams fp;
+  std::memset(&fp, 0, sizeof fp);
   st::Variant w;
   int rc = fill_params(ctx, &fc, stp, rp, &fp.p, &w);
   if (rc != ST_OK) return rc;
@@ -719,17 +727,36 @@ int build_fans(st_context* ctx, const st_camera* cam, const st_spacetime* stp, c
   if (!ctx->d_fan && cudaMalloc(&ctx->d_fan, FAN_N * sizeof(float4)) != cudaSuccess) return ST_ENOMEM;
   if (!ctx->d_fine && cudaMalloc(&ctx->d_fine, FAN_FINE * sizeof(float4)) != cudaSuccess) return ST_ENOMEM;
   if (!ctx->d_band && cudaMalloc(&ctx->d_band, 2 * sizeof(float)) != cudaSuccess) return ST_ENOMEM;
-  ST_CUDA(cudaMemsetAsync(ctx->d_band, 0, 2 * sizeof(float), s));
+  if (!ctx->side && cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess) return ST_ECUDA;
+  if (!ctx->ev_coarse && cudaEventCreateWithFlags(&ctx->ev_coarse, cudaEventDisableTiming) != cudaSuccess)
+    return ST_ECUDA;
+  if (!ctx->ev_fine && cudaEventCreateWithFlags(&ctx->ev_fine, cudaEventDisableTiming) != cudaSuccess)
+    return ST_ECUDA;
   fp.out = ctx->d_fan;
   fp.n = FAN_N;
   fp.band = 0;
   fp.band_lohi = ctx->d_band;
-  ST_CUDA(st::launch_skyfan(rp->precision, fp, s));
-  ST_CUDA(st::launch_fanband(ctx->d_fan, FAN_N, FAN_PAD, ctx->d_band, s));
-  fp.out = ctx->d_fine;
-  fp.n = FAN_FINE;
-  fp.band = 1;
-  ST_CUDA(st::launch_skyfan(rp->precision, fp, s));
+  const bool cached = ctx->fan_valid && ctx->fan_prec == rp->precision &&
+                      std::memcmp(&ctx->fan_key, &fp, sizeof fp) == 0;
+  if (!cached) {
+    ctx->fan_valid = false;
+    // coarse fan and its band on the main stream; the fine fan (which only
+    // the composite reads) on the side stream, overlapping the layer pass
+    ST_CUDA(cudaMemsetAsync(ctx->d_band, 0, 2 * sizeof(float), s));
+    ST_CUDA(st::launch_skyfan(rp->precision, fp, s));
+    ST_CUDA(st::launch_fanband(ctx->d_fan, FAN_N, FAN_PAD, ctx->d_band, s));
+    ST_CUDA(cudaEventRecord(ctx->ev_coarse, s));
+    ST_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_coarse, 0));
+    st::lay::FanParams ff = fp;
+    ff.out = ctx->d_fine;
+    ff.n = FAN_FINE;
+    ff.band = 1;
+    ST_CUDA(st::launch_skyfan(rp->precision, ff, ctx->side));
+    ST_CUDA(cudaEventRecord(ctx->ev_fine, ctx->side));
+    ctx->fan_key = fp;
+    ctx->fan_prec = rp->precision;
+    ctx->fan_valid = true;
+  }
   // the radial axis of the static frame at the camera: the forward vector of
   // a camera at rest looking straight out (any completion of the basis)
   double xh[3];
@@ -977,6 +1004,9 @@ void st_context_destroy(st_context* ctx) {
   cudaFree(ctx->d_fine);
   cudaFree(ctx->d_band);
   cudaFree(ctx->d_layer);
+  if (ctx->ev_coarse) cudaEventDestroy(ctx->ev_coarse);
+  if (ctx->ev_fine) cudaEventDestroy(ctx->ev_fine);
+  if (ctx->side) cudaStreamDestroy(ctx->side);
   cudaFree(ctx->d_vol);
   cudaFree(ctx->d_fb);
   cudaFree(ctx->d_rgb);
@@ -1030,6 +1060,7 @@ int st_sky_fan(st_context* ctx, const st_camera* cam, const st_spacetime* stp, c
   cudaStream_t s = ctx->stream;
   double er[4];
   if ((rc = build_fans(ctx, cam, stp, rp, p, er, s)) != ST_OK) return rc;
+  ST_CUDA(cudaStreamWaitEvent(s, ctx->ev_fine, 0));
   ST_CUDA(cudaMemcpyAsync(fan, ctx->d_fan, FAN_N * sizeof(float4), cudaMemcpyDeviceToHost, s));
   ST_CUDA(cudaMemcpyAsync(fine, ctx->d_fine, FAN_FINE * sizeof(float4), cudaMemcpyDeviceToHost, s));
   ST_CUDA(cudaMemcpyAsync(band, ctx->d_band, 2 * sizeof(float), cudaMemcpyDeviceToHost, s));
@@ -1096,6 +1127,7 @@ int st_render_layered(st_context* ctx, const st_camera* cam, const st_spacetime*
     p.diag = host_diag ? ctx->d_diag : nullptr;
     p.first_pass = (k == 0) ? 1 : 0;
     p.weight = (float)(1.0 / passes.size());
+    if (k == 0) ST_CUDA(cudaStreamWaitEvent(s, ctx->ev_fine, 0));
     ST_CUDA(st::launch_composite(rp->precision, p, cp, s));
     ++launches;
   }
