@@ -124,3 +124,21 @@ def test_layered_rejects_what_the_fan_cannot_index(built_lib):
         with pytest.raises(_abi.StError) as e:
             ctx.render_layered_raw(moving, wl.bh, p)
         assert e.value.code == _abi.ST_EUNSUPPORTED
+
+
+def test_fan_cache_follows_the_camera_radius(built_lib):
+    wl = _scene(disc=True, w=96, h=54)
+    sky = workloads.sky(512, 256)
+    other = Camera.look_at((0.0, -25.0, 3.0), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), wl.cam.fov_factor)
+    with Context(sky, disc=wl.disc, emitter=wl.emitter) as ctx:
+        p = _params(ctx, wl, FP32)
+        a = ctx.render_layered_raw(wl.cam, wl.bh, p)
+        b = ctx.render_layered_raw(other, wl.bh, p)
+        a2 = ctx.render_layered_raw(wl.cam, wl.bh, p)     # fans rebuilt for r = 30
+        a3 = ctx.render_layered_raw(wl.cam, wl.bh, p)     # fans reused
+        fan_a, _, _ = ctx.sky_fan(wl.cam, wl.bh, p)
+        fan_b, _, _ = ctx.sky_fan(other, wl.bh, p)
+    assert not np.array_equal(a.image, b.image)
+    np.testing.assert_array_equal(a.image, a2.image)
+    np.testing.assert_array_equal(a.image, a3.image)
+    assert not np.array_equal(fan_a, fan_b)
