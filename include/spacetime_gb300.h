@@ -185,6 +185,15 @@ typedef struct {
                                 radius-adaptive step / free up to 50 dt
                                 (DRAFT, FP32 or FP64, pixel schedule) */
   double tol;                /* adaptive tolerance (`tol`, default 1e-4) */
+  /* adaptive refinement (render_draft_mtl `refine`, src/metal.jl:2104-2240):
+   * refine > 1 flags pixels whose per-ray luminance std-dev over the base
+   * passes exceeds refine_var * (mean + 0.01) or whose Bardeen graze fraction
+   * exceeds refine_graze, and re-renders their bounding box (+ refine_margin
+   * pixels) refine - 1 more times with fresh strata; DRAFT, no surrogate */
+  int refine;                /* default 1 (off) */
+  double refine_var;         /* default 0.35 */
+  double refine_graze;       /* default 0.05 */
+  int refine_margin;         /* default 8 */
 } st_render_params;
 
 typedef struct {

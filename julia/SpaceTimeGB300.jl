@@ -50,6 +50,7 @@ mutable struct StRenderParams
     surrogate::Cint; surrogate_sigma::Float64
     block_x::Cint; block_y::Cint; chunk_steps::Cint; graph::Cint
     order::Cint; tol::Float64
+    refine::Cint; refine_var::Float64; refine_graze::Float64; refine_margin::Cint
     StRenderParams() = new()
 end
 struct StStarfield

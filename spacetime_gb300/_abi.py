@@ -83,6 +83,7 @@ class StRenderParams(C.Structure):
         ("surrogate", C.c_int), ("surrogate_sigma", C.c_double),
         ("block_x", C.c_int), ("block_y", C.c_int), ("chunk_steps", C.c_int), ("graph", C.c_int),
         ("order", C.c_int), ("tol", C.c_double),
+        ("refine", C.c_int), ("refine_var", C.c_double), ("refine_graze", C.c_double), ("refine_margin", C.c_int),
     ]
 
 

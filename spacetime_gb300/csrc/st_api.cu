@@ -327,6 +327,10 @@ struct st_context {
   bool fan_valid = false;
   cudaStream_t side = nullptr;  // the fine fan runs here, beside the layer pass
   cudaEvent_t ev_coarse = nullptr, ev_fine = nullptr;
+  // adaptive refinement: per-pixel luminance moments, the flagged box
+  float4* d_stat = nullptr;
+  size_t stat_cap = 0;
+  unsigned* d_box = nullptr;
   st_surrogate* sur = nullptr;  // attached surrogate (not owned)
   int* d_list = nullptr;        // surrogate fallback pixels
   size_t list_cap = 0;
@@ -524,10 +528,12 @@ struct Motion {
 // The samples^2 passes of render_draft_mtl (src/metal.jl:2091-2168) or of
 // render's stratified offsets (src/raytrace.jl:375-419).  Host draws use
 // splitmix64 seeded by p->seed.
-std::vector<PassPlan> plan_passes(const st_render_params* rp, const st_camera* cam) {
+std::vector<PassPlan> plan_passes(const st_render_params* rp, const st_camera* cam, int block = 0) {
   const int S = rp->samples;
   const int n = S * S;
-  st::Rng rng{rp->seed ^ 0x5eed5eedull};
+  // block b > 0: a refinement block, with fresh strata and pass numbers
+  // continuing after the base passes (src/metal.jl:2116-2120, 2218-2227)
+  st::Rng rng{(rp->seed ^ 0x5eed5eedull) + 0x9e3779b97f4a7c15ull * (unsigned long long)block};
   std::vector<int> order(n), lens(n), tperm(n);
   for (int k = 0; k < n; ++k) { order[k] = k; lens[k] = k; tperm[k] = k; }
   if (rp->pixel_jitter) st::shuffle(order, rng);
@@ -549,16 +555,17 @@ std::vector<PassPlan> plan_passes(const st_render_params* rp, const st_camera* c
       pp.jv = (b + 0.5) / S + shift;
       pp.jw = 0.0;
     }
-    pp.jseed = 15485863 + (k + 1);
+    const int pass = block * n + k + 1;
+    pp.jseed = 15485863 + pass;
     if (dof) {
       const int lm = lens[k];
       pp.lens_u0 = (double)(lm / S) / S;
       pp.lens_v0 = (double)(lm % S) / S;
       pp.lens_w = 1.0 / S;
-      pp.lens_seed = k + 1;
+      pp.lens_seed = pass;
     }
     pp.time_m = tperm[k];
-    pp.shutter_seed = 104729 + (k + 1);  // clear of the lens seeds (src/metal.jl:2148-2150)
+    pp.shutter_seed = 104729 + pass;  // clear of the lens seeds (src/metal.jl:2148-2150)
     out[k] = pp;
   }
   return out;
@@ -577,6 +584,32 @@ int pose_params(st_context* ctx, const st_camera* cam, const st_camera* pose, co
   pc.fov_factor = pose->fov_factor;
   st::Variant w;
   return fill_params(ctx, &pc, stp, rp, out, &w);
+}
+
+// Adaptive refinement (src/metal.jl:2189-2213): a pixel is flagged when its
+// per-ray luminance std-dev exceeds var (mean + 0.01) or its graze fraction
+// exceeds graze; box = {min col, min row} (init all ones) and {max col + 1,
+// max row + 1} (init 0) of the flagged pixels.
+__global__ void refine_box_kernel(const float4* __restrict__ stat, int W, int H, float var, float graze,
+                                  unsigned* box) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= W || j >= H) return;
+  const float4 s4 = stat[j * W + i];
+  const float s2 = s4.y - s4.x * s4.x;
+  if ((s2 > 0.f && sqrtf(s2) > var * (s4.x + 0.01f)) || s4.z > graze) {
+    atomicMin(box + 0, (unsigned)i);
+    atomicMin(box + 1, (unsigned)j);
+    atomicMax(box + 2, (unsigned)(i + 1));
+    atomicMax(box + 3, (unsigned)(j + 1));
+  }
+}
+
+// The refined box holds refine x the weight of the rest: renormalise.
+__global__ void scale_box_kernel(float4* fb, int W, int c0, int r0, int cols, int rows, float s) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= cols || j >= rows) return;
+  float4& o = fb[(r0 + j) * W + (c0 + i)];
+  o.x *= s; o.y *= s; o.z *= s;
 }
 
 int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
@@ -608,16 +641,26 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
     if (!ctx->d_count && cudaMalloc(&ctx->d_count, sizeof(int)) != cudaSuccess) return ST_ENOMEM;
     v.sched = ST_SCHED_PIXEL;
   }
+  const int refine = rp->refine > 1 ? rp->refine : 1;
+  if (refine > 1) {
+    if (rp->semantics != ST_SEM_DRAFT || rp->surrogate) return ST_EUNSUPPORTED;
+    if ((rc = ensure(&ctx->d_stat, &ctx->stat_cap, npix)) != ST_OK) return rc;
+    if (!ctx->d_box && cudaMalloc(&ctx->d_box, 4 * sizeof(unsigned)) != cudaSuccess) return ST_ENOMEM;
+    v.sched = ST_SCHED_PIXEL;  // refinement passes dispatch a box of the pixel grid
+  }
   ST_CUDA(cudaMemsetAsync(ctx->d_counters, 0, st::CNT_N * sizeof(unsigned long long), s));
   const std::vector<PassPlan> passes = plan_passes(rp, cam);
   p.weight = (float)(1.0 / passes.size());
   ST_CUDA(cudaEventRecord(ctx->ev0, s));
+  if (refine > 1) {
+    ST_CUDA(cudaMemsetAsync(ctx->d_stat, 0, npix * sizeof(float4), s));
+    p.stat = ctx->d_stat;
+  }
   int launches = 0;
-  for (size_t k = 0; k < passes.size(); ++k) {
-    const PassPlan& pp = passes[k];
+  auto run_pass = [&](const PassPlan& pp, bool first) -> int {
     p.ju = pp.ju; p.jv = pp.jv; p.jw = pp.jw; p.jseed = pp.jseed;
     p.lens_u0 = pp.lens_u0; p.lens_v0 = pp.lens_v0; p.lens_w = pp.lens_w; p.lens_seed = pp.lens_seed;
-    p.first_pass = (k == 0) ? 1 : 0;
+    p.first_pass = first ? 1 : 0;
     if (mo) {
       // this pass's pose: the stratum midpoint, or its start with the end
       // pose for the per-pixel shutter
@@ -655,6 +698,39 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
     }
     ST_CUDA(st::launch_trace(v, p, rp->block_x, rp->block_y, ctx->num_sms, s));
     ++launches;
+    return ST_OK;
+  };
+  for (size_t k = 0; k < passes.size(); ++k)
+    if ((rc = run_pass(passes[k], k == 0)) != ST_OK) return rc;
+  if (refine > 1) {
+    // the flagged box (+ margin), re-rendered refine - 1 more times with fresh
+    // strata, then renormalised (src/metal.jl:2189-2240)
+    p.stat = nullptr;
+    ST_CUDA(cudaMemsetAsync(ctx->d_box, 0xFF, 2 * sizeof(unsigned), s));
+    ST_CUDA(cudaMemsetAsync(ctx->d_box + 2, 0, 2 * sizeof(unsigned), s));
+    const dim3 blk(16, 8), grd((rp->width + 15) / 16, (rp->height + 7) / 8);
+    refine_box_kernel<<<grd, blk, 0, s>>>(ctx->d_stat, rp->width, rp->height, (float)rp->refine_var,
+                                          (float)rp->refine_graze, ctx->d_box);
+    ST_CUDA(cudaGetLastError());
+    unsigned box[4];
+    ST_CUDA(cudaMemcpyAsync(box, ctx->d_box, sizeof box, cudaMemcpyDeviceToHost, s));
+    ST_CUDA(cudaStreamSynchronize(s));
+    if (box[2] > 0) {
+      const int m = std::max(rp->refine_margin, 0);
+      const int c0 = std::max((int)box[0] - m, 0), r0 = std::max((int)box[1] - m, 0);
+      const int c1 = std::min((int)box[2] + m, rp->width), r1 = std::min((int)box[3] + m, rp->height);
+      p.box_col0 = c0; p.box_row0 = r0; p.box_cols = c1 - c0; p.box_rows = r1 - r0;
+      for (int b = 1; b < refine; ++b) {
+        const std::vector<PassPlan> more = plan_passes(rp, cam, b);
+        for (const PassPlan& pp : more)
+          if ((rc = run_pass(pp, false)) != ST_OK) return rc;
+      }
+      const dim3 gb((p.box_cols + 15) / 16, (p.box_rows + 7) / 8);
+      scale_box_kernel<<<gb, blk, 0, s>>>(ctx->d_fb, rp->width, c0, r0, p.box_cols, p.box_rows,
+                                          1.0f / (float)refine);
+      ST_CUDA(cudaGetLastError());
+      p.box_cols = 0;
+    }
   }
   ST_CUDA(cudaEventRecord(ctx->ev1, s));
   unsigned long long cnt[st::CNT_N];
@@ -844,6 +920,10 @@ void st_render_params_default(st_render_params* p, int semantics) {
   p->chunk_steps = 32;
   p->order = 4;
   p->tol = 1e-4;
+  p->refine = 1;
+  p->refine_var = 0.35;
+  p->refine_graze = 0.05;
+  p->refine_margin = 8;
   if (semantics == ST_SEM_RENDER) {
     // render(...; width=400, height=200, samples=1): FP64 like the CPU path
     p->width = 400; p->height = 200;
@@ -1000,6 +1080,8 @@ void st_context_destroy(st_context* ctx) {
   cudaFree(ctx->d_sky);
   cudaFree(ctx->d_lut);
   cudaFree(ctx->d_star_lut);
+  cudaFree(ctx->d_stat);
+  cudaFree(ctx->d_box);
   cudaFree(ctx->d_fan);
   cudaFree(ctx->d_fine);
   cudaFree(ctx->d_band);

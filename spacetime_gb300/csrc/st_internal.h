@@ -74,6 +74,11 @@ struct TraceParams {
   const float4* star_lut;    // [star_lut_size] RGB_, the stars' own white point
   int star_lut_size, star_seed;
   double star_lut_tmin, star_lut_tmax;
+  // adaptive refinement (src/metal.jl:1640-1700, 2104-2240): per-pixel
+  // (sum w L, sum w L^2, sum w graze, -) over the base passes, or null; and
+  // the dispatch box of a refinement pass (box_cols = 0: the whole frame)
+  float4* stat;
+  int box_col0, box_row0, box_cols, box_rows;
   // layered engine's disc / gas layer (src/metal.jl:1096-1135, 1204-1212,
   // 1616-1626; Schwarzschild, DRAFT): layer = 1 traces only emission and
   // transmittance, culling rays the deflection fan proves stay outside

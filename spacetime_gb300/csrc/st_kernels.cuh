@@ -44,6 +44,11 @@ __global__ void __launch_bounds__(128, ORD == 4 ? ST_MINB : ST_MINB_ADAPTIVE) tr
   using R = typename RealOf<PREC>::T;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (p.box_cols > 0) {  // a refinement pass over its box only
+    if (i >= p.box_cols || j >= p.box_rows) i = p.width;  // idle
+    i += p.box_col0;
+    j += p.box_row0;
+  }
   if (p.pix_list) {  // 1-D over a compacted pixel list
     const int t = blockIdx.x * (blockDim.x * blockDim.y) + threadIdx.y * blockDim.x + threadIdx.x;
     if (t < *p.n_list) {
@@ -156,6 +161,7 @@ cudaError_t launch_variant(const TraceParams& p, int sched, int bx, int by, int 
     if (bx <= 0 || by <= 0 || bx * by != 128) { bx = 16; by = 8; }
     dim3 block(bx, by);
     dim3 grid((p.width + bx - 1) / bx, (p.height + by - 1) / by);
+    if (p.box_cols > 0) grid = dim3((p.box_cols + bx - 1) / bx, (p.box_rows + by - 1) / by);
     if (p.pix_list) grid = dim3((unsigned)(((long long)p.width * p.height + 127) / 128), 1);
     else if (p.frames) grid.z = (unsigned)(p.n_frames > 0 ? p.n_frames : 1);
     if constexpr (SEM == ST_SEM_DRAFT && PREC != ST_PREC_FP32_GUARDED) {

@@ -1179,6 +1179,16 @@ __device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typena
     st.flags |= ST_RAY_BLACK;
   }
   const float w = p.weight;
+  if (p.stat) {
+    // per-ray luminance moments and the graze fraction for adaptive
+    // refinement (src/metal.jl:1640-1700); weights sum to 1 over the base passes
+    const float L = 0.2126f * (float)rgb[0] + 0.7152f * (float)rgb[1] + 0.0722f * (float)rgb[2];
+    float4 s4 = p.stat[out_index];
+    s4.x += w * L;
+    s4.y += w * L * L;
+    if (st.flags & ST_RAY_GRAZE) s4.z += w;
+    p.stat[out_index] = s4;
+  }
   float4 o = make_float4(w * (float)rgb[0], w * (float)rgb[1], w * (float)rgb[2], (float)st.alpha);
   if (!p.first_pass) {
     const float4 prev = p.out[out_index];

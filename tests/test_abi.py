@@ -55,6 +55,8 @@ int main(void) {
   O(st_render_params, seed) O(st_render_params, chunk_steps) O(st_render_params, surrogate_sigma)
   O(st_stats, d2h_bytes) O(st_ray_diag, flags) O(st_ray_diag, fp64_steps)
   O(st_render_params, graph) O(st_render_params, order) O(st_render_params, tol)
+  O(st_render_params, refine) O(st_render_params, refine_var) O(st_render_params, refine_margin)
+  S(st_starfield) O(st_starfield, table_size) O(st_starfield, seed) O(st_starfield, galactic)
   return 0;
 }
 """
@@ -69,7 +71,7 @@ def test_struct_layouts_match_ctypes(tmp_path):
                if line)
     mirror = {"st_camera": _abi.StCamera, "st_spacetime": _abi.StSpacetime, "st_disc": _abi.StDisc,
               "st_volume": _abi.StVolume, "st_render_params": _abi.StRenderParams, "st_stats": _abi.StStats,
-              "st_ray_diag": _abi.StRayDiag}
+              "st_ray_diag": _abi.StRayDiag, "st_starfield": _abi.StStarfield}
     for name, cls in mirror.items():
         assert int(got[name]) == C.sizeof(cls), name
     for key, val in got.items():
