@@ -33,6 +33,9 @@
  *                          fan_band_kernel!, src/metal.jl:2416-2517, 2888-2898)
  *   st_render_layered      render_layered_gpu!, src/metal.jl:3040-3147 (layer pass of
  *                          trace_kernel_mtl!, sky_composite_kernel!, :2707-2880)
+ *   st_render_depth        render_depth_mtl, src/metal.jl:1935-1990 (trace_kernel_mtl!
+ *                          with NB > 0: :1170-1175, 1425-1426, 1489-1497, 1556-1563,
+ *                          1687-1690)
  *
  * Output layout: linear HDR RGB float32 in the reference's column-major
  * (3, width, height) order, i.e. out[3*(i + width*j) + c] for 0-based pixel
@@ -283,6 +286,20 @@ int st_render_device(st_context* ctx, const st_camera* cam, const st_spacetime* 
 int st_render_motion(st_context* ctx, const st_camera* cam, const st_camera* poses, int nposes,
                      int per_pixel_shutter, const st_spacetime* st, const st_render_params* p,
                      float* out_rgb, st_ray_diag* diag, st_stats* stats);
+
+/* Depth-bucketed draft frame (render_depth_mtl): the DRAFT trace with each
+ * disc / gas emission written into one of nbuckets path-length buckets instead
+ * of the pixel sum.  Path length ell is the integral of |dx/dlambda| over the
+ * accepted steps; bucket 1 takes ell <= 1.5 M, buckets 1..nbuckets-1 are
+ * log-spaced to 120 M (index trunc((ln ell - ln 1.5) (nbuckets - 2) / ln 80) + 1,
+ * clamped), and bucket nbuckets holds the escaped sky times the remaining
+ * transmittance.  out_buckets is the reference's (3 nbuckets, width, height)
+ * column-major array: out[3 nbuckets (i + width j) + 3 b + c] for 0-based
+ * bucket b and channel c; the samples^2 passes are averaged as in st_render.
+ * nbuckets in [3, 64] (ST_EINVAL otherwise; the reference requires >= 3).
+ * DRAFT only, no surrogate, no refinement (ST_EUNSUPPORTED). */
+int st_render_depth(st_context* ctx, const st_camera* cam, const st_spacetime* st, const st_render_params* p,
+                    int nbuckets, float* out_buckets, st_stats* stats);
 
 /* Raw HDR frame files, save_raw / load_raw (src/rawio.jl:18-42): a linear,
  * unclamped 32-bit float RGB TIFF in display orientation (the reference's

@@ -80,6 +80,8 @@ def lib() -> C.CDLL:
         dp = P(C.c_double)
         L.orc_render.argtypes = [P(OrcScene), FP, C.c_void_p, C.c_int]
         L.orc_render.restype = C.c_int
+        L.orc_render_depth.argtypes = [P(OrcScene), C.c_int, FP, C.c_int]
+        L.orc_render_depth.restype = C.c_int
         L.orc_trace_dirs.argtypes = [P(OrcScene), C.c_int, P(C.c_double), C.c_void_p, C.c_int]
         L.orc_trace_dirs.restype = C.c_int
         L.orc_rhs.argtypes = [C.c_int, dp, C.c_double, C.c_double, C.c_double, dp]
@@ -339,6 +341,17 @@ class Scene:
         if rc != 0:
             raise RuntimeError(f"orc_render failed ({rc})")
         return out, rays
+
+    def render_depth(self, nb: int, nthreads: int = 0):
+        """One unweighted DRAFT pass split into nb depth buckets:
+        (rows, cols, nb, 3), the last bucket the sky (orc_render_depth)."""
+        s = self.s
+        out = np.zeros((s.rows, s.cols, nb, 3), dtype=np.float32)
+        rc = lib().orc_render_depth(C.byref(s), int(nb), out.ctypes.data_as(FP), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"orc_render_depth failed ({rc})")
+        return out
+
 
 
 def scene_for(w, sky, integrator, width=None, height=None, rect=None, **kw) -> Scene:

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <vector>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -708,7 +709,20 @@ void star_light(const orc_scene* s, bool draft, double dx, double dy, double dz,
   rgb[0] = ar; rgb[1] = ag; rgb[2] = ab;
 }
 
-void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
+// Depth bucket of path length ell, 1-based (src/metal.jl:1489-1492): bucket 1
+// below 1.5 M, then trunc((ln ell - ln 1.5) (nb - 2) 0.22820) + 1 clamped to
+// [1, nb - 1]; bucket nb is the sky's.
+int depth_bucket(double ell, int nb) {
+  if (ell <= 1.5) return 1;
+  const double bscale = nb > 2 ? (nb - 2) * 0.22820 : 1.0;
+  const int b = (int)((std::log(ell) - 0.405465) * bscale) + 1;
+  return std::min(std::max(b, 1), nb - 1);
+}
+
+// bk (3 nb doubles, may be null): depth-bucket mode; emission is moved into
+// bk as it happens and the sky (times the transmittance) into the last bucket
+// (src/metal.jl:1170-1175, 1425-1426, 1489-1497, 1556-1563, 1687-1690).
+void trace_ray(const Scene& S, int i0, int j0, RayOut* ro, double* bk = nullptr, int nb = 0) {
   const orc_scene* s = S.s;
   const Phys& P = S.P;
   const double M = P.M;
@@ -797,6 +811,12 @@ void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
   double march_acc = 0.0;
   bool hit = false, escaped = false, budget = true;
   double lambda = 0.0;
+  double ell = 0.0;  // depth buckets: path length
+  auto flush_bucket = [&]() {
+    if (!bk) return;
+    double* b = bk + 3 * (depth_bucket(ell, nb) - 1);
+    for (int c = 0; c < 3; ++c) { b[c] += acc[c]; acc[c] = 0.0; }
+  };
   double k1[6];
   P.rhs(y, pt, k1);
   int rhs_evals = 1;
@@ -951,7 +971,9 @@ void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
       lambda += h_used;
       const double vlen = std::max(std::sqrt(k1[0] * k1[0] + k1[1] * k1[1] + k1[2] * k1[2]), 1e-20);
       bool stop = false;
+      if (bk) ell += h_used * vlen;
       if (S.vol_on) stop = march_gas(S, y, yn, pt, h_used, vlen, r2, scam, &march_acc, acc, &alpha);
+      flush_bucket();
       if (stop) {
         for (int c = 0; c < 6; ++c) y[c] = yn[c];
         ++steps;
@@ -967,6 +989,7 @@ void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
           for (int c = 0; c < 6; ++c) ye[c] = y[c] + cfz * (yn[c] - y[c]);
         }
         disc_event(ye, pt);
+        flush_bucket();
       }
       // exit landing: the first state beyond r_escape is replaced by the state on it
       if (s->exit_landing) {
@@ -1010,6 +1033,8 @@ void trace_ray(const Scene& S, int i0, int j0, RayOut* ro) {
     }
     sky_tint(scam, sky);
     for (int c = 0; c < 3; ++c) rgb[c] += alpha * sky[c];
+    if (bk)
+      for (int c = 0; c < 3; ++c) bk[3 * (nb - 1) + c] += alpha * sky[c];
   }
   rec.flags |= (escaped ? ORC_RAY_ESCAPED : 0) | (hit ? ORC_RAY_CAPTURED : 0) | (budget ? ORC_RAY_BUDGET : 0) |
                (black ? ORC_RAY_BLACK : 0);
@@ -1070,6 +1095,29 @@ int orc_render(const orc_scene* s, float* out_rgb, orc_ray* rays, int nthreads) 
       if (out_rgb)
         for (int c = 0; c < 3; ++c) out_rgb[3 * o + c] = (float)ro.rgb[c];
       if (rays) rays[o] = ro.rec;
+    }
+  }
+  return 0;
+}
+
+int orc_render_depth(const orc_scene* s, int nb, float* out, int nthreads) {
+  if (!s || !out || nb < 3 || s->width <= 0 || s->height <= 0 || s->cols <= 0 || s->rows <= 0) return 1;
+  if (std::fabs(s->a) > s->M || s->semantics != ORC_SEM_DRAFT) return 1;
+  Scene S;
+  setup_scene(s, S);
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  const int cols = s->cols, rows = s->rows;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int jj = 0; jj < rows; ++jj) {
+    std::vector<double> bk(3 * (size_t)nb);
+    for (int ii = 0; ii < cols; ++ii) {
+      std::fill(bk.begin(), bk.end(), 0.0);
+      RayOut ro;
+      trace_ray(S, s->col0 + ii, s->row0 + jj, &ro, bk.data(), nb);
+      float* o = out + 3 * (size_t)nb * ((size_t)ii + (size_t)cols * jj);
+      for (int k = 0; k < 3 * nb; ++k) o[k] = (float)bk[k];
     }
   }
   return 0;

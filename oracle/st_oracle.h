@@ -129,6 +129,11 @@ typedef struct {
  * i.e. [rows][cols][3]) and optionally the per-ray records ([rows][cols]). */
 int orc_render(const orc_scene* sc, float* out_rgb, orc_ray* rays, int nthreads);
 
+/* DRAFT render of the sub-rectangle with emission split into nb >= 3 depth
+ * buckets (render_depth_mtl, src/metal.jl:1935-1990): out[rows][cols][nb][3],
+ * one unweighted pass; bucket nb - 1 (0-based) holds the sky. */
+int orc_render_depth(const orc_scene* sc, int nb, float* out, int nthreads);
+
 /* Trace n rays from the scene's camera along camera-frame directions
  * dirs[n][3] = (cf, cr, cu) (forward, right, up coefficients of the tetrad,
  * as a pixel's projection produces them), no lens, jitter or shutter: the

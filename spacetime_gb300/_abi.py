@@ -124,6 +124,7 @@ EXPORTS = [
     "st_surrogate_train", "st_render_frames_noalloc", "st_context_set_surrogate",
     "st_starfield_default", "st_context_set_starfield", "st_render_motion",
     "st_save_raw", "st_load_raw_size", "st_load_raw", "st_sky_fan", "st_render_layered",
+    "st_render_depth",
 ]
 ST_FAN_N, ST_FAN_FINE = 4096, 1024
 
@@ -203,6 +204,9 @@ def load(path: str | None = None) -> C.CDLL:
     lib.st_render_layered.argtypes = [C.c_void_p, P(StCamera), P(StSpacetime), P(StRenderParams), C.c_int, C.c_int,
                                       P(C.c_float), C.c_void_p, P(StStats)]
     lib.st_render_layered.restype = C.c_int
+    lib.st_render_depth.argtypes = [C.c_void_p, P(StCamera), P(StSpacetime), P(StRenderParams), C.c_int,
+                                    P(C.c_float), P(StStats)]
+    lib.st_render_depth.restype = C.c_int
     for name in ("st_context_create", "st_context_set_disc", "st_context_set_volume", "st_render",
                  "st_render_diag", "st_render_device", "st_render_frames", "st_camera_tetrad",
                  "st_surrogate_create", "st_surrogate_num_params", "st_surrogate_get_params",

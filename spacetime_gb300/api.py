@@ -6,6 +6,7 @@
     render(cam, bh, sky; disc, width, height)    src/raytrace.jl:339-428
     Context(sky; disc, volume)                   MetalPreviewContext, src/metal.jl:129-182
     render_draft(ctx, cam, bh; ...)              render_draft_mtl, src/metal.jl:2040-2242
+    render_depth(ctx, cam, bh; nbuckets, ...)    render_depth_mtl, src/metal.jl:1935-1990
 
 Images come back as float32 arrays of shape (height, width, 3): element
 [j, i] is pixel (i, j) of the reference's Matrix{RGBf}(width, height), i.e.
@@ -25,7 +26,7 @@ from .scene import Camera, Volume, lens_fov
 
 __all__ = [
     "Schwarzschild", "Kerr", "Blackbody", "AccretionDisc", "Lens", "Camera", "Context",
-    "render", "render_draft", "render_frames", "camera_tetrad", "RenderResult",
+    "render", "render_draft", "render_depth", "render_frames", "camera_tetrad", "RenderResult",
 ]
 
 
@@ -304,6 +305,17 @@ class Context:
                    "st_render_layered")
         return RenderResult(img, stats.as_dict(), d.reshape(p.height, p.width) if diag else None)
 
+    def render_depth_raw(self, cam: Camera, bh, p: _abi.StRenderParams, nbuckets: int = 10) -> RenderResult:
+        """Depth-bucketed frame (st_render_depth): image has shape
+        (height, width, nbuckets, 3); bucket nbuckets - 1 is the sky."""
+        img = np.empty((p.height, p.width, nbuckets, 3), dtype=np.float32)
+        stats = _abi.StStats()
+        _abi.check(self._lib.st_render_depth(self._h, C.byref(_st_camera(cam)), C.byref(_st_spacetime(bh)),
+                                             C.byref(p), int(nbuckets), img.ctypes.data_as(C.POINTER(C.c_float)),
+                                             C.byref(stats)),
+                   "st_render_depth")
+        return RenderResult(img, stats.as_dict())
+
     def render_frames_raw(self, cams, bh, p: _abi.StRenderParams) -> RenderResult:
         n = len(cams)
         arr = (_abi.StCamera * n)(*[_st_camera(c) for c in cams])
@@ -371,6 +383,25 @@ def render_draft(ctx: Context, cam: Camera, bh, *, width: int = 1920, height: in
                  else [camera_at((m + 0.5) / n) for m in range(n)])
         return ctx.render_motion_raw(cam2, poses, bh, p, per_pixel_shutter=per_pixel_shutter).image
     return ctx.render_raw(cam2, bh, p).image
+
+
+def render_depth(ctx: Context, cam: Camera, bh, *, width: int = 1920, height: int = 1080, samples: int = 2,
+                 dt: float = 0.02, nbuckets: int = 10, fisheye_deg: float = 0.0, relativistic: bool = False,
+                 precision="fp32", seed: int = 0, **kw) -> np.ndarray:
+    """render_depth_mtl(ctx, cam, st; width, height, samples, dt, nbuckets,
+    fisheye_deg, relativistic) (src/metal.jl:1935-1990): a pinhole (or
+    fisheye) draft frame with emission split into nbuckets path-length
+    buckets, log-spaced over 1.5-120 M, the last holding the sky.  Returns
+    (height, width, nbuckets, 3); summing over buckets gives the plain frame.
+    Raises ValueError for nbuckets < 3, as the reference does."""
+    if nbuckets < 3:
+        raise ValueError("nbuckets must be >= 3")
+    cam2 = Camera(cam.pos, cam.fwd, cam.right, cam.up_local, cam.fov_factor, cam.velocity,
+                  _abi.ST_PROJ_FISHEYE if fisheye_deg > 0 else _abi.ST_PROJ_PINHOLE, fisheye_deg, 0.0, 1.0)
+    kw.setdefault("pixel_jitter", 0)
+    p = ctx.params(_abi.ST_SEM_DRAFT, width=width, height=height, samples=samples, dt=dt,
+                   relativistic=int(relativistic), precision=_prec(precision), seed=seed, **kw)
+    return ctx.render_depth_raw(cam2, bh, p, nbuckets).image
 
 
 def render_frames(ctx: Context, cams, bh, *, width: int, height: int, dt: float = 0.02, precision="fp32g",

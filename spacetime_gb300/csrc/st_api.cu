@@ -330,6 +330,8 @@ struct st_context {
   // adaptive refinement: per-pixel luminance moments, the flagged box
   float4* d_stat = nullptr;
   size_t stat_cap = 0;
+  float* d_buckets = nullptr;  // depth buckets, 3 nb floats per pixel
+  size_t buckets_cap = 0;
   unsigned* d_box = nullptr;
   st_surrogate* sur = nullptr;  // attached surrogate (not owned)
   int* d_list = nullptr;        // surrogate fallback pixels
@@ -525,6 +527,12 @@ struct Motion {
   int per_pixel;
 };
 
+// Depth-bucket output of render_depth_mtl (src/metal.jl:1935-1990).
+struct Depth {
+  int nb;
+  float* host;  // (3 nb, width, height)
+};
+
 // The samples^2 passes of render_draft_mtl (src/metal.jl:2091-2168) or of
 // render's stratified offsets (src/raytrace.jl:375-419).  Host draws use
 // splitmix64 seeded by p->seed.
@@ -614,7 +622,7 @@ __global__ void scale_box_kernel(float4* fb, int W, int c0, int r0, int cols, in
 
 int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
               float* host_rgb, st_ray_diag* host_diag, const float** dev_rgba, st_stats* stats,
-              const Motion* mo = nullptr) {
+              const Motion* mo = nullptr, const Depth* depth = nullptr) {
   const auto t0 = std::chrono::steady_clock::now();
   TraceParams p;
   st::Variant v;
@@ -642,6 +650,14 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
     v.sched = ST_SCHED_PIXEL;
   }
   const int refine = rp->refine > 1 ? rp->refine : 1;
+  if (depth) {
+    // emission binned by path length replaces the plain frame
+    if (rp->semantics != ST_SEM_DRAFT || rp->surrogate || refine > 1) return ST_EUNSUPPORTED;
+    if ((rc = ensure(&ctx->d_buckets, &ctx->buckets_cap, 3 * (size_t)depth->nb * npix)) != ST_OK) return rc;
+    ST_CUDA(cudaMemsetAsync(ctx->d_buckets, 0, 3 * (size_t)depth->nb * npix * sizeof(float), s));
+    p.nb = depth->nb;
+    p.buckets = ctx->d_buckets;
+  }
   if (refine > 1) {
     if (rp->semantics != ST_SEM_DRAFT || rp->surrogate) return ST_EUNSUPPORTED;
     if ((rc = ensure(&ctx->d_stat, &ctx->stat_cap, npix)) != ST_OK) return rc;
@@ -746,6 +762,11 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
   if (host_diag) {
     ST_CUDA(cudaMemcpyAsync(host_diag, ctx->d_diag, npix * sizeof(st_ray_diag), cudaMemcpyDeviceToHost, s));
     d2h += npix * sizeof(st_ray_diag);
+  }
+  if (depth) {
+    const size_t nbytes = 3 * (size_t)depth->nb * npix * sizeof(float);
+    ST_CUDA(cudaMemcpyAsync(depth->host, ctx->d_buckets, nbytes, cudaMemcpyDeviceToHost, s));
+    d2h += nbytes;
   }
   ST_CUDA(cudaStreamSynchronize(s));
   if (dev_rgba) *dev_rgba = reinterpret_cast<const float*>(ctx->d_fb);
@@ -1081,6 +1102,7 @@ void st_context_destroy(st_context* ctx) {
   cudaFree(ctx->d_lut);
   cudaFree(ctx->d_star_lut);
   cudaFree(ctx->d_stat);
+  cudaFree(ctx->d_buckets);
   cudaFree(ctx->d_box);
   cudaFree(ctx->d_fan);
   cudaFree(ctx->d_fine);
@@ -1128,6 +1150,14 @@ int st_render_motion(st_context* ctx, const st_camera* cam, const st_camera* pos
   if (p->surrogate) return ST_EUNSUPPORTED;
   const Motion mo{poses, nposes, per_pixel_shutter ? 1 : 0};
   return do_render(ctx, cam, st, p, out_rgb, diag, nullptr, stats, &mo);
+}
+
+int st_render_depth(st_context* ctx, const st_camera* cam, const st_spacetime* st, const st_render_params* p,
+                    int nbuckets, float* out_buckets, st_stats* stats) {
+  if (!out_buckets) return ST_EINVAL;
+  if (nbuckets < 3 || nbuckets > 64) return ST_EINVAL;
+  const Depth d{nbuckets, out_buckets};
+  return do_render(ctx, cam, st, p, nullptr, nullptr, nullptr, stats, nullptr, &d);
 }
 
 int st_sky_fan(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,

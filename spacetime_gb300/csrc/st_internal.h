@@ -74,6 +74,12 @@ struct TraceParams {
   const float4* star_lut;    // [star_lut_size] RGB_, the stars' own white point
   int star_lut_size, star_seed;
   double star_lut_tmin, star_lut_tmax;
+  // depth buckets (render_depth_mtl, src/metal.jl:1170-1175, 1425-1426,
+  // 1489-1497, 1556-1563, 1687-1690): nb > 0 routes emission into
+  // buckets[pixel][3 nb] by path length, log-spaced over [1.5, 120] M, and the
+  // escaped sky into the last bucket
+  int nb;
+  float* buckets;
   // adaptive refinement (src/metal.jl:1640-1700, 2104-2240): per-pixel
   // (sum w L, sum w L^2, sum w graze, -) over the base passes, or null; and
   // the dispatch box of a refinement pass (box_cols = 0: the whole frame)

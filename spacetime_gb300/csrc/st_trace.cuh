@@ -324,7 +324,31 @@ struct RayState {
   R k1c[6];
   bool k1_valid;
   R r_layer_prev;  // layer pass: previous radius beyond the gate
+  R ell;           // depth buckets: path length travelled
 };
+
+// Depth bucket of path length ell (1-based as in the reference): the first
+// below 1.5 M, log-spaced to 120 M, the last (nb) kept for the sky.
+template <typename R>
+__device__ __forceinline__ int depth_bucket(R ell, int nb) {
+  if (ell <= R(1.5)) return 1;
+  const R bscale = nb > 2 ? R(nb - 2) * R(0.22820f) : R(1);
+  const int b = (int)((log_(ell) - R(0.405465f)) * bscale) + 1;
+  return min(max(b, 1), nb - 1);
+}
+
+// Depth-bucket mode keeps nothing in acc between steps: the emission of one
+// step (disc crossing or gas samples) is moved into the bucket of the path
+// length reached at that step, src/metal.jl:1489-1497, 1556-1563.
+template <typename R>
+__device__ __forceinline__ void flush_bucket(const TraceParams& p, int pix, R ell, R* acc) {
+  if (acc[0] == R(0) && acc[1] == R(0) && acc[2] == R(0)) return;
+  float* b = p.buckets + (size_t)pix * 3 * p.nb + 3 * (depth_bucket(ell, p.nb) - 1);
+  b[0] += p.weight * (float)acc[0];
+  b[1] += p.weight * (float)acc[1];
+  b[2] += p.weight * (float)acc[2];
+  acc[0] = R(0); acc[1] = R(0); acc[2] = R(0);
+}
 
 // Internal ray flag of the layer pass: the fan proves the ray misses the gate.
 constexpr int ST_RAY_LAYER_CULLED = 1 << 20;
@@ -565,6 +589,7 @@ __device__ void init_ray_dir(const TraceParams& p, const CamView& cam, int i1, i
   st.r_cross = -1.f;
   st.g_cross = 0.f;
   st.r_layer_prev = R(-1);
+  st.ell = R(0);
   if constexpr (!KERR && SEM == ST_SEM_DRAFT) {
     // Layer pass: a ray launched beyond the gate whose fan entry (by its
     // local angle to the radial axis) escapes with periapsis beyond the gate
@@ -998,8 +1023,11 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
 
   if constexpr (SEM == ST_SEM_DRAFT) {
     const R vlen = max_(sqrt_(k1[0] * k1[0] + k1[1] * k1[1] + k1[2] * k1[2]), R(1e-20));
+    if (p.nb > 0) st.ell += h * vlen;
     if constexpr (VOL) {
-      if (march_gas(p, yp, y, r2, h, vlen, st)) return true;
+      const bool opaque = march_gas(p, yp, y, r2, h, vlen, st);
+      if (p.nb > 0) flush_bucket(p, st.pix, st.ell, st.acc);
+      if (opaque) return true;
     } else {
       if (p.disc_on && st.alpha > R(0.001) && yp[2] * y[2] < R(0)) {
         const R cfz = yp[2] / (yp[2] - y[2]);
@@ -1020,6 +1048,7 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
           st.g_cross = (float)g;
           st.flags |= ST_RAY_CROSSED;
         }
+        if (p.nb > 0) flush_bucket(p, st.pix, st.ell, st.acc);
       }
     }
     if (p.exit_landing) {
@@ -1175,6 +1204,12 @@ __device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typena
     rgb[0] += st.alpha * sky[0];
     rgb[1] += st.alpha * sky[1];
     rgb[2] += st.alpha * sky[2];
+    if (p.nb > 0) {  // the background lives in the last (infinity) bucket
+      float* b = p.buckets + (size_t)out_index * 3 * p.nb + 3 * (p.nb - 1);
+      b[0] += p.weight * (float)(st.alpha * sky[0]);
+      b[1] += p.weight * (float)(st.alpha * sky[1]);
+      b[2] += p.weight * (float)(st.alpha * sky[2]);
+    }
   } else {
     st.flags |= ST_RAY_BLACK;
   }
@@ -1189,12 +1224,14 @@ __device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typena
     if (st.flags & ST_RAY_GRAZE) s4.z += w;
     p.stat[out_index] = s4;
   }
-  float4 o = make_float4(w * (float)rgb[0], w * (float)rgb[1], w * (float)rgb[2], (float)st.alpha);
-  if (!p.first_pass) {
-    const float4 prev = p.out[out_index];
-    o.x += prev.x; o.y += prev.y; o.z += prev.z;
+  if (!p.nb) {  // bucketed emission was written during the march
+    float4 o = make_float4(w * (float)rgb[0], w * (float)rgb[1], w * (float)rgb[2], (float)st.alpha);
+    if (!p.first_pass) {
+      const float4 prev = p.out[out_index];
+      o.x += prev.x; o.y += prev.y; o.z += prev.z;
+    }
+    p.out[out_index] = o;
   }
-  p.out[out_index] = o;
   if (p.diag) {
     st_ray_diag d;
     d.dir[0] = (double)d0; d.dir[1] = (double)d1; d.dir[2] = (double)d2;
