@@ -280,6 +280,48 @@ def layered_variant(ctx_cls, device: int, flush, reps: int = 3) -> dict:
     return out
 
 
+def fluid_variant(ctx_cls, device: int, steps: int = 200) -> dict:
+    """The live fluid disc (DiscFluidSim / step_sim!, dt 0.08, jacobi 8) on two
+    grids: config 1's gas grid (256 x 64 x 32, ISCO to 25 M) and the
+    reference's default DiscVolume grid (192 x 256 x 48, 3-20 M).  Device time
+    per step through the CUDA graph and as plain stream launches (4 kernels a
+    step), and the oracle's single-thread CPU time per step."""
+    import time
+
+    import numpy as np
+    from oracle import oracle as O
+    from spacetime_gb300 import workloads
+    from spacetime_gb300.api import AccretionDisc, Blackbody, DiscFluidSim
+    from spacetime_gb300.scene import make_volume
+    out = {}
+    for name, vol, disc in (
+            ("config1_grid_256x64x32", workloads.config1().vol, AccretionDisc(2.32, 25.0, Blackbody(), 0.0)),
+            ("default_grid_192x256x48", make_volume(inner=3.0, outer=20.0, nr=192, nphi=256, nz=48, seed=3),
+             AccretionDisc(3.0, 20.0, Blackbody(wb_temperature=10000.0), 0.8))):
+        ctx = ctx_cls(workloads.sky(256, 128), disc=disc, volume=vol, device=device)
+        sim = DiscFluidSim(ctx, vol, disc)
+        sim.step(dt=0.08, nsteps=20, graph=True, timed=True)          # warm-up (and graph build)
+        ms_graph = sim.step(dt=0.08, nsteps=steps, graph=True, timed=True) / steps
+        sim.step(dt=0.08, nsteps=20, graph=False, timed=True)
+        ms_plain = sim.step(dt=0.08, nsteps=steps, graph=False, timed=True) / steps
+        nr, nphi, nz = vol.shape
+        orc = O.FluidSim(vol, disc.inner_radius, disc.outer_radius, falloff=disc.density_falloff)
+        t0 = time.perf_counter()
+        orc.step(dt=0.08, jacobi=8, nsteps=5, volume=True)
+        cpu_ms = (time.perf_counter() - t0) * 1e3 / 5
+        # algorithmic bytes: every field read and written once per kernel, the texture written once
+        n = nr * nphi
+        algo = (19 * n + n * nz) * 4
+        out[name] = {"us_per_step_graph": ms_graph * 1e3, "us_per_step_stream": ms_plain * 1e3,
+                     "launches_per_step": 4, "algorithmic_bytes_per_step": algo,
+                     "achieved_GBs_graph": algo / (ms_graph * 1e-3) / 1e9,
+                     "oracle_cpu_ms_per_step_1_thread": cpu_ms,
+                     "speedup_vs_oracle": cpu_ms / ms_graph}
+        sim.close()
+        ctx.close()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -397,10 +439,18 @@ def main(argv=None):
                     help="trained surrogate parameters (.npy; 'shipped' = spacetime_gb300/data/surrogate_kerr.npy) "
                          "for config1_thin / config1_nogas")
     ap.add_argument("--sigma", type=float, default=4e-4, help="surrogate gate: max predicted std-dev (rad)")
+    ap.add_argument("--fluid-only", action="store_true",
+                    help="print only the fluid disc timing (DiscFluidSim / step_sim!) as one JSON line")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.fluid_only:
+        import torch
+        from spacetime_gb300.api import Context
+        torch.cuda.set_device(0)
+        print(json.dumps({"fluid_disc": fluid_variant(Context, 0, steps=args.steps)}), flush=True)
+        return 0
     if args.workload in ("config2", "config4"):
         return run_track(args)
 
@@ -522,6 +572,10 @@ def main(argv=None):
             variants["layered_schwarzschild"] = layered_variant(Context, local, flush)
         except Exception as e:  # report, do not fail the bench
             variants["layered_schwarzschild"] = {"failed": str(e)}
+        try:
+            variants["fluid_disc"] = fluid_variant(Context, local)
+        except Exception as e:  # report, do not fail the bench
+            variants["fluid_disc"] = {"failed": str(e)}
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         try:

@@ -36,6 +36,8 @@
  *   st_render_depth        render_depth_mtl, src/metal.jl:1935-1990 (trace_kernel_mtl!
  *                          with NB > 0: :1170-1175, 1425-1426, 1489-1497, 1556-1563,
  *                          1687-1690)
+ *   st_fluid_create / st_fluid_step  DiscFluidSim(vol, disc; M, forcing, drag, relax) and
+ *                          step_sim!(sim, ctx; dt, jacobi), src/disc_sim.jl:38-91, 280-320
  *
  * Output layout: linear HDR RGB float32 in the reference's column-major
  * (3, width, height) order, i.e. out[3*(i + width*j) + c] for 0-based pixel
@@ -300,6 +302,41 @@ int st_render_motion(st_context* ctx, const st_camera* cam, const st_camera* pos
  * DRAFT only, no surrogate, no refinement (ST_EUNSUPPORTED). */
 int st_render_depth(st_context* ctx, const st_camera* cam, const st_spacetime* st, const st_render_params* p,
                     int nbuckets, float* out_buckets, st_stats* stats);
+
+/* ---- live fluid disc (DiscFluidSim, src/disc_sim.jl) -------------------------
+ * A 2-D stable-fluids solver (semi-Lagrangian advection on the Keplerian
+ * shear, curl-noise forcing, Jacobi pressure projection, MacCormack density
+ * advection relaxed toward the disc profile) on the context volume's own
+ * (log s, phi) grid; every step extrudes the surface density through the
+ * vertical envelope exp(-z^2 / 2 H^2), H = scale_height s, into the
+ * context's density texture, so the next render traces the new gas.  The
+ * solver starts from the texture's midplane slice (k = (nz + 1) / 2,
+ * 1-based) normalised to a peak of 1.  Units: M-time; velocities in grid
+ * cells per M-time.  The context must hold a volume (ST_ESTATE otherwise) and
+ * must outlive the solver; replacing its volume with another grid makes
+ * st_fluid_step return ST_ESTATE. */
+typedef struct st_fluid st_fluid;
+typedef struct {
+  double M;                  /* default 1 */
+  double forcing;            /* eddy forcing amplitude, default 6 */
+  double drag;               /* velocity damping per M-time, default 0.15 */
+  double relax;              /* density relaxation toward the profile per M-time, default 0.05 */
+  double scale_height;       /* the volume's H(s) = scale_height s, default 0.08 */
+} st_fluid_params;
+void st_fluid_params_default(st_fluid_params* p);
+/* disc: the AccretionDisc whose radial profile (inner, outer, falloff) the
+ * density relaxes toward. */
+int st_fluid_create(st_fluid** out, st_context* ctx, const st_disc* disc, const st_fluid_params* p);
+/* nsteps steps of dt (step_sim! defaults: dt 0.05, jacobi 8, i.e.
+ * 2 ceil(jacobi / 2) Jacobi sweeps), queued on the context's stream.
+ * use_graph = 1 replays a CUDA graph of the step's launches; ms (may be
+ * NULL) receives the device time of the steps (the call then waits for them). */
+int st_fluid_step(st_fluid* f, double dt, int jacobi, int nsteps, int use_graph, float* ms);
+/* Host copies of the solver state ((nr, nphi) column-major; any may be NULL):
+ * the velocity, the surface density, the context's density texture
+ * ((nr, nphi, nz)) and the simulation clock. */
+int st_fluid_state(st_fluid* f, float* vu, float* vv, float* dens, float* volume, double* t);
+void st_fluid_destroy(st_fluid* f);
 
 /* Raw HDR frame files, save_raw / load_raw (src/rawio.jl:18-42): a linear,
  * unclamped 32-bit float RGB TIFF in display orientation (the reference's

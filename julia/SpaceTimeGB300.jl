@@ -4,6 +4,8 @@
 #   render(cam, bh, sky; disc, width, height, samples, relativistic)   (src/raytrace.jl:339)
 #   GB300Context(sky, w, h; disc, volume)                             (MetalPreviewContext, src/metal.jl:129)
 #   render_draft_mtl(ctx, cam, st; width, height, samples, dt, ...)   (src/metal.jl:2040)
+#   render_depth_mtl(ctx, cam, st; nbuckets, ...)                     (src/metal.jl:1945)
+#   DiscFluidSim(vol, disc; ...), step_sim!(sim, ctx; dt, jacobi)     (src/disc_sim.jl:45, 287)
 # Images come back as Matrix{RGBf}(width, height), the reference's layout.
 # This file is not exercised in this repository's CI (no Julia toolchain);
 # the same ABI is tested through Python ctypes (tests/test_abi.py and the GPU tests).
@@ -185,6 +187,56 @@ function render_draft_gb300(ctx::GB300Context, cam::Camera, bh; width::Int=1920,
                 ctx.handle, Ref(c), poses, length(poses), per_pixel_shutter, st, p, out, C_NULL, C_NULL),
           "st_render_motion")
     [RGBf(out[1, i, j], out[2, i, j], out[3, i, j]) for i in 1:width, j in 1:height]
+end
+
+"""`render_depth_mtl(ctx, cam, st; width, height, samples, dt, nbuckets, fisheye_deg, relativistic)`
+(src/metal.jl:1935-1990): the (3*nbuckets, width, height) Float32 array of emission binned by path
+length, the last bucket the sky."""
+function render_depth_gb300(ctx::GB300Context, cam::Camera, bh; width::Int=1920, height::Int=1080,
+                            samples::Int=2, dt::Real=0.02, nbuckets::Int=10, fisheye_deg::Real=0.0,
+                            relativistic::Bool=false, precision::Int=ST_PREC_FP32)
+    nbuckets >= 3 || throw(ArgumentError("nbuckets must be ≥ 3"))
+    p = default_params(ST_SEM_DRAFT)
+    p.width = width; p.height = height; p.samples = samples; p.dt = dt
+    p.relativistic = relativistic; p.precision = precision; p.pixel_jitter = false
+    c = st_camera(cam; fisheye_deg)
+    out = Array{Float32,3}(undef, 3 * nbuckets, width, height)
+    st = Ref(StSpacetime(bh.M, spin(bh)))
+    check(ccall((:st_render_depth, libst), Cint,
+                (Ptr{Cvoid}, Ref{StCamera}, Ref{StSpacetime}, Ref{StRenderParams}, Cint, Ptr{Float32}, Ptr{Cvoid}),
+                ctx.handle, Ref(c), st, p, nbuckets, out, C_NULL), "st_render_depth")
+    out
+end
+
+struct StFluidParams
+    M::Float64; forcing::Float64; drag::Float64; relax::Float64; scale_height::Float64
+end
+
+mutable struct GB300FluidSim
+    handle::Ptr{Cvoid}
+    ctx::GB300Context
+end
+
+"""`DiscFluidSim(vol, disc; M, forcing, drag, relax)` (src/disc_sim.jl:38-91) on the context's gas grid;
+`vol` is the DiscVolume the context was built with."""
+function GB300FluidSim(ctx::GB300Context, vol::DiscVolume, disc::AccretionDisc; M::Real=1.0,
+                       forcing::Real=6.0, drag::Real=0.15, relax::Real=0.05)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    fp = Ref(StFluidParams(M, forcing, drag, relax, vol.scale_height))
+    check(ccall((:st_fluid_create, libst), Cint, (Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ref{StDisc}, Ref{StFluidParams}),
+                h, ctx.handle, Ref(st_disc(disc, ST_EMIT_KS_EXACT)), fp), "st_fluid_create")
+    sim = GB300FluidSim(h[], ctx)
+    finalizer(s -> ccall((:st_fluid_destroy, libst), Cvoid, (Ptr{Cvoid},), s.handle), sim)
+    sim
+end
+
+"""`step_sim!(sim, ctx; dt, jacobi)` (src/disc_sim.jl:287-320): one step, queued on the context's
+stream, written into its gas texture."""
+function step_sim_gb300!(sim::GB300FluidSim, ctx::GB300Context; dt::Real=0.05, jacobi::Int=8)
+    ctx === sim.ctx || throw(ArgumentError("the solver writes into the context it was built on"))
+    check(ccall((:st_fluid_step, libst), Cint, (Ptr{Cvoid}, Cdouble, Cint, Cint, Cint, Ptr{Cfloat}),
+                sim.handle, dt, jacobi, 1, 1, C_NULL), "st_fluid_step")
+    nothing
 end
 
 end # module

@@ -60,6 +60,12 @@ RAY_DTYPE = np.dtype([
     ("pad", "<i4"),
 ])
 
+class OrcFluid(C.Structure):
+    _fields_ = [("nr", C.c_int), ("nphi", C.c_int), ("nz", C.c_int),
+                ("vu", FP), ("vv", FP), ("dens", FP), ("base", FP), ("env", FP), ("shear", FP),
+                ("t", C.c_float), ("forcing", C.c_double), ("drag", C.c_double), ("relax", C.c_double)]
+
+
 _lib = None
 
 
@@ -80,6 +86,11 @@ def lib() -> C.CDLL:
         dp = P(C.c_double)
         L.orc_render.argtypes = [P(OrcScene), FP, C.c_void_p, C.c_int]
         L.orc_render.restype = C.c_int
+        L.orc_fluid_init.argtypes = [P(OrcFluid), FP, C.c_float, C.c_float, C.c_float, C.c_double, C.c_double,
+                                     C.c_double, C.c_double, C.c_double]
+        L.orc_fluid_init.restype = C.c_int
+        L.orc_fluid_step.argtypes = [P(OrcFluid), FP, C.c_double, C.c_int, C.c_int]
+        L.orc_fluid_step.restype = C.c_int
         L.orc_render_depth.argtypes = [P(OrcScene), C.c_int, FP, C.c_int]
         L.orc_render_depth.restype = C.c_int
         L.orc_trace_dirs.argtypes = [P(OrcScene), C.c_int, P(C.c_double), C.c_void_p, C.c_int]
@@ -367,3 +378,44 @@ def scene_for(w, sky, integrator, width=None, height=None, rect=None, **kw) -> S
                 volume=w.vol, exit_landing=w.params.get("exit_landing"), rect=rect, nmax=w.params.get("nmax", 0))
     args.update(kw)
     return Scene(**args)
+
+
+# ---- live fluid disc ---------------------------------------------------------
+
+class FluidSim:
+    """DiscFluidSim twin (orc_fluid_*): fields are (nphi, nr) float32 arrays,
+    the C-order view of the reference's (nr, nphi) column-major matrices."""
+
+    def __init__(self, volume, inner, outer, falloff=0.0, M=1.0, forcing=6.0, drag=0.15, relax=0.05):
+        nr, nphi, nz = volume.shape
+        self.shape = (nr, nphi, nz)
+        self.vu = np.zeros((nphi, nr), np.float32)
+        self.vv = np.zeros((nphi, nr), np.float32)
+        self.dens = np.zeros((nphi, nr), np.float32)
+        self.base = np.zeros((nphi, nr), np.float32)
+        self.env = np.zeros((nz, nr), np.float32)
+        self.shear = np.zeros(nr, np.float32)
+        f = OrcFluid()
+        f.nr, f.nphi, f.nz = nr, nphi, nz
+        for k in ("vu", "vv", "dens", "base", "env", "shear"):
+            setattr(f, k, getattr(self, k).ctypes.data_as(FP))
+        f.forcing, f.drag, f.relax = forcing, drag, relax
+        self.f = f
+        dens = np.ascontiguousarray(volume.density, dtype=np.float32)
+        rc = lib().orc_fluid_init(C.byref(f), dens.ctypes.data_as(FP), volume.log_s_in, volume.log_s_out,
+                                  volume.z_max, volume.scale_height, M, inner, outer, falloff)
+        if rc != 0:
+            raise RuntimeError(f"orc_fluid_init failed ({rc})")
+
+    @property
+    def t(self) -> float:
+        return float(self.f.t)
+
+    def step(self, dt=0.05, jacobi=8, nsteps=1, volume=False):
+        """nsteps steps; with volume=True also the extruded (nz, nphi, nr) texture."""
+        nr, nphi, nz = self.shape
+        vol = np.zeros((nz, nphi, nr), np.float32) if volume else None
+        rc = lib().orc_fluid_step(C.byref(self.f), vol.ctypes.data_as(FP) if volume else None, dt, jacobi, nsteps)
+        if rc != 0:
+            raise RuntimeError(f"orc_fluid_step failed ({rc})")
+        return vol

@@ -140,6 +140,25 @@ int orc_render_depth(const orc_scene* sc, int nb, float* out, int nthreads);
  * twin of the layered engine's deflection fan.  Pixel fields are unused. */
 int orc_trace_dirs(const orc_scene* sc, int n, const double* dirs, orc_ray* rays, int nthreads);
 
+/* --- live fluid disc (DiscFluidSim / step_sim!, src/disc_sim.jl) ---------
+ * All arrays are caller-owned, (nr, nphi) column-major unless noted. */
+typedef struct {
+  int nr, nphi, nz;
+  float* vu; float* vv;      /* velocity, grid cells per M-time */
+  float* dens;               /* surface density */
+  float* base;               /* relaxation target (radial profile) */
+  float* env;                /* (nr, nz) vertical envelope */
+  float* shear;              /* [nr] Keplerian shear, phi cells per M-time */
+  float t;                   /* simulation clock */
+  double forcing, drag, relax;
+} orc_fluid;
+/* DiscFluidSim construction from a (nr, nphi, nz) density texture. */
+int orc_fluid_init(orc_fluid* f, const float* vol_density, float log_s_in, float log_s_out, float z_max,
+                   double scale_height, double M, double inner, double outer, double falloff);
+/* nsteps step_sim! steps; vol_out (may be NULL) receives the extruded
+ * (nr, nphi, nz) texture of the final state. */
+int orc_fluid_step(orc_fluid* f, float* vol_out, double dt, int jacobi, int nsteps);
+
 /* --- unit pieces, for known-answer tests --- */
 void orc_rhs(int kerr, const double s[6], double pt, double M, double a, double d[6]);
 void orc_camera_tetrad(const double pos[3], const double fwd[3], const double right[3],

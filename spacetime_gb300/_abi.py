@@ -53,6 +53,11 @@ class StDisc(C.Structure):
     ]
 
 
+class StFluidParams(C.Structure):
+    _fields_ = [("M", C.c_double), ("forcing", C.c_double), ("drag", C.c_double), ("relax", C.c_double),
+                ("scale_height", C.c_double)]
+
+
 class StVolume(C.Structure):
     _fields_ = [
         ("density", C.POINTER(C.c_float)), ("nr", C.c_int), ("nphi", C.c_int), ("nz", C.c_int),
@@ -124,7 +129,8 @@ EXPORTS = [
     "st_surrogate_train", "st_render_frames_noalloc", "st_context_set_surrogate",
     "st_starfield_default", "st_context_set_starfield", "st_render_motion",
     "st_save_raw", "st_load_raw_size", "st_load_raw", "st_sky_fan", "st_render_layered",
-    "st_render_depth",
+    "st_render_depth", "st_fluid_params_default", "st_fluid_create", "st_fluid_step", "st_fluid_state",
+    "st_fluid_destroy",
 ]
 ST_FAN_N, ST_FAN_FINE = 4096, 1024
 
@@ -207,6 +213,17 @@ def load(path: str | None = None) -> C.CDLL:
     lib.st_render_depth.argtypes = [C.c_void_p, P(StCamera), P(StSpacetime), P(StRenderParams), C.c_int,
                                     P(C.c_float), P(StStats)]
     lib.st_render_depth.restype = C.c_int
+    lib.st_fluid_params_default.argtypes = [P(StFluidParams)]
+    lib.st_fluid_params_default.restype = None
+    lib.st_fluid_create.argtypes = [P(C.c_void_p), C.c_void_p, P(StDisc), P(StFluidParams)]
+    lib.st_fluid_create.restype = C.c_int
+    lib.st_fluid_step.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, C.c_int, P(C.c_float)]
+    lib.st_fluid_step.restype = C.c_int
+    lib.st_fluid_state.argtypes = [C.c_void_p, P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_float),
+                                   P(C.c_double)]
+    lib.st_fluid_state.restype = C.c_int
+    lib.st_fluid_destroy.argtypes = [C.c_void_p]
+    lib.st_fluid_destroy.restype = None
     for name in ("st_context_create", "st_context_set_disc", "st_context_set_volume", "st_render",
                  "st_render_diag", "st_render_device", "st_render_frames", "st_camera_tetrad",
                  "st_surrogate_create", "st_surrogate_num_params", "st_surrogate_get_params",

@@ -7,6 +7,7 @@
     Context(sky; disc, volume)                   MetalPreviewContext, src/metal.jl:129-182
     render_draft(ctx, cam, bh; ...)              render_draft_mtl, src/metal.jl:2040-2242
     render_depth(ctx, cam, bh; nbuckets, ...)    render_depth_mtl, src/metal.jl:1935-1990
+    DiscFluidSim(ctx, vol, disc), step_sim       src/disc_sim.jl:38-91, 280-320
 
 Images come back as float32 arrays of shape (height, width, 3): element
 [j, i] is pixel (i, j) of the reference's Matrix{RGBf}(width, height), i.e.
@@ -27,6 +28,7 @@ from .scene import Camera, Volume, lens_fov
 __all__ = [
     "Schwarzschild", "Kerr", "Blackbody", "AccretionDisc", "Lens", "Camera", "Context",
     "render", "render_draft", "render_depth", "render_frames", "camera_tetrad", "RenderResult",
+    "DiscFluidSim", "step_sim",
 ]
 
 
@@ -402,6 +404,77 @@ def render_depth(ctx: Context, cam: Camera, bh, *, width: int = 1920, height: in
     p = ctx.params(_abi.ST_SEM_DRAFT, width=width, height=height, samples=samples, dt=dt,
                    relativistic=int(relativistic), precision=_prec(precision), seed=seed, **kw)
     return ctx.render_depth_raw(cam2, bh, p, nbuckets).image
+
+
+class DiscFluidSim:
+    """DiscFluidSim(ctx, vol, disc; M, forcing, drag, relax) (src/disc_sim.jl:38-91):
+    the live fluid disc on the context volume's grid.  step() is step_sim!
+    (src/disc_sim.jl:280-320): it advances the solver and writes the extruded
+    density into the context's gas texture, so the next render sees it.  vol
+    is the Volume the context holds (for its scale height).  Fields come back
+    as (nphi, nr) float32 arrays (the reference's (nr, nphi) column-major)."""
+
+    def __init__(self, ctx: Context, vol: Volume, disc: AccretionDisc, *, M: float = 1.0, forcing: float = 6.0,
+                 drag: float = 0.15, relax: float = 0.05):
+        if ctx.volume is None:
+            raise ValueError("the context holds no volume")
+        self._lib = ctx._lib
+        self.ctx = ctx                     # the solver writes into this context's texture
+        self.shape = vol.shape
+        fp = _abi.StFluidParams(M, forcing, drag, relax, vol.scale_height)
+        bb = disc.blackbody
+        d = _abi.StDisc(disc.inner_radius, disc.outer_radius, disc.density_falloff, bb.wb_temperature,
+                        bb.table_min, bb.table_max, bb.table_size, _abi.ST_EMIT_KS_EXACT)
+        h = C.c_void_p()
+        _abi.check(self._lib.st_fluid_create(C.byref(h), ctx._h, C.byref(d), C.byref(fp)), "st_fluid_create")
+        self._h = h
+
+    def step(self, dt: float = 0.05, jacobi: int = 8, nsteps: int = 1, graph: bool = True,
+             timed: bool = False) -> float | None:
+        """nsteps solver steps; timed=True waits and returns their device ms."""
+        ms = C.c_float(0.0)
+        _abi.check(self._lib.st_fluid_step(self._h, float(dt), int(jacobi), int(nsteps), int(graph),
+                                           C.byref(ms) if timed else None), "st_fluid_step")
+        return float(ms.value) if timed else None
+
+    def state(self, volume: bool = False) -> dict:
+        nr, nphi, nz = self.shape
+        out = {k: np.empty((nphi, nr), np.float32) for k in ("vu", "vv", "dens")}
+        vol = np.empty((nz, nphi, nr), np.float32) if volume else None
+        t = C.c_double(0.0)
+        fp = C.POINTER(C.c_float)
+        _abi.check(self._lib.st_fluid_state(self._h, out["vu"].ctypes.data_as(fp), out["vv"].ctypes.data_as(fp),
+                                            out["dens"].ctypes.data_as(fp),
+                                            vol.ctypes.data_as(fp) if volume else None, C.byref(t)),
+                   "st_fluid_state")
+        out["t"] = t.value
+        if volume:
+            out["volume"] = vol
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.st_fluid_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def step_sim(sim: DiscFluidSim, ctx: Context | None = None, *, dt: float = 0.05, jacobi: int = 8) -> None:
+    """step_sim!(sim, ctx; dt, jacobi) (src/disc_sim.jl:287-320)."""
+    if ctx is not None and ctx is not sim.ctx:
+        raise ValueError("the solver writes into the context it was built on")
+    sim.step(dt=dt, jacobi=jacobi)
 
 
 def render_frames(ctx: Context, cams, bh, *, width: int, height: int, dt: float = 0.02, precision="fp32g",

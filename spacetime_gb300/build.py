@@ -24,10 +24,12 @@ MINB_FP32G = os.environ.get("ST_MINB_FP32G", "4")
 UNIT_FLAGS = {
     "st_trace_fp32.cu": (["--use_fast_math"] if FAST else []) + [f"-DST_MINB={MINB_FP32}"],
     "st_trace_fp32_guarded.cu": (["--use_fast_math"] if FAST else []) + [f"-DST_MINB={MINB_FP32G}"],
+    # the fluid solver rounds every float operation as written (no contraction)
+    "st_fluid.cu": ["-fmad=false"],
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["st_trace_fp64.cu", "st_trace_fp32.cu", "st_trace_fp32_guarded.cu", "st_api.cu", "st_surrogate.cu", "st_noalloc.cu",
-           "st_layered.cu", "st_rawio.cpp"]
+           "st_layered.cu", "st_rawio.cpp", "st_fluid.cu"]
 
 
 def nvcc() -> str:

@@ -653,6 +653,8 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
   if (depth) {
     // emission binned by path length replaces the plain frame
     if (rp->semantics != ST_SEM_DRAFT || rp->surrogate || refine > 1) return ST_EUNSUPPORTED;
+    if (p.order != 4) return ST_EUNSUPPORTED;  // render_depth_mtl integrates with RK4
+    v.sched = ST_SCHED_PIXEL;                  // the bucket kernels are pixel-scheduled
     if ((rc = ensure(&ctx->d_buckets, &ctx->buckets_cap, 3 * (size_t)depth->nb * npix)) != ST_OK) return rc;
     ST_CUDA(cudaMemsetAsync(ctx->d_buckets, 0, 3 * (size_t)depth->nb * npix * sizeof(float), s));
     p.nb = depth->nb;
@@ -906,6 +908,19 @@ static int upload_lut(st_context* ctx, double wb, double tmin, double tmax, int 
   return ST_OK;
 }
 
+
+namespace st {
+int context_volume(st_context* ctx, CtxVolume* out) {
+  if (!ctx || !out) return ST_EINVAL;
+  out->device = ctx->device;
+  out->stream = ctx->stream;
+  out->d_vol = ctx->d_vol;
+  out->meta = ctx->vol;
+  out->on = ctx->vol_on && ctx->d_vol != nullptr;
+  return ST_OK;
+}
+
+}  // namespace st
 
 extern "C" {
 

@@ -9,6 +9,17 @@
 
 namespace st {
 
+// The context's gas volume as another unit sees it (st_api.cu owns the
+// context; the fluid solver writes the density texture in place).
+struct CtxVolume {
+  int device;
+  cudaStream_t stream;
+  float* d_vol;              // (nr, nphi, nz) column-major
+  st_volume meta;            // grid and bounds; meta.density is null
+  bool on;
+};
+int context_volume(st_context* ctx, CtxVolume* out);
+
 // Counters written by the trace kernels (one slot each, 64-bit).
 enum { CNT_STEPS = 0, CNT_FP64 = 1, CNT_GAS = 2, CNT_RAYS = 3, CNT_SURR = 4, CNT_QUEUE = 5,
        CNT_STATUS = 6, CNT_N = 8 };

@@ -39,7 +39,7 @@ __device__ __forceinline__ void flush_counters(const TraceParams& p, unsigned lo
 
 // One thread per pixel over a 2-D grid of tiles (blockDim.x * blockDim.y a
 // multiple of 32; threads are linearised so a warp covers a compact tile).
-template <int PREC, int KERR, int VOL, int SEM, int ORD = 4>
+template <int PREC, int KERR, int VOL, int SEM, int ORD = 4, int DEPTH = 0>
 __global__ void __launch_bounds__(128, ORD == 4 ? ST_MINB : ST_MINB_ADAPTIVE) trace_pixel_kernel(const __grid_constant__ TraceParams p) {
   using R = typename RealOf<PREC>::T;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -72,9 +72,9 @@ __global__ void __launch_bounds__(128, ORD == 4 ? ST_MINB : ST_MINB_ADAPTIVE) tr
     }
     init_ray<PREC, KERR, SEM>(p, cam, i, j, st);
     st.pix = base + j * p.width + i;
-    while (!step_ray<PREC, KERR, VOL, SEM, ORD>(p, st)) {
+    while (!step_ray<PREC, KERR, VOL, SEM, ORD, DEPTH>(p, st)) {
     }
-    finish_ray<PREC, KERR, SEM>(p, st, st.pix, p.frames ? st.pix : j * p.width + i);
+    finish_ray<PREC, KERR, SEM, DEPTH>(p, st, st.pix, p.frames ? st.pix : j * p.width + i);
     steps = st.steps; f64 = st.fp64_steps; gas = st.gas; rays = 1;
   }
   flush_counters(p, steps, f64, gas, rays);
@@ -164,6 +164,10 @@ cudaError_t launch_variant(const TraceParams& p, int sched, int bx, int by, int 
     if (p.box_cols > 0) grid = dim3((p.box_cols + bx - 1) / bx, (p.box_rows + by - 1) / by);
     if (p.pix_list) grid = dim3((unsigned)(((long long)p.width * p.height + 127) / 128), 1);
     else if (p.frames) grid.z = (unsigned)(p.n_frames > 0 ? p.n_frames : 1);
+    if constexpr (SEM == ST_SEM_DRAFT) {
+      // depth buckets: their own instantiation, so the plain kernels carry none of it
+      if (p.nb > 0) { trace_pixel_kernel<PREC, KERR, VOL, SEM, 4, 1><<<grid, block, 0, s>>>(p); return cudaGetLastError(); }
+    }
     if constexpr (SEM == ST_SEM_DRAFT && PREC != ST_PREC_FP32_GUARDED) {
       if (p.order == 45) { trace_pixel_kernel<PREC, KERR, VOL, SEM, 45><<<grid, block, 0, s>>>(p); return cudaGetLastError(); }
       if (p.order == 46) { trace_pixel_kernel<PREC, KERR, VOL, SEM, 46><<<grid, block, 0, s>>>(p); return cudaGetLastError(); }

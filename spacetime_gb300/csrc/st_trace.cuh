@@ -906,7 +906,7 @@ __device__ __forceinline__ void renorm_fp64(float* y, float* lo, float pt, doubl
 // One integration step for the variant; returns true when the ray is done.
 // Mirrors the step loop of src/metal.jl:1201-1572 (DRAFT) and the callback
 // structure of src/raytrace.jl:339-373 (RENDER).
-template <int PREC, int KERR, int VOL, int SEM, int ORD = 4>
+template <int PREC, int KERR, int VOL, int SEM, int ORD = 4, int DEPTH = 0>
 __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename RealOf<PREC>::T>& st) {
   using R = typename RealOf<PREC>::T;
   const R M = PR(M), a = PR(a);
@@ -1023,10 +1023,10 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
 
   if constexpr (SEM == ST_SEM_DRAFT) {
     const R vlen = max_(sqrt_(k1[0] * k1[0] + k1[1] * k1[1] + k1[2] * k1[2]), R(1e-20));
-    if (p.nb > 0) st.ell += h * vlen;
+    if constexpr (DEPTH) st.ell += h * vlen;
     if constexpr (VOL) {
       const bool opaque = march_gas(p, yp, y, r2, h, vlen, st);
-      if (p.nb > 0) flush_bucket(p, st.pix, st.ell, st.acc);
+      if constexpr (DEPTH) flush_bucket(p, st.pix, st.ell, st.acc);
       if (opaque) return true;
     } else {
       if (p.disc_on && st.alpha > R(0.001) && yp[2] * y[2] < R(0)) {
@@ -1048,7 +1048,7 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
           st.g_cross = (float)g;
           st.flags |= ST_RAY_CROSSED;
         }
-        if (p.nb > 0) flush_bucket(p, st.pix, st.ell, st.acc);
+        if constexpr (DEPTH) flush_bucket(p, st.pix, st.ell, st.acc);
       }
     }
     if (p.exit_landing) {
@@ -1155,7 +1155,7 @@ __device__ __forceinline__ void star_light(const TraceParams& p, R dx, R dy, R d
 }
 
 // Classification, sky and output (src/metal.jl:1629-1704, src/raytrace.jl:267-298).
-template <int PREC, int KERR, int SEM>
+template <int PREC, int KERR, int SEM, int DEPTH = 0>
 __device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typename RealOf<PREC>::T>& st, int out_index,
                                            int diag_index) {
   using R = typename RealOf<PREC>::T;
@@ -1204,7 +1204,7 @@ __device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typena
     rgb[0] += st.alpha * sky[0];
     rgb[1] += st.alpha * sky[1];
     rgb[2] += st.alpha * sky[2];
-    if (p.nb > 0) {  // the background lives in the last (infinity) bucket
+    if constexpr (DEPTH) {  // the background lives in the last (infinity) bucket
       float* b = p.buckets + (size_t)out_index * 3 * p.nb + 3 * (p.nb - 1);
       b[0] += p.weight * (float)(st.alpha * sky[0]);
       b[1] += p.weight * (float)(st.alpha * sky[1]);
@@ -1224,7 +1224,7 @@ __device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typena
     if (st.flags & ST_RAY_GRAZE) s4.z += w;
     p.stat[out_index] = s4;
   }
-  if (!p.nb) {  // bucketed emission was written during the march
+  if constexpr (!DEPTH) {  // bucketed emission was written during the march
     float4 o = make_float4(w * (float)rgb[0], w * (float)rgb[1], w * (float)rgb[2], (float)st.alpha);
     if (!p.first_pass) {
       const float4 prev = p.out[out_index];

@@ -153,5 +153,6 @@ def test_julia_binding_structs_follow_the_c_layout():
     """The Julia module's ccall structs list the C structs' fields in order."""
     src = open(os.path.join(os.path.dirname(__file__), "..", "julia", "SpaceTimeGB300.jl")).read()
     for jname, cstruct in (("StRenderParams", _abi.StRenderParams), ("StStarfield", _abi.StStarfield),
-                           ("StCamera", _abi.StCamera), ("StDisc", _abi.StDisc), ("StVolume", _abi.StVolume)):
+                           ("StCamera", _abi.StCamera), ("StDisc", _abi.StDisc), ("StVolume", _abi.StVolume),
+                           ("StFluidParams", _abi.StFluidParams)):
         assert _julia_fields(src, jname) == [f for f, _ in cstruct._fields_], jname
