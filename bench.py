@@ -234,7 +234,8 @@ def layered_variant(ctx_cls, device: int, flush, reps: int = 3) -> dict:
     (static camera at r = 30 M, Lens(24)) with the kernel's rules and its thin
     disc (3-20 M, exact emitter) at 1920x1080, FP32.  The full per-pixel trace
     against the layered frame (fan-driven sky, disc layer at the display and
-    at half resolution): time per frame with the fans built (first frame at a
+    at half resolution, the latter also with the foveated ring pass at the
+    display resolution for rays of periapsis below 6 M): time per frame with the fans built (first frame at a
     radius) and cached (every later frame at that radius), and the radiance
     difference from the full trace."""
     import numpy as np
@@ -262,14 +263,15 @@ def layered_variant(ctx_cls, device: int, flush, reps: int = 3) -> dict:
     out["full_trace"] = {"ms_per_step": ms_full, "value": 1920 * 1080 / (ms_full * 1e-3) / 1e6,
                          "steps": full.stats["steps"]}
     lum = np.maximum(full.image.astype(np.float64).sum(-1), 1e-6)
-    for name, size in (("layered", None), ("layered_half_res_layer", (960, 540))):
+    for name, size, ring in (("layered", None, 0.0), ("layered_half_res_layer", (960, 540), 0.0),
+                             ("layered_half_res_layer_ring", (960, 540), 6.0)):
         # a radius not yet seen: the fans are built with the frame
         from spacetime_gb300.scene import Camera
         other = Camera.look_at((0.0, -25.0, 3.0), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), w.cam.fov_factor)
-        ctx.render_layered_raw(other, w.bh, p, layer_size=size)
+        ctx.render_layered_raw(other, w.bh, p, layer_size=size, ring_rmin=ring)
         torch.cuda.synchronize()
-        cold = ctx.render_layered_raw(w.cam, w.bh, p, layer_size=size)
-        lay, ms = timed(lambda: ctx.render_layered_raw(w.cam, w.bh, p, layer_size=size))
+        cold = ctx.render_layered_raw(w.cam, w.bh, p, layer_size=size, ring_rmin=ring)
+        lay, ms = timed(lambda: ctx.render_layered_raw(w.cam, w.bh, p, layer_size=size, ring_rmin=ring))
         rel = np.abs(lay.image.astype(np.float64) - full.image).sum(-1) / lum
         out[name] = {"ms_per_step": ms, "value": 1920 * 1080 / (ms * 1e-3) / 1e6,
                      "ms_first_frame_at_radius": cold.stats["kernel_ms"], "steps": lay.stats["steps"],

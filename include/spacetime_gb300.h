@@ -33,6 +33,8 @@
  *                          fan_band_kernel!, src/metal.jl:2416-2517, 2888-2898)
  *   st_render_layered      render_layered_gpu!, src/metal.jl:3040-3147 (layer pass of
  *                          trace_kernel_mtl!, sky_composite_kernel!, :2707-2880)
+ *   st_render_layered_ring the same with its foveated ring pass (ring_out, ring_rmin,
+ *                          ring_box; _ring_screen_box :2522-2666)
  *   st_render_depth        render_depth_mtl, src/metal.jl:1935-1990 (trace_kernel_mtl!
  *                          with NB > 0: :1170-1175, 1425-1426, 1489-1497, 1556-1563,
  *                          1687-1690)
@@ -372,6 +374,19 @@ int st_sky_fan(st_context* ctx, const st_camera* cam, const st_spacetime* st, co
  * direction per pixel (last pass). */
 int st_render_layered(st_context* ctx, const st_camera* cam, const st_spacetime* st, const st_render_params* p,
                       int layer_width, int layer_height, float* out_rgb, st_ray_diag* diag, st_stats* stats);
+/* The layered frame with the foveated ring pass (render_layered_gpu!'s
+ * ring_out / ring_rmin / ring_box, src/metal.jl:3102-3118, 2846-2863): a second
+ * layer of ring_width x ring_height (<= 0: the display) traced only for the
+ * rays whose fan periapsis is below ring_rmin (the wound rays of the photon
+ * ring; the others are transparent), blended over the bulk layer with weight
+ * 1 - smoothstep((r_p - 0.8 ring_rmin) / (0.2 ring_rmin)).  ring_box = 1
+ * dispatches only the screen box that can hold wound rays (a probe grid of
+ * camera rays against the impact-parameter bound 1.06 R / sqrt(1 - 2M/R),
+ * R = ring_rmin); outside it the ring layer is transparent either way.
+ * ring_rmin = 0 is st_render_layered. */
+int st_render_layered_ring(st_context* ctx, const st_camera* cam, const st_spacetime* st, const st_render_params* p,
+                           int layer_width, int layer_height, int ring_width, int ring_height, double ring_rmin,
+                           int ring_box, float* out_rgb, st_ray_diag* diag, st_stats* stats);
 
 /* Render `nframes` camera poses (a camera track) in one persistent launch;
  * out_rgb holds nframes frames back to back. */

@@ -129,7 +129,7 @@ EXPORTS = [
     "st_surrogate_train", "st_render_frames_noalloc", "st_context_set_surrogate",
     "st_starfield_default", "st_context_set_starfield", "st_render_motion",
     "st_save_raw", "st_load_raw_size", "st_load_raw", "st_sky_fan", "st_render_layered",
-    "st_render_depth", "st_fluid_params_default", "st_fluid_create", "st_fluid_step", "st_fluid_state",
+    "st_render_depth", "st_render_layered_ring", "st_fluid_params_default", "st_fluid_create", "st_fluid_step", "st_fluid_state",
     "st_fluid_destroy",
 ]
 ST_FAN_N, ST_FAN_FINE = 4096, 1024
@@ -210,6 +210,10 @@ def load(path: str | None = None) -> C.CDLL:
     lib.st_render_layered.argtypes = [C.c_void_p, P(StCamera), P(StSpacetime), P(StRenderParams), C.c_int, C.c_int,
                                       P(C.c_float), C.c_void_p, P(StStats)]
     lib.st_render_layered.restype = C.c_int
+    lib.st_render_layered_ring.argtypes = [C.c_void_p, P(StCamera), P(StSpacetime), P(StRenderParams), C.c_int,
+                                           C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, P(C.c_float),
+                                           C.c_void_p, P(StStats)]
+    lib.st_render_layered_ring.restype = C.c_int
     lib.st_render_depth.argtypes = [C.c_void_p, P(StCamera), P(StSpacetime), P(StRenderParams), C.c_int,
                                     P(C.c_float), P(StStats)]
     lib.st_render_depth.restype = C.c_int

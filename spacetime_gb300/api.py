@@ -293,18 +293,25 @@ class Context:
         return fan, fine, band
 
     def render_layered_raw(self, cam: Camera, bh, p: _abi.StRenderParams, layer_size=None,
-                           diag: bool = False) -> RenderResult:
+                           diag: bool = False, ring_rmin: float = 0.0, ring_size=None,
+                           ring_box: bool = True) -> RenderResult:
         """The layered engine's frame (render_layered_gpu!): fan-driven sky,
-        disc / gas layer at layer_size = (width, height) (default: the display)."""
+        disc / gas layer at layer_size = (width, height) (default: the display);
+        ring_rmin > 0 adds the foveated ring pass at ring_size (default: the
+        display) for rays whose fan periapsis is below ring_rmin."""
         lw, lh = layer_size if layer_size is not None else (0, 0)
         img = np.empty((p.height, p.width, 3), dtype=np.float32)
         d = np.empty(p.height * p.width, dtype=_abi.DIAG_DTYPE) if diag else None
         stats = _abi.StStats()
-        _abi.check(self._lib.st_render_layered(self._h, C.byref(_st_camera(cam)), C.byref(_st_spacetime(bh)),
-                                               C.byref(p), int(lw), int(lh),
-                                               img.ctypes.data_as(C.POINTER(C.c_float)),
-                                               C.c_void_p(d.ctypes.data) if diag else None, C.byref(stats)),
-                   "st_render_layered")
+        args = (self._h, C.byref(_st_camera(cam)), C.byref(_st_spacetime(bh)), C.byref(p), int(lw), int(lh))
+        tail = (img.ctypes.data_as(C.POINTER(C.c_float)), C.c_void_p(d.ctypes.data) if diag else None,
+                C.byref(stats))
+        if ring_rmin > 0:
+            rw, rh = ring_size if ring_size is not None else (0, 0)
+            _abi.check(self._lib.st_render_layered_ring(*args, int(rw), int(rh), float(ring_rmin), int(ring_box),
+                                                        *tail), "st_render_layered_ring")
+        else:
+            _abi.check(self._lib.st_render_layered(*args, *tail), "st_render_layered")
         return RenderResult(img, stats.as_dict(), d.reshape(p.height, p.width) if diag else None)
 
     def render_depth_raw(self, cam: Camera, bh, p: _abi.StRenderParams, nbuckets: int = 10) -> RenderResult:

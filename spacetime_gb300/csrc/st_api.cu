@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -320,6 +321,8 @@ struct st_context {
   float* d_band = nullptr;
   float4* d_layer = nullptr;
   size_t layer_cap = 0;
+  float4* d_ring = nullptr;  // the ring pass's layer
+  size_t ring_cap = 0;
   // the fans depend only on the camera radius and the integration rules:
   // the parameters of the last build, and whether the buffers hold them
   st::lay::FanParams fan_key;
@@ -922,6 +925,211 @@ int context_volume(st_context* ctx, CtxVolume* out) {
 
 }  // namespace st
 
+namespace {
+
+// Foveated ring pass options (render_layered_gpu!, src/metal.jl:3040-3118).
+struct Ring {
+  int width, height;  // ring layer size (<= 0: the display)
+  double rmin;        // periapsis bound in M; <= 0 = no ring pass
+  int box;            // dispatch only the screen box that can hold wound rays
+};
+struct RingBox {
+  int c0, cols, r0, rows;
+};
+
+// Screen box of the rays the ring pass keeps (_ring_screen_box,
+// src/metal.jl:2522-2666).  In Schwarzschild a ray's periapsis is below R > 3M
+// exactly when its impact parameter b = |x x p| / |p_t| is below
+// b(R) = R / sqrt(1 - 2M/R) (captured rays included), and b is conserved, so
+// a probe grid of camera rays built as the kernel builds them (tetrad,
+// projection, index lowering; pixel centres) decides it without
+// integration.  The box of the probes under 1.06 b(R), padded by two probe
+// spacings + 3 pixels, contains the wound set; a set smaller than the probe
+// spacing is seeded at the nearest-approach probe.  Leaves *box as the whole
+// layer when no bound applies or the box covers more than 55 % of it.
+void ring_screen_box(const TraceParams& p, const st_render_params* rp, double ring_rmin, int rw, int rh,
+                     RingBox* box) {
+  *box = RingBox{0, rw, 0, rh};
+  const double M = p.M;
+  if (!(ring_rmin > 2.0 * M)) return;
+  const double bR = ring_rmin / std::sqrt(1.0 - 2.0 * M / ring_rmin) * 1.06;
+  const double x = p.pos[0], y = p.pos[1], z = p.pos[2];
+  const double r = std::sqrt(x * x + y * y + z * z);
+  if (!(r > 2.0 * M)) return;
+  const double f = 2.0 * M / r;
+  const bool fish = p.projection == ST_PROJ_FISHEYE;
+  const int probes = 81, margin = 3;
+  const int nv = std::max(9, probes);
+  const int nu = std::max(9, (int)std::nearbyint((double)probes * rw / rh));
+  const double half_h = rh / 2.0;
+  int imin = INT_MAX, imax = INT_MIN, jmin = INT_MAX, jmax = INT_MIN;
+  double bbest = INFINITY;
+  int ibest = 1, jbest = 1;
+  for (int pj = 1; pj <= nv; ++pj)
+    for (int pi = 1; pi <= nu; ++pi) {
+      const double ipx = 1.0 + (pi - 1) * (double)(rw - 1) / (nu - 1);
+      const double jpx = 1.0 + (pj - 1) * (double)(rh - 1) / (nv - 1);
+      const double u = (ipx - 1.0 + 0.5 - rw / 2.0) / half_h;
+      const double v = (jpx - 1.0 + 0.5 - rh / 2.0) / half_h;
+      double cr, cu, cf;
+      if (fish) {
+        const double rho = std::sqrt(u * u + v * v);
+        const double th = rho * p.fisheye_rad;
+        const double sth = std::sin(th);
+        const double inv = rho > 1e-8 ? 1.0 / rho : 0.0;
+        cr = sth * u * inv; cu = sth * v * inv; cf = std::cos(th);
+      } else {
+        const double dxl = u * p.fov, dyl = v * p.fov;
+        const double nu_ = std::sqrt(dxl * dxl + dyl * dyl + 1.0);
+        cr = dxl / nu_; cu = dyl / nu_; cf = 1.0 / nu_;
+      }
+      double q[4];
+      for (int c = 0; c < 4; ++c) q[c] = cf * p.Ef[c] + cr * p.Er[c] + cu * p.Eu[c] - p.U[c];
+      const double lq = q[0] + (x * q[1] + y * q[2] + z * q[3]) / r;
+      const double pt = -q[0] + f * lq;
+      const double flr = f * lq / r;
+      const double px = q[1] + flr * x, py = q[2] + flr * y, pz = q[3] + flr * z;
+      const double E = std::fabs(pt);
+      if (!(E > 1e-12)) continue;
+      const double Lx = y * pz - z * py, Ly = z * px - x * pz, Lz = x * py - y * px;
+      const double b = std::sqrt(Lx * Lx + Ly * Ly + Lz * Lz) / E;
+      const int ip = (int)std::nearbyint(ipx), jp = (int)std::nearbyint(jpx);
+      if (b < bbest) { bbest = b; ibest = ip; jbest = jp; }
+      if (b < bR) {
+        imin = std::min(imin, ip); imax = std::max(imax, ip);
+        jmin = std::min(jmin, jp); jmax = std::max(jmax, jp);
+      }
+    }
+  if (imin > imax) { imin = imax = ibest; jmin = jmax = jbest; }
+  const int du = 2 * (int)std::ceil((double)(rw - 1) / (nu - 1)) + margin;
+  const int dv = 2 * (int)std::ceil((double)(rh - 1) / (nv - 1)) + margin;
+  const int c0 = std::min(std::max(imin - du, 1), rw) - 1;
+  const int c1 = std::min(std::max(imax + du, 1), rw);
+  const int r0 = std::min(std::max(jmin - dv, 1), rh) - 1;
+  const int r1 = std::min(std::max(jmax + dv, 1), rh);
+  const int cols = c1 - c0, rows = r1 - r0;
+  if ((double)cols * rows > 0.55 * rw * rh) return;
+  *box = RingBox{c0, cols, r0, rows};
+  (void)rp;
+}
+
+int layered_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
+                   int layer_width, int layer_height, const Ring& ring, float* out_rgb, st_ray_diag* host_diag,
+                   st_stats* stats) {
+  if (!ctx || !out_rgb) return ST_EINVAL;
+  int rc = layered_check(cam, stp, rp);
+  if (rc != ST_OK) return rc;
+  const auto t0 = std::chrono::steady_clock::now();
+  TraceParams p;
+  st::Variant v;
+  if ((rc = fill_params(ctx, cam, stp, rp, &p, &v)) != ST_OK) return rc;
+  const int lw = layer_width > 0 ? layer_width : rp->width, lh = layer_height > 0 ? layer_height : rp->height;
+  if (lw < 2 || lh < 2 || (long long)lw * lh > (1ll << 30)) return ST_EINVAL;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
+  cudaStream_t s = ctx->stream;
+  const size_t npix = (size_t)rp->width * rp->height;
+  if ((rc = ensure(&ctx->d_fb, &ctx->fb_cap, npix)) != ST_OK) return rc;
+  if ((rc = ensure(&ctx->d_rgb, &ctx->rgb_cap, 3 * npix)) != ST_OK) return rc;
+  if (host_diag && (rc = ensure(&ctx->d_diag, &ctx->diag_cap, npix)) != ST_OK) return rc;
+  const bool matter = ctx->disc_on || ctx->vol_on;
+  if (matter && (rc = ensure(&ctx->d_layer, &ctx->layer_cap, (size_t)lw * lh)) != ST_OK) return rc;
+  // the ring pass (render_layered_gpu!'s ring_out / ring_rmin, src/metal.jl:3102-3118)
+  const bool use_ring = matter && ring.rmin > 0.0;
+  const int rw = ring.width > 0 ? ring.width : rp->width, rh = ring.height > 0 ? ring.height : rp->height;
+  if (use_ring && (rw < 2 || rh < 2 || (long long)rw * rh > (1ll << 30))) return ST_EINVAL;
+  if (use_ring && (rc = ensure(&ctx->d_ring, &ctx->ring_cap, (size_t)rw * rh)) != ST_OK) return rc;
+  ST_CUDA(cudaMemsetAsync(ctx->d_counters, 0, st::CNT_N * sizeof(unsigned long long), s));
+  ST_CUDA(cudaEventRecord(ctx->ev0, s));
+  double er[4];
+  if ((rc = build_fans(ctx, cam, stp, rp, p, er, s)) != ST_OK) return rc;
+  for (int k = 0; k < 4; ++k) p.er[k] = er[k];
+  // the gate: no ray whose periapsis stays beyond it meets the disc or the gas
+  double gate = 0.0;
+  if (ctx->disc_on) gate = std::max(gate, ctx->disc.outer);
+  if (ctx->vol_on && p.vol_rb2 > 0.0) gate = std::max(gate, std::sqrt(p.vol_rb2));
+  const std::vector<PassPlan> passes = plan_passes(rp, cam);
+  int launches = 0;
+  RingBox box{0, rw, 0, rh};
+  if (use_ring && ring.box) ring_screen_box(p, rp, ring.rmin, rw, rh, &box);
+  for (size_t k = 0; k < passes.size(); ++k) {
+    const PassPlan& pp = passes[k];
+    p.ju = pp.ju; p.jv = pp.jv; p.jw = pp.jw; p.jseed = pp.jseed;
+    p.lens_u0 = pp.lens_u0; p.lens_v0 = pp.lens_v0; p.lens_w = pp.lens_w; p.lens_seed = pp.lens_seed;
+    st::lay::CompParams cp{ctx->d_fan, FAN_N, ctx->d_fine, FAN_FINE, ctx->d_band, nullptr, lw, lh,
+                           nullptr, 0, 0, 0.f};
+    if (matter) {
+      // the disc / gas layer of this pass at the layer resolution
+      TraceParams lp = p;
+      lp.width = lw;
+      lp.height = lh;
+      lp.layer = 1;
+      lp.layer_gate = gate;
+      lp.fan = ctx->d_fan;
+      lp.fan_n = FAN_N;
+      lp.out = ctx->d_layer;
+      lp.diag = nullptr;
+      lp.first_pass = 1;
+      lp.weight = 1.0f;
+      st::fill_float_copies(&lp);
+      st::Variant lv = v;
+      lv.sched = ST_SCHED_PIXEL;
+      ST_CUDA(st::launch_trace(lv, lp, rp->block_x, rp->block_y, ctx->num_sms, s));
+      ++launches;
+      cp.layer = ctx->d_layer;
+      if (use_ring) {
+        // a finer layer of the wound rays only, over the box that can hold them
+        ST_CUDA(st::launch_fill_transparent(ctx->d_ring, (size_t)rw * rh, s));
+        TraceParams rq = lp;
+        rq.width = rw;
+        rq.height = rh;
+        rq.ring_rmin = ring.rmin;
+        rq.out = ctx->d_ring;
+        rq.box_col0 = box.c0; rq.box_cols = box.cols;
+        rq.box_row0 = box.r0; rq.box_rows = box.rows;
+        ST_CUDA(st::launch_trace(lv, rq, rp->block_x, rp->block_y, ctx->num_sms, s));
+        launches += 2;
+        cp.ring = ctx->d_ring;
+        cp.rw = rw;
+        cp.rh = rh;
+        cp.ring_rmin = (float)ring.rmin;
+      }
+    }
+    p.out = ctx->d_fb;
+    p.diag = host_diag ? ctx->d_diag : nullptr;
+    p.first_pass = (k == 0) ? 1 : 0;
+    p.weight = (float)(1.0 / passes.size());
+    if (k == 0) ST_CUDA(cudaStreamWaitEvent(s, ctx->ev_fine, 0));
+    ST_CUDA(st::launch_composite(rp->precision, p, cp, s));
+    ++launches;
+  }
+  ST_CUDA(cudaEventRecord(ctx->ev1, s));
+  unsigned long long cnt[st::CNT_N];
+  ST_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
+  ST_CUDA(st::launch_pack_rgb(ctx->d_fb, ctx->d_rgb, (int)npix, s));
+  ST_CUDA(cudaMemcpyAsync(out_rgb, ctx->d_rgb, 3 * npix * sizeof(float), cudaMemcpyDeviceToHost, s));
+  if (host_diag)
+    ST_CUDA(cudaMemcpyAsync(host_diag, ctx->d_diag, npix * sizeof(st_ray_diag), cudaMemcpyDeviceToHost, s));
+  ST_CUDA(cudaStreamSynchronize(s));
+  const int status = cnt[st::CNT_STATUS] ? (int)cnt[st::CNT_STATUS] : ST_OK;
+  if (stats) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) != cudaSuccess) { (void)cudaGetLastError(); ms = 0.f; }
+    std::memset(stats, 0, sizeof(*stats));
+    stats->kernel_ms = ms;
+    stats->rays = npix * passes.size();
+    stats->steps = cnt[st::CNT_STEPS];
+    stats->gas_samples = cnt[st::CNT_GAS];
+    stats->launches = launches + 3;
+    stats->status = status;
+    stats->h2d_bytes = sizeof(TraceParams) * (launches + 3);
+    stats->d2h_bytes = 3 * npix * sizeof(float) + sizeof cnt;
+    stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return status;
+}
+
+}  // namespace
+
 extern "C" {
 
 int st_abi_version(void) { return ST_ABI_VERSION; }
@@ -1123,6 +1331,7 @@ void st_context_destroy(st_context* ctx) {
   cudaFree(ctx->d_fine);
   cudaFree(ctx->d_band);
   cudaFree(ctx->d_layer);
+  cudaFree(ctx->d_ring);
   if (ctx->ev_coarse) cudaEventDestroy(ctx->ev_coarse);
   if (ctx->ev_fine) cudaEventDestroy(ctx->ev_fine);
   if (ctx->side) cudaStreamDestroy(ctx->side);
@@ -1197,91 +1406,16 @@ int st_sky_fan(st_context* ctx, const st_camera* cam, const st_spacetime* stp, c
 
 int st_render_layered(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
                       int layer_width, int layer_height, float* out_rgb, st_ray_diag* host_diag, st_stats* stats) {
-  if (!ctx || !out_rgb) return ST_EINVAL;
-  int rc = layered_check(cam, stp, rp);
-  if (rc != ST_OK) return rc;
-  const auto t0 = std::chrono::steady_clock::now();
-  TraceParams p;
-  st::Variant v;
-  if ((rc = fill_params(ctx, cam, stp, rp, &p, &v)) != ST_OK) return rc;
-  const int lw = layer_width > 0 ? layer_width : rp->width, lh = layer_height > 0 ? layer_height : rp->height;
-  if (lw < 2 || lh < 2 || (long long)lw * lh > (1ll << 30)) return ST_EINVAL;
-  if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
-  cudaStream_t s = ctx->stream;
-  const size_t npix = (size_t)rp->width * rp->height;
-  if ((rc = ensure(&ctx->d_fb, &ctx->fb_cap, npix)) != ST_OK) return rc;
-  if ((rc = ensure(&ctx->d_rgb, &ctx->rgb_cap, 3 * npix)) != ST_OK) return rc;
-  if (host_diag && (rc = ensure(&ctx->d_diag, &ctx->diag_cap, npix)) != ST_OK) return rc;
-  const bool matter = ctx->disc_on || ctx->vol_on;
-  if (matter && (rc = ensure(&ctx->d_layer, &ctx->layer_cap, (size_t)lw * lh)) != ST_OK) return rc;
-  ST_CUDA(cudaMemsetAsync(ctx->d_counters, 0, st::CNT_N * sizeof(unsigned long long), s));
-  ST_CUDA(cudaEventRecord(ctx->ev0, s));
-  double er[4];
-  if ((rc = build_fans(ctx, cam, stp, rp, p, er, s)) != ST_OK) return rc;
-  for (int k = 0; k < 4; ++k) p.er[k] = er[k];
-  // the gate: no ray whose periapsis stays beyond it meets the disc or the gas
-  double gate = 0.0;
-  if (ctx->disc_on) gate = std::max(gate, ctx->disc.outer);
-  if (ctx->vol_on && p.vol_rb2 > 0.0) gate = std::max(gate, std::sqrt(p.vol_rb2));
-  const std::vector<PassPlan> passes = plan_passes(rp, cam);
-  int launches = 0;
-  for (size_t k = 0; k < passes.size(); ++k) {
-    const PassPlan& pp = passes[k];
-    p.ju = pp.ju; p.jv = pp.jv; p.jw = pp.jw; p.jseed = pp.jseed;
-    p.lens_u0 = pp.lens_u0; p.lens_v0 = pp.lens_v0; p.lens_w = pp.lens_w; p.lens_seed = pp.lens_seed;
-    st::lay::CompParams cp{ctx->d_fan, FAN_N, ctx->d_fine, FAN_FINE, ctx->d_band, nullptr, lw, lh};
-    if (matter) {
-      // the disc / gas layer of this pass at the layer resolution
-      TraceParams lp = p;
-      lp.width = lw;
-      lp.height = lh;
-      lp.layer = 1;
-      lp.layer_gate = gate;
-      lp.fan = ctx->d_fan;
-      lp.fan_n = FAN_N;
-      lp.out = ctx->d_layer;
-      lp.diag = nullptr;
-      lp.first_pass = 1;
-      lp.weight = 1.0f;
-      st::fill_float_copies(&lp);
-      st::Variant lv = v;
-      lv.sched = ST_SCHED_PIXEL;
-      ST_CUDA(st::launch_trace(lv, lp, rp->block_x, rp->block_y, ctx->num_sms, s));
-      ++launches;
-      cp.layer = ctx->d_layer;
-    }
-    p.out = ctx->d_fb;
-    p.diag = host_diag ? ctx->d_diag : nullptr;
-    p.first_pass = (k == 0) ? 1 : 0;
-    p.weight = (float)(1.0 / passes.size());
-    if (k == 0) ST_CUDA(cudaStreamWaitEvent(s, ctx->ev_fine, 0));
-    ST_CUDA(st::launch_composite(rp->precision, p, cp, s));
-    ++launches;
-  }
-  ST_CUDA(cudaEventRecord(ctx->ev1, s));
-  unsigned long long cnt[st::CNT_N];
-  ST_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters, sizeof cnt, cudaMemcpyDeviceToHost, s));
-  ST_CUDA(st::launch_pack_rgb(ctx->d_fb, ctx->d_rgb, (int)npix, s));
-  ST_CUDA(cudaMemcpyAsync(out_rgb, ctx->d_rgb, 3 * npix * sizeof(float), cudaMemcpyDeviceToHost, s));
-  if (host_diag)
-    ST_CUDA(cudaMemcpyAsync(host_diag, ctx->d_diag, npix * sizeof(st_ray_diag), cudaMemcpyDeviceToHost, s));
-  ST_CUDA(cudaStreamSynchronize(s));
-  const int status = cnt[st::CNT_STATUS] ? (int)cnt[st::CNT_STATUS] : ST_OK;
-  if (stats) {
-    float ms = 0.f;
-    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) != cudaSuccess) { (void)cudaGetLastError(); ms = 0.f; }
-    std::memset(stats, 0, sizeof(*stats));
-    stats->kernel_ms = ms;
-    stats->rays = npix * passes.size();
-    stats->steps = cnt[st::CNT_STEPS];
-    stats->gas_samples = cnt[st::CNT_GAS];
-    stats->launches = launches + 3;
-    stats->status = status;
-    stats->h2d_bytes = sizeof(TraceParams) * (launches + 3);
-    stats->d2h_bytes = 3 * npix * sizeof(float) + sizeof cnt;
-    stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-  }
-  return status;
+  return layered_render(ctx, cam, stp, rp, layer_width, layer_height, Ring{0, 0, 0.0, 0}, out_rgb, host_diag, stats);
+}
+
+int st_render_layered_ring(st_context* ctx, const st_camera* cam, const st_spacetime* stp,
+                           const st_render_params* rp, int layer_width, int layer_height, int ring_width,
+                           int ring_height, double ring_rmin, int ring_box, float* out_rgb, st_ray_diag* host_diag,
+                           st_stats* stats) {
+  if (!(ring_rmin >= 0.0) || !std::isfinite(ring_rmin)) return ST_EINVAL;
+  return layered_render(ctx, cam, stp, rp, layer_width, layer_height,
+                        Ring{ring_width, ring_height, ring_rmin, ring_box ? 1 : 0}, out_rgb, host_diag, stats);
 }
 
 int st_render_device(st_context* ctx, const st_camera* cam, const st_spacetime* st, const st_render_params* p,

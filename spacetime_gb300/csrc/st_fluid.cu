@@ -87,9 +87,17 @@ __device__ __forceinline__ int jmod(int a, int n) {
   return r < 0 ? r + n : r;
 }
 
+// jmod for a in [-n, 2n) by compare (the footprints and halos stay there);
+// anything else falls back to the division.
+__device__ __forceinline__ int jwrap(int a, int n) {
+  const int b = a < 0 ? a + n : (a >= n ? a - n : a);
+  return (b >= 0 && b < n) ? b : jmod(a, n);
+}
+
 // Corners of the bilinear footprint of (x, y): radius clamped, phi periodic.
 struct Foot {
   int o00, o10, o01, o11;  // storage offsets of (i0, j0a), (i0+1, j0a), (i0, j1a), (i0+1, j1a)
+  int i0, j0a, j1a;        // the corners' 1-based indices
   float tx, ty;
 };
 
@@ -101,8 +109,9 @@ __device__ __forceinline__ Foot footprint(float x, float y, int nr, int nphi) {
   const float yw = y - (float)nphi * floorf((y - 1.0f) / (float)nphi);
   const int j0 = (int)floorf(yw);
   f.ty = yw - (float)j0;
-  const int j0a = jmod(j0 - 1, nphi) + 1;
-  const int j1a = jmod(j0, nphi) + 1;
+  const int j0a = jwrap(j0 - 1, nphi) + 1;
+  const int j1a = jwrap(j0, nphi) + 1;
+  f.i0 = i0; f.j0a = j0a; f.j1a = j1a;
   f.o00 = (i0 - 1) + nr * (j0a - 1);
   f.o10 = f.o00 + 1;
   f.o01 = (i0 - 1) + nr * (j1a - 1);
@@ -136,9 +145,9 @@ struct Fields {
 // (k_advect_vel!, k_force!: src/disc_sim.jl:136-172).
 __global__ void fluid_velocity_kernel(Fields F, int parity, float dt, float amp, float drag) {
   const int nr = F.nr, nphi = F.nphi;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= nr * nphi) return;
-  const int i = idx % nr + 1, j = idx / nr + 1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;  // one grid row per phi row
+  if (i > nr) return;
+  const int idx = (i - 1) + nr * (j - 1);
   const float x = (float)i - dt * F.vu[idx];
   const float y = (float)j - dt * (F.vv[idx] + F.shear[i - 1]);
   const Foot q = footprint(x, y, nr, nphi);
@@ -166,11 +175,11 @@ __global__ void fluid_velocity_kernel(Fields F, int parity, float dt, float amp,
 // 0.25 ((((0 + 0) + 0) + 0) - dv) = 0.25 (-dv)); with no sweeps p stays 0.
 __global__ void fluid_divergence_kernel(Fields F, int first_sweep) {
   const int nr = F.nr, nphi = F.nphi;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= nr * nphi) return;
-  const int i = idx % nr + 1, j = idx / nr + 1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
+  if (i > nr) return;
+  const int idx = (i - 1) + nr * (j - 1);
   const int ip = min(i + 1, nr), im = max(i - 1, 1);
-  const int jp = jmod(j, nphi) + 1, jm = jmod(j - 2, nphi) + 1;
+  const int jp = jwrap(j, nphi) + 1, jm = jwrap(j - 2, nphi) + 1;
   const float dv = 0.5f * (F.vu2[(ip - 1) + nr * (j - 1)] - F.vu2[(im - 1) + nr * (j - 1)] +
                            F.vv2[(i - 1) + nr * (jp - 1)] - F.vv2[(i - 1) + nr * (jm - 1)]);
   F.div[idx] = dv;
@@ -197,40 +206,44 @@ __global__ void __launch_bounds__(256) fluid_pressure_kernel(Fields F, int src, 
   const int j0 = blockIdx.y * TJ + 1 - H;
   const float* __restrict__ pin = src ? F.prs[1] : F.prs[0];
   float* __restrict__ pout = src ? F.prs[0] : F.prs[1];
-  for (int l = threadIdx.x; l < RN; l += blockDim.x) {
-    const int li = l % RI, lj = l / RI;
-    const int gi = i0 + li;
-    const int gj = jmod(j0 + lj - 1, nphi) + 1;
-    float pv = 0.0f, dv = 0.0f;
-    if (gi >= 1 && gi <= nr) {
-      const int o = (gi - 1) + nr * (gj - 1);
-      pv = pin[o];
-      dv = F.div[o];
+  // blockDim = (32, 8): x runs along i (coalesced), y along phi
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int lj = ty; lj < RJ; lj += 8) {
+    const int gj = jwrap(j0 + lj - 1, nphi) + 1;
+    for (int li = tx; li < RI; li += 32) {
+      const int gi = i0 + li;
+      float pv = 0.0f, dv = 0.0f;
+      if (gi >= 1 && gi <= nr) {
+        const int o = (gi - 1) + nr * (gj - 1);
+        pv = pin[o];
+        dv = F.div[o];
+      }
+      P0[li + RI * lj] = pv;
+      D[li + RI * lj] = dv;
     }
-    P0[l] = pv;
-    D[l] = dv;
   }
   __syncthreads();
   float* cur = P0;
   float* nxt = P1;
   for (int k = 1; k <= sweeps; ++k) {
     // valid region after this sweep: margin k from every side of the staged block
-    for (int l = threadIdx.x; l < RN; l += blockDim.x) {
-      const int li = l % RI, lj = l / RI;
-      if (li < k || li >= RI - k || lj < k || lj >= RJ - k) continue;
-      const int gi = i0 + li;
-      if (gi < 1 || gi > nr) continue;
-      const int lip = gi + 1 <= nr ? li + 1 : li;  // clamped radial neighbours
-      const int lim = gi - 1 >= 1 ? li - 1 : li;
-      const float s = cur[lip + RI * lj] + cur[lim + RI * lj] + cur[li + RI * (lj + 1)] + cur[li + RI * (lj - 1)];
-      nxt[l] = 0.25f * (s - D[l]);
+    for (int lj = k + ty; lj < RJ - k; lj += 8) {
+      for (int li = k + tx; li < RI - k; li += 32) {
+        const int gi = i0 + li;
+        if (gi < 1 || gi > nr) continue;
+        const int lip = gi + 1 <= nr ? li + 1 : li;  // clamped radial neighbours
+        const int lim = gi - 1 >= 1 ? li - 1 : li;
+        const int l = li + RI * lj;
+        const float sum = cur[lip + RI * lj] + cur[lim + RI * lj] + cur[l + RI] + cur[l - RI];
+        nxt[l] = 0.25f * (sum - D[l]);
+      }
     }
     __syncthreads();
     float* tmp = cur; cur = nxt; nxt = tmp;
   }
   // the tile's own cells
-  for (int l = threadIdx.x; l < TI * TJ; l += blockDim.x) {
-    const int ti = l % TI, tj = l / TI;
+  for (int tj = ty; tj < TJ; tj += 8) {
+    const int ti = tx;
     const int gi = blockIdx.x * TI + 1 + ti, gjr = blockIdx.y * TJ + 1 + tj;
     if (gi > nr || gjr > nphi) continue;
     const int li = ti + H, lj = tj + H;
@@ -247,8 +260,8 @@ __global__ void __launch_bounds__(256) fluid_pressure_kernel(Fields F, int src, 
 }
 
 // Forward semi-Lagrangian density sample at cell (ci, cj) (k_adv_scalar!).
-__device__ __forceinline__ float advect_at(const Fields& F, const float* __restrict__ d, int o, float dt) {
-  const int ci = o % F.nr + 1, cj = o / F.nr + 1;
+__device__ __forceinline__ float advect_at(const Fields& F, const float* __restrict__ d, int ci, int cj, float dt) {
+  const int o = (ci - 1) + F.nr * (cj - 1);
   const float x = (float)ci - dt * F.vu[o];
   const float y = (float)cj - dt * (F.vv[o] + F.shear[ci - 1]);
   return bilerp(d, footprint(x, y, F.nr, F.nphi));
@@ -259,13 +272,13 @@ __device__ __forceinline__ float advect_at(const Fields& F, const float* __restr
 // through the envelope (k_extrude!, :253-266).  Thread 0 advances the clock.
 __global__ void fluid_density_kernel(Fields F, int parity, float dt, float relax) {
   const int nr = F.nr, nphi = F.nphi;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1;
   const float t = F.t[parity];
-  if (idx == 0) F.t[1 - parity] = t + dt;
-  if (idx >= nr * nphi) return;
+  if (i == 1 && j == 1) F.t[1 - parity] = t + dt;
+  if (i > nr) return;
+  const int idx = (i - 1) + nr * (j - 1);
   const float* __restrict__ d = parity ? F.dens[1] : F.dens[0];
   float* __restrict__ dout = parity ? F.dens[0] : F.dens[1];
-  const int i = idx % nr + 1, j = idx / nr + 1;
   // forward: d1 = d at the backtraced point; its corners bound the limiter
   const float x = (float)i - dt * F.vu[idx];
   const float y = (float)j - dt * (F.vv[idx] + F.shear[i - 1]);
@@ -278,8 +291,8 @@ __global__ void fluid_density_kernel(Fields F, int parity, float dt, float relax
   const float xb = (float)i - ndt * F.vu[idx];
   const float yb = (float)j - ndt * (F.vv[idx] + F.shear[i - 1]);
   const Foot qb = footprint(xb, yb, nr, nphi);
-  const float c00 = advect_at(F, d, qb.o00, dt), c10 = advect_at(F, d, qb.o10, dt);
-  const float c01 = advect_at(F, d, qb.o01, dt), c11 = advect_at(F, d, qb.o11, dt);
+  const float c00 = advect_at(F, d, qb.i0, qb.j0a, dt), c10 = advect_at(F, d, qb.i0 + 1, qb.j0a, dt);
+  const float c01 = advect_at(F, d, qb.i0, qb.j1a, dt), c11 = advect_at(F, d, qb.i0 + 1, qb.j1a, dt);
   const float ea = c00 + qb.tx * (c10 - c00);
   const float eb = c01 + qb.tx * (c11 - c01);
   const float d2 = ea + qb.ty * (eb - ea);
@@ -288,8 +301,20 @@ __global__ void fluid_density_kernel(Fields F, int parity, float dt, float relax
   const float tgt = F.base[idx] * expf(1.2f * (2.0f * n - 1.0f));
   const float dn = fmaxf(a + relax * dt * (tgt - a), 0.0f);
   dout[idx] = dn;
+  // the envelope loads of a batch are issued before its stores, so the
+  // column's latency is paid once per eight cells rather than per cell
   const size_t plane = (size_t)nr * nphi;
-  for (int k = 0; k < F.nz; ++k) F.vol[idx + plane * k] = dn * F.env[(i - 1) + nr * k];
+  const float* __restrict__ env = F.env + (i - 1);
+  float* __restrict__ vol = F.vol + idx;
+  int k = 0;
+  for (; k + 8 <= F.nz; k += 8) {
+    float e[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) e[q] = __ldg(env + (size_t)nr * (k + q));
+#pragma unroll
+    for (int q = 0; q < 8; ++q) vol[plane * (k + q)] = dn * e[q];
+  }
+  for (; k < F.nz; ++k) vol[plane * k] = dn * __ldg(env + (size_t)nr * k);
 }
 
 }  // namespace fluid
@@ -326,8 +351,11 @@ int launch_step(st_fluid* f, int parity, float dt, int jacobi, cudaStream_t s) {
       cv.meta.nz != f->nz)
     return ST_ESTATE;
   F.vol = cv.d_vol;
-  const int n = f->nr * f->nphi;
-  const int B = 256, G = (n + B - 1) / B;
+  // one 64-thread block per 64 cells of an s row, one grid row per phi row:
+  // the grids are a few tens of thousands of cells, so small blocks spread
+  // them over all SMs, and the 2-D grid gives (i, j) without a division
+  const int B = 64;
+  const dim3 G((f->nr + B - 1) / B, f->nphi);
   fluid_velocity_kernel<<<G, B, 0, s>>>(F, parity, dt, (float)f->forcing, (float)f->drag);
   // 2 ceil(jacobi / 2) sweeps (src/disc_sim.jl:305-308); the first runs in the
   // divergence kernel, the rest in blocked passes of at most MAX_SWEEPS
@@ -342,7 +370,7 @@ int launch_step(st_fluid* f, int parity, float dt, int jacobi, cudaStream_t s) {
     const int last = left == 0 ? 1 : 0;
     const int H = k + last;
     const size_t smem = 3 * (size_t)(TI + 2 * H) * (TJ + 2 * H) * sizeof(float);
-    fluid_pressure_kernel<<<grid, 256, smem, s>>>(F, src, k, last);
+    fluid_pressure_kernel<<<grid, dim3(32, 8), smem, s>>>(F, src, k, last);
     src = 1 - src;
   } while (left > 0);
   fluid_density_kernel<<<G, B, 0, s>>>(F, parity, dt, (float)f->relax);
@@ -378,6 +406,7 @@ int st_fluid_create(st_fluid** out, st_context* ctx, const st_disc* disc, const 
   if (st::context_volume(ctx, &cv) != ST_OK || !cv.on || !cv.d_vol) return ST_ESTATE;
   const int nr = cv.meta.nr, nphi = cv.meta.nphi, nz = cv.meta.nz;
   if (nr < 2 || nphi < 1 || nz < 2) return ST_ESTATE;
+  if (nphi > 65535) return ST_EUNSUPPORTED;  // one grid row per phi row
   if (cudaSetDevice(cv.device) != cudaSuccess) return ST_ECUDA;
   const size_t n = (size_t)nr * nphi;
   // initial density: the volume's midplane slice k = (nz + 1) / 2 (1-based),

