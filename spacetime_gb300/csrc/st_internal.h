@@ -132,6 +132,8 @@ struct TraceParams {
   // double -> float conversion issues on the FP64 pipe)
   struct Flt {
     float M, a, rkill2, vol_rb2, hcap, dt, hcoef, tspan, ds_gas, zmax, r_isco, E_isco, L_isco, opac, emis, disc_inner, disc_outer, disc_falloff, lut_tmin, lut_tmax, ls_in, ls_out, crit_r2, r_guard2, tol, layer_gate;
+    // float step rule without per-step divisions: hcoef / M and 1 / max(rkill2, 1e-6)
+    float hcoef_m, inv_rkill2;
   } f;
 };
 
@@ -163,6 +165,8 @@ inline void fill_float_copies(TraceParams* p) {
   p->f.r_guard2 = (float)p->r_guard2;
   p->f.tol = (float)p->tol;
   p->f.layer_gate = (float)p->layer_gate;
+  p->f.hcoef_m = (float)(p->hcoef / p->M);
+  p->f.inv_rkill2 = (float)(1.0 / (p->rkill2 > 1e-6 ? p->rkill2 : 1e-6));
 }
 
 // Variant key of the compiled kernels (the reference's Val{...} switches,

@@ -124,7 +124,9 @@ __device__ __forceinline__ R ks_r2(R x, R y, R z, R a) {
 //   d(L.p)/dr     = ((a^2 - r^2) A - 2 r a B) / (r^2 + a^2)^2 - z p_z / r^2
 //   dp_xy         = G r^3/Sigma (x, y) + f l / (r^2 + a^2) (r p_x - a p_y, r p_y + a p_x)
 //   dp_z          = G z r (r^2 + a^2) / Sigma + l^2/2 df/dz + f l p_z / r
-// where G = l^2/2 df/dr + f l d(L.p)/dr collects every term along grad r.
+// where G = l^2/2 df/dr + f l d(L.p)/dr collects every term along grad r, and
+// the f derivatives are taken from f itself: df/dr = (f/r)(3 a^2 z^2 - r^4)/Sigma,
+// df/dz = -2 a^2 z f / Sigma.
 // r2_known: this state's ks_r2_f32 when the caller has it, else negative.
 __device__ __forceinline__ void rhs_kerr_f32(const float* s, float pt, float M, float a, float* d,
                                              float r2_known = -1.f) {
@@ -150,16 +152,17 @@ __device__ __forceinline__ void rhs_kerr_f32(const float* s, float pt, float M, 
   d[0] = fmaf(-Fi, fmaf(r, x, a * y), px);
   d[1] = fmaf(-Fi, fmaf(r, y, -(a * x)), py);
   d[2] = fmaf(-flir, z, pz);
-  const float hl2 = 0.5f * ell * ell;
-  const float isig2 = isig * isig;
-  const float dfdr = (2.f * M) * r2 * fmaf(3.f, q, -(r2 * r2)) * isig2;
-  const float dfz0 = (-4.f * M * a2) * (r3 * z) * isig2;
+  // l^2/2 df/dr = (l/2) (f l / r) (3 a^2 z^2 - r^4) / Sigma, since
+  // df/dr = (f / r) (3 a^2 z^2 - r^4) / Sigma
+  const float hd = (0.5f * ell) * flir * fmaf(3.f, q, -(r2 * r2)) * isig;
   const float dldr = fmaf(-zpz, ir * ir, fmaf(a2 - r2, A, -((2.f * a) * r * B)) * (ira * ira));
-  const float G = fmaf(hl2, dfdr, fl * dldr);
+  const float G = fmaf(fl, dldr, hd);
   const float Gr = G * rsig;
   d[3] = fmaf(Gr, x, Fi * fmaf(r, px, -(a * py)));
   d[4] = fmaf(Gr, y, Fi * fmaf(r, py, a * px));
-  d[5] = fmaf(G, (z * r) * (r2a * isig), fmaf(hl2, dfz0, flir * pz));
+  // G dr/dz + l^2/2 df/dz + f l p_z / r, with dr/dz = z r (r^2 + a^2) / Sigma and
+  // l^2/2 df/dz = -a^2 z l (f l) / Sigma
+  d[5] = fmaf(z, fmaf(G * r, r2a, -((a2 * ell) * fl)) * isig, flir * pz);
 }
 
 // Kerr, src/metal.jl:466-508 (implicit-quartic r, four derivative terms).
@@ -1079,10 +1082,14 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
   }
   // radius-adaptive step, src/metal.jl:1250-1260
   const R cap = (VOL && r2 < PR(vol_rb2)) ? R(2) : PR(hcap);
-  R h = PR(dt) * min_(max_(PR(hcoef) * r / M, R(1)), cap);
+  R h;
+  if constexpr (IsD<R>::v) h = PR(dt) * min_(max_(PR(hcoef) * r / M, R(1)), cap);
+  else h = PR(dt) * min_(max_(p.f.hcoef_m * r, R(1)), cap);
   if constexpr (KERR) {
     const R rk = PR(rkill2);
-    const R fr = clamp_((rk2 - rk) / max_(rk, R(1e-6)), R(0), R(1));
+    R fr;
+    if constexpr (IsD<R>::v) fr = clamp_((rk2 - rk) / max_(rk, R(1e-6)), R(0), R(1));
+    else fr = clamp_((rk2 - rk) * p.f.inv_rkill2, R(0), R(1));
     h *= R(0.12) + R(0.88) * fr;
   }
   if constexpr (SEM == ST_SEM_RENDER) h = min_(h, PR(tspan) - st.lambda);
@@ -1181,8 +1188,9 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
       }
     }
     if (p.exit_landing) {
-      const R rn = sqrt_(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
-      if (rn > st.r_esc) {
+      const R rn2 = y[0] * y[0] + y[1] * y[1] + y[2] * y[2];
+      if (rn2 > st.r_esc * st.r_esc) {  // beyond the escape sphere (squared: no root per step)
+        const R rn = sqrt_(rn2);
         R yt[6];
         land_on_sphere<KERR>(yp, st.pt, M, a, h, k1, r, rn, st.r_esc, yt);
 #pragma unroll
