@@ -324,6 +324,11 @@ def fluid_variant(ctx_cls, device: int, steps: int = 200) -> dict:
     return out
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum of the 1920x1080 config-1 FP32 launch
+# (26.14 MB read, 0.07 MB written; profiles/trace_fp32_kerr_gas_1080p_dram.md)
+TRACE_1080P_DRAM_BYTES = 26_140_160 + 71_424
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -589,6 +594,15 @@ def main(argv=None):
                 if (W, H) == (1920, 1080) else cpu_baseline(workload=args.workload)
         except Exception as e:  # report, do not fail the bench
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
+    # DRAM bytes of one launch, from an ncu capture of this exact frame (the
+    # two dram__bytes counters take one pass, so it was captured at full size)
+    if args.workload == "config1" and (W, H) == (1920, 1080) and args.precision == "fp32" and args.schedule == "pixel":
+        traffic = TRACE_1080P_DRAM_BYTES
+        traffic_note = ("dram__bytes_read.sum + dram__bytes_write.sum of one launch, ncu "
+                        "(profiles/trace_fp32_kerr_gas_1080p_dram.md): compulsory reads of the gas texture, "
+                        "table and sampled sky; the kernel is issue-bound, HBM idle")
+    else:
+        traffic, traffic_note = None, "captured for the default 1920x1080 FP32 frame only"
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -617,7 +631,8 @@ def main(argv=None):
         },
         "roofline": {
             "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-            "frac": achieved / fp32_peak, "traffic": None,
+            "frac": achieved / fp32_peak, "traffic": traffic,
+            "traffic_note": traffic_note,
             "peak_note": f"nominal FP32 FMA rate: {sms} SMs x 128 lanes x 2 x {sm_max:.0f} MHz "
                          "(MEASURED_PEAKS.json has no FP32 figure)",
             "flops_per_step": flops_per_step(True), "flops_per_gas_sample": FLOPS_GAS_SAMPLE,
