@@ -134,6 +134,11 @@ struct TraceParams {
     float M, a, rkill2, vol_rb2, hcap, dt, hcoef, tspan, ds_gas, zmax, r_isco, E_isco, L_isco, opac, emis, disc_inner, disc_outer, disc_falloff, lut_tmin, lut_tmax, ls_in, ls_out, crit_r2, r_guard2, tol, layer_gate;
     // float step rule without per-step divisions: hcoef / M and 1 / max(rkill2, 1e-6)
     float hcoef_m, inv_rkill2;
+    // float gas-grid index scales: (nr - 1) / (ls_out - ls_in), nphi / 2 pi,
+    // (nz - 1) / (2 zmax)
+    float vol_sr, vol_sp, vol_sz;
+    // blackbody table index scale (lut_size - 1) / (lut_tmax - lut_tmin)
+    float lut_sc;
   } f;
 };
 
@@ -167,6 +172,10 @@ inline void fill_float_copies(TraceParams* p) {
   p->f.layer_gate = (float)p->layer_gate;
   p->f.hcoef_m = (float)(p->hcoef / p->M);
   p->f.inv_rkill2 = (float)(1.0 / (p->rkill2 > 1e-6 ? p->rkill2 : 1e-6));
+  p->f.vol_sr = p->ls_out > p->ls_in ? (float)((p->nr - 1) / (p->ls_out - p->ls_in)) : 0.f;
+  p->f.vol_sp = (float)(p->nphi / 6.283185307179586);
+  p->f.vol_sz = p->zmax > 0.0 ? (float)((p->nz - 1) / (2.0 * p->zmax)) : 0.f;
+  p->f.lut_sc = p->lut_tmax > p->lut_tmin ? (float)((p->lut_size - 1) / (p->lut_tmax - p->lut_tmin)) : 0.f;
 }
 
 // Variant key of the compiled kernels (the reference's Val{...} switches,

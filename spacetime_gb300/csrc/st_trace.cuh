@@ -338,10 +338,15 @@ __device__ __forceinline__ R emitter_opz(R sx, R sy, R psx, R psy, R E, R M, R a
 template <typename R>
 __device__ __forceinline__ float4 lut_color(const TraceParams& p, R T, bool render_rule) {
   const R tmin = PR(lut_tmin), tmax = PR(lut_tmax);
-  const R fr = (clamp_(T, tmin, tmax) - tmin) / (tmax - tmin);
   int idx;
-  if (render_rule) idx = (int)rint(fr * R(p.lut_size - 1));
-  else idx = (int)(fr * (R(p.lut_size) - R(1)) + R(0.5));
+  if constexpr (IsD<R>::v) {
+    const R fr = (clamp_(T, tmin, tmax) - tmin) / (tmax - tmin);
+    if (render_rule) idx = (int)rint(fr * R(p.lut_size - 1));
+    else idx = (int)(fr * (R(p.lut_size) - R(1)) + R(0.5));
+  } else {  // the index scale comes from the host: no division per lookup
+    const R x = (clamp_(T, tmin, tmax) - tmin) * p.f.lut_sc;
+    idx = render_rule ? (int)rintf(x) : (int)(x + R(0.5));
+  }
   idx = min(max(idx, 0), p.lut_size - 1);
   return __ldg(p.lut + idx);
 }
@@ -356,12 +361,19 @@ __device__ __forceinline__ R sample_volume(const TraceParams& p, R sc, R phi, R 
   if (ls <= lin || ls >= lout) return R(0);
   const int nr = p.nr, nphi = p.nphi, nz = p.nz;
   const R two_pi = R(6.283185307179586);
-  const R fr = (ls - lin) / (lout - lin) * R(nr - 1);
   // phi comes from atan2, so |phi| <= pi and mod(phi, 2 pi) is one conditional add
   R pm = phi;
   if (pm < R(0)) pm += two_pi;
-  const R fp = pm / two_pi * R(nphi);
-  const R fz = (z + zmax) / (R(2) * zmax) * R(nz - 1);
+  R fr, fp, fz;
+  if constexpr (IsD<R>::v) {
+    fr = (ls - lin) / (lout - lin) * R(nr - 1);
+    fp = pm / two_pi * R(nphi);
+    fz = (z + zmax) / (R(2) * zmax) * R(nz - 1);
+  } else {  // the three scales come from the host: no division per sample
+    fr = (ls - lin) * p.f.vol_sr;
+    fp = pm * p.f.vol_sp;
+    fz = (z + zmax) * p.f.vol_sz;
+  }
   const int i0 = min(max((int)floor_(fr), 0), nr - 2);
   const R tr = fr - R(i0);
   const int j0 = (int)floor_(fp);
