@@ -1,0 +1,76 @@
+"""Edge cases of the render entry points on the GPU.
+
+- Ragged and degenerate frames (1x1, a single row or column, sizes that are
+  no multiple of the 16x8 tile or of the 8x4 persistent tile) render every
+  pixel and agree with the oracle's FP64 twin at the parity tolerance
+  (radiance p99 <= 1e-5), for both schedules.
+- Arguments the reference rejects come back as ST_EINVAL without touching
+  the device: sizes <= 0 or beyond 2^30 pixels, samples <= 0, dt <= 0,
+  |a| > M (src/gr.jl:31), an unknown integrator order.
+"""
+import types
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from spacetime_gb300 import _abi, workloads
+from spacetime_gb300.api import Context, Kerr
+
+from .helpers import compare, gpu_render, oracle_scene
+
+pytestmark = pytest.mark.gpu
+
+FP64 = _abi.ST_PREC_FP64
+
+
+@pytest.fixture(scope="module")
+def sky():
+    return workloads.sky(512, 256)
+
+
+def _draft_disc():
+    w = workloads.config0()
+    w.semantics = _abi.ST_SEM_DRAFT
+    w.emitter = _abi.ST_EMIT_KS_EXACT
+    w.params = dict(samples=1, pixel_jitter=0, exit_landing=1)
+    return w
+
+
+@pytest.mark.parametrize("size", [(1, 1), (1, 9), (17, 1), (17, 3), (33, 27)])
+@pytest.mark.parametrize("schedule", [_abi.ST_SCHED_PIXEL, _abi.ST_SCHED_PERSISTENT])
+def test_ragged_frames_match_the_twin(built_lib, sky, size, schedule):
+    w = _draft_disc().scaled(*size)
+    g = gpu_render(w, sky, FP64, schedule=schedule)
+    assert g.image.shape == (size[1], size[0], 3)
+    assert np.isfinite(g.image).all()
+    assert g.stats["rays"] == size[0] * size[1]
+    ref, rays = oracle_scene(w, sky, O.INT_RK4).render()
+    c = compare(g.image, g.diag, ref, rays)
+    assert c["class_mismatch"] == 0, c
+    assert c["rad_p99"] <= 1e-5, c
+
+
+def test_arguments_the_reference_rejects(built_lib, sky):
+    w = _draft_disc().scaled(8, 8)
+    with Context(sky, disc=w.disc, emitter=w.emitter) as ctx:
+        def code(bh=w.bh, **kw):
+            args = dict(width=8, height=8)
+            args.update(kw)
+            p = ctx.params(_abi.ST_SEM_DRAFT, **args)
+            # a one-pixel host buffer: the library validates before it writes
+            with pytest.raises(_abi.StError) as e:
+                ctx.render_raw(w.cam, bh, p, out=np.empty((1, 1, 3), np.float32))
+            return e.value.code
+        assert code(width=0) == _abi.ST_EINVAL
+        assert code(height=-3) == _abi.ST_EINVAL
+        assert code(width=1 << 16, height=1 << 15) == _abi.ST_EINVAL   # 2^31 pixels
+        assert code(samples=0) == _abi.ST_EINVAL
+        assert code(dt=0.0) == _abi.ST_EINVAL
+        assert code(order=5) == _abi.ST_EINVAL
+        assert code(bh=types.SimpleNamespace(M=1.0, a=1.5)) == _abi.ST_EINVAL   # past the C ABI
+        with pytest.raises(ValueError):
+            Kerr(1.0, 1.5)                                                    # and in the Python API
+        # the context is still usable afterwards
+        ok = ctx.render_raw(w.cam, w.bh, ctx.params(_abi.ST_SEM_DRAFT, width=8, height=8))
+        assert np.isfinite(ok.image).all()
