@@ -162,18 +162,22 @@ function set_starfield_gb300!(ctx::GB300Context; strength::Real=1.0, texture_wei
           "st_context_set_starfield")
 end
 
-"""`render_draft_mtl(ctx, cam, st; ...)` on the GPU with the Metal kernel's rules; with
-`camera_at` (a function of the shutter fraction s in [0, 1) returning a Camera) it renders
-motion blur, midpoint or per-pixel shutter, through st_render_motion."""
+"""`render_draft_mtl(ctx, cam, st; ...)` on the GPU with the Metal kernel's rules, same
+keywords (src/metal.jl:2040-2054) including `refine`; with `camera_at` (a function of the
+shutter fraction s in [0, 1) returning a Camera) it renders motion blur, midpoint or
+per-pixel shutter, through st_render_motion."""
 function render_draft_gb300(ctx::GB300Context, cam::Camera, bh; width::Int=1920, height::Int=1080,
                             samples::Int=2, dt::Real=0.02, fisheye_deg::Real=0.0, aperture_world::Real=0.0,
                             focus_dist::Real=1.0, relativistic::Bool=false, precision::Int=ST_PREC_FP32,
                             pixel_jitter::Bool=true, camera_at::Union{Function,Nothing}=nothing,
-                            per_pixel_shutter::Bool=false, order::Int=4, tol::Real=1e-4)
+                            per_pixel_shutter::Bool=false, order::Int=4, tol::Real=1e-4,
+                            refine::Int=1, refine_var::Real=0.35, refine_graze::Real=0.05,
+                            refine_margin::Int=8)
     p = default_params(ST_SEM_DRAFT)
     p.width = width; p.height = height; p.samples = samples; p.dt = dt
     p.relativistic = relativistic; p.precision = precision; p.pixel_jitter = pixel_jitter
     p.order = order; p.tol = tol
+    p.refine = refine; p.refine_var = refine_var; p.refine_graze = refine_graze; p.refine_margin = refine_margin
     c = st_camera(cam; fisheye_deg, aperture_world, focus_dist)
     camera_at === nothing && return st_render!(ctx, c, bh, p)
     n = samples^2
