@@ -21,9 +21,11 @@ LIB = os.environ.get("SPACETIME_GB300_LIB", os.path.join(HERE, "libspacetime_gb3
 FAST = os.environ.get("ST_FASTMATH", "1") == "1"
 MINB_FP32 = os.environ.get("ST_MINB_FP32", "7")
 MINB_FP32G = os.environ.get("ST_MINB_FP32G", "4")
+MINB_FP64 = os.environ.get("ST_MINB_FP64", "1")
 UNIT_FLAGS = {
     "st_trace_fp32.cu": (["--use_fast_math"] if FAST else []) + [f"-DST_MINB={MINB_FP32}"],
     "st_trace_fp32_guarded.cu": (["--use_fast_math"] if FAST else []) + [f"-DST_MINB={MINB_FP32G}"],
+    "st_trace_fp64.cu": [f"-DST_MINB={MINB_FP64}"],
     # the fluid solver rounds every float operation as written (no contraction)
     "st_fluid.cu": ["-fmad=false"],
 }
