@@ -282,6 +282,58 @@ def layered_variant(ctx_cls, device: int, flush, reps: int = 3) -> dict:
     return out
 
 
+def features_variant(ctx_cls, device: int, flush, reps: int = 3) -> dict:
+    """The draft renderer's optional features on config 1's 1920x1080 frame
+    (Kerr a=0.9 with gas, FP32), device time per frame beside the plain frame
+    of the same passes: procedural stars; 4 jittered passes plain, with a
+    per-pixel motion-blur shutter (camera_at moving the camera 0.2 M along
+    its right axis), and with adaptive refinement (refine 3); depth buckets
+    (10, one pass)."""
+    import numpy as np
+    import torch
+    from spacetime_gb300 import _abi, workloads
+    from spacetime_gb300.api import Starfield
+    from spacetime_gb300.scene import Camera
+    w = workloads.config1()
+    ctx = ctx_cls(workloads.sky(), disc=w.disc, volume=w.vol, emitter=w.emitter, device=device)
+    base = dict(w.params)
+
+    def params(**kw):
+        q = dict(base)
+        q.update(kw)
+        return ctx.params(w.semantics, width=1920, height=1080, precision=_abi.ST_PREC_FP32, **q)
+
+    def timed(fn):
+        fn()
+        ts = []
+        for _ in range(reps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ts.append(fn().stats["kernel_ms"])
+        return float(np.median(ts))
+
+    out = {"workload": "config1 camera, hole and gas, 1920x1080, kernel rules, FP32"}
+    one = params()
+    out["plain_1_pass_ms"] = timed(lambda: ctx.render_raw(w.cam, w.bh, one))
+    out["depth_buckets_10_ms"] = timed(lambda: ctx.render_depth_raw(w.cam, w.bh, one, 10))
+    ctx.set_starfield(Starfield(height=1080, fov_factor=w.cam.fov_factor))
+    out["starfield_1_pass_ms"] = timed(lambda: ctx.render_raw(w.cam, w.bh, one))
+    ctx.set_starfield(None)
+    four = params(samples=2, pixel_jitter=1, seed=3)
+    out["plain_4_passes_ms"] = timed(lambda: ctx.render_raw(w.cam, w.bh, four))
+    c = w.cam
+    poses = [Camera(c.pos + (0.2 * m / 4) * c.right, c.fwd, c.right, c.up_local, c.fov_factor, c.velocity)
+             for m in range(5)]
+    out["motion_blur_4_passes_ms"] = timed(lambda: ctx.render_motion_raw(c, poses, w.bh, four,
+                                                                          per_pixel_shutter=True))
+    ref = params(samples=2, pixel_jitter=1, seed=3, refine=3)
+    r = ctx.render_raw(w.cam, w.bh, ref)
+    out["refine_3_ms"] = timed(lambda: ctx.render_raw(w.cam, w.bh, ref))
+    out["refine_3_rays_per_pixel"] = r.stats["rays"] / (1920 * 1080)
+    ctx.close()
+    return out
+
+
 def fluid_variant(ctx_cls, device: int, steps: int = 200) -> dict:
     """The live fluid disc (DiscFluidSim / step_sim!, dt 0.08, jacobi 8) on two
     grids: config 1's gas grid (256 x 64 x 32, ISCO to 25 M) and the
@@ -583,6 +635,10 @@ def main(argv=None):
             variants["fluid_disc"] = fluid_variant(Context, local)
         except Exception as e:  # report, do not fail the bench
             variants["fluid_disc"] = {"failed": str(e)}
+        try:
+            variants["features"] = features_variant(Context, local, flush)
+        except Exception as e:  # report, do not fail the bench
+            variants["features"] = {"failed": str(e)}
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         try:
