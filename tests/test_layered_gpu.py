@@ -190,3 +190,23 @@ def test_ring_pass(built_lib):
     print("ring region: half-res median", np.median(e_lo), "ring median", np.median(e_ring),
           "ms", ring.stats["kernel_ms"], nobox.stats["kernel_ms"], lo.stats["kernel_ms"], hi.stats["kernel_ms"])
     assert np.mean(e_ring) < np.mean(e_lo)
+
+
+def test_layered_with_gas_matches_full_trace(built_lib):
+    """The layer pass with a gas volume (the gate is the gas sphere): emission
+    is traced identically inside it, the sky comes from the fan outside."""
+    from spacetime_gb300.scene import make_volume
+    wl = _scene(disc=True, w=160, h=90)
+    vol = make_volume(inner=3.0, outer=20.0, nr=96, nphi=64, nz=16, seed=4)
+    sky = workloads.sky(512, 256)
+    with Context(sky, disc=wl.disc, volume=vol, emitter=wl.emitter) as ctx:
+        p = _params(ctx, wl, FP32)
+        lay = ctx.render_layered_raw(wl.cam, wl.bh, p)
+        full = ctx.render_raw(wl.cam, wl.bh, p)
+    assert lay.stats["gas_samples"] > 0 and lay.stats["status"] == _abi.ST_OK
+    lum = np.maximum(full.image.astype(np.float64).sum(-1), 1e-6)
+    rel = np.abs(lay.image - full.image).sum(-1) / lum
+    print("layered + gas vs trace: median", np.median(rel), "p99", np.percentile(rel, 99),
+          "gas samples", lay.stats["gas_samples"], full.stats["gas_samples"])
+    assert np.median(rel) <= 1e-4
+    assert np.percentile(rel, 99) <= 1e-2
