@@ -442,6 +442,20 @@ def run_track(args):
     ms = float(np.mean(kms))
     value = rays / (ms * 1e-3) / 1e6
     kerr = getattr(w.bh, "a", 0.0) != 0.0
+    variants = {}
+    if args.precision == "fp32" and not args.no_variants:
+        # the same track on the plain FP64-guarded path (renormalisation every 256
+        # steps, FP64 steps inside 3 M and for near-critical rays inside 4 M)
+        pg = ctx.params(w.semantics, width=w.width, height=w.height, precision=_abi.ST_PREC_FP32_GUARDED,
+                        r_guard=3.0, crit_band=0.05, crit_r=4.0, renorm_every=256, **w.params)
+        autotune.apply(pg, tuned)
+        pg.graph = 1
+        ctx.render_frames_raw(w.cams, w.bh, pg)
+        rg = ctx.render_frames_raw(w.cams, w.bh, pg)
+        msg = rg.stats["kernel_ms"]
+        variants["fp32_fp64_guarded"] = {"value": rays / (msg * 1e-3) / 1e6, "ms_per_step": msg,
+                                         "fp64_steps_per_track": rg.stats["fp64_steps"],
+                                         "speedup_of_value": (rays / (ms * 1e-3)) / (rays / (msg * 1e-3))}
     flops = st["steps"] * flops_per_step(kerr) + st["gas_samples"] * FLOPS_GAS_SAMPLE
     achieved = flops / (ms * 1e-3) / 1e12
     sms = torch.cuda.get_device_properties(local).multi_processor_count
@@ -466,6 +480,7 @@ def run_track(args):
         "e2e": {"value": rays / (float(np.mean(tot)) * 1e-3) / 1e6, "unit": UNIT,
                 "h2d_bytes_per_step": int(st["h2d_bytes"]), "d2h_bytes_per_step": int(rays * 12)},
         "gpu_launches": args.steps * 2, "clocks": clk, "cpu_baseline": cpu,
+        "variants": variants,
     }
     print(json.dumps(line))
     ctx.close()
