@@ -72,8 +72,10 @@ __global__ void __launch_bounds__(128, ORD == 4 ? ST_MINB : ST_MINB_ADAPTIVE) tr
     }
     init_ray<PREC, KERR, SEM>(p, cam, i, j, st);
     st.pix = base + j * p.width + i;
-    while (!step_ray<PREC, KERR, VOL, SEM, ORD, DEPTH>(p, st)) {
-    }
+    if (final_at_launch<SEM>(p, st.flags)) st.flags |= ST_RAY_CAPTURED;
+    else
+      while (!step_ray<PREC, KERR, VOL, SEM, ORD, DEPTH>(p, st)) {
+      }
     finish_ray<PREC, KERR, SEM, DEPTH>(p, st, st.pix, p.frames ? st.pix : j * p.width + i);
     steps = st.steps; f64 = st.fp64_steps; gas = st.gas; rays = 1;
   }
@@ -135,7 +137,8 @@ __global__ void __launch_bounds__(128, ST_MINB) trace_persistent_kernel(const __
       continue;
     }
     if (active) {
-      bool fin = false;
+      bool fin = final_at_launch<SEM>(p, st.flags);
+      if (fin) st.flags |= ST_RAY_CAPTURED;
       for (int s = 0; s < p.chunk_steps && !fin; ++s) fin = step_ray<PREC, KERR, VOL, SEM>(p, st);
       if (fin) {
         finish_ray<PREC, KERR, SEM>(p, st, out_idx, out_idx);

@@ -484,6 +484,16 @@ __device__ __forceinline__ void flush_bucket(const TraceParams& p, int pix, R el
   acc[0] = R(0); acc[1] = R(0); acc[2] = R(0);
 }
 
+// A DRAFT ray the Bardeen launch test proves captured is black whatever its
+// integration does (the classification of src/metal.jl:1633-1636); with neither
+// disc nor gas in the scene there is nothing for it to collect on the way in,
+// so its pixel is final at launch and the integration is skipped.
+template <int SEM>
+__device__ __forceinline__ bool final_at_launch(const TraceParams& p, int flags) {
+  if constexpr (SEM != ST_SEM_DRAFT) return false;
+  return (flags & ST_RAY_BCAPT) && !p.disc_on && !p.vol_on && !p.layer;
+}
+
 // Internal ray flag of the layer pass: the fan proves the ray misses the gate.
 constexpr int ST_RAY_LAYER_CULLED = 1 << 20;
 

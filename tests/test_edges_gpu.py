@@ -74,3 +74,23 @@ def test_arguments_the_reference_rejects(built_lib, sky):
         # the context is still usable afterwards
         ok = ctx.render_raw(w.cam, w.bh, ctx.params(_abi.ST_SEM_DRAFT, width=8, height=8))
         assert np.isfinite(ok.image).all()
+
+
+def test_captured_rays_finish_at_launch_without_matter(built_lib, sky):
+    """With neither disc nor gas, a ray the Bardeen launch test proves captured
+    is black whatever its integration does and collects nothing, so the kernel
+    finishes it at launch: its pixel is black with zero steps, and the frame
+    still matches the FP64 twin (which integrates every ray) at the parity
+    tolerance."""
+    w = workloads.config1_nogas().scaled(96, 54)
+    w.params = dict(samples=1, pixel_jitter=0, exit_landing=1)
+    g = gpu_render(w, sky, FP64)
+    bcapt = (g.diag["flags"] & _abi.ST_RAY_BCAPT) > 0
+    assert bcapt.sum() > 100
+    assert np.all(g.diag["steps"][bcapt] == 0)
+    assert np.all(g.image[bcapt] == 0.0)
+    ref, rays = oracle_scene(w, sky, O.INT_RK4).render()
+    assert np.all(rays["steps"][bcapt] > 0)            # the twin integrates them
+    c = compare(g.image, g.diag, ref, rays)
+    assert c["class_mismatch"] == 0, c
+    assert c["dir_median"] <= 1e-9 and c["rad_p99"] <= 1e-5, c
