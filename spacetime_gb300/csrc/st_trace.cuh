@@ -103,10 +103,11 @@ __device__ __forceinline__ void rhs_schw(const R* s, R pt, R M, R* d) {
 
 // Kerr-Schild r^2 from the implicit quartic, in float (the form both the
 // RHS and the step's kill test use, so a step can pass it to its first RHS).
+// With w/2 = (x^2 + y^2 + z^2 - a^2)/2 the root is w/2 + sqrt((w/2)^2 + a^2 z^2).
 __device__ __forceinline__ float ks_r2_f32(float x, float y, float z, float a) {
   const float a2 = a * a, z2 = z * z;
-  const float w = fmaf(x, x, fmaf(y, y, z2)) - a2;
-  return 0.5f * (w + sqrtf(fmaf(w, w, 4.f * (a2 * z2))));
+  const float wh = fmaf(fmaf(x, x, fmaf(y, y, z2)), 0.5f, -(0.5f * a2));
+  return wh + sqrtf(fmaf(wh, wh, a2 * z2));
 }
 
 template <typename R>
@@ -118,15 +119,18 @@ __device__ __forceinline__ R ks_r2(R x, R y, R z, R a) {
 }
 
 // Kerr in float: the same Hamiltonian derivatives regrouped to share their
-// products (about a fifth fewer multiplies than the term-by-term form).
-// With N = (r x + a y, r y - a x), A = p_x x + p_y y and B = p_x y - p_y x:
-//   L.p           = (r A + a B) / (r^2 + a^2) + z p_z / r
-//   d(L.p)/dr     = ((a^2 - r^2) A - 2 r a B) / (r^2 + a^2)^2 - z p_z / r^2
+// products (about a quarter fewer multiplies than the term-by-term form).
+// With A = p_x x + p_y y, B = p_x y - p_y x, T = (r A + a B)/(r^2 + a^2) and
+// Z = z p_z / r:
+//   l = L.p - p_t = T + Z - p_t
+//   dl/dr         = (A - 2 r T)/(r^2 + a^2) - Z / r
+//   dx_xy         = p_xy - f l / (r^2 + a^2) (r x + a y, r y - a x)
 //   dp_xy         = G r^3/Sigma (x, y) + f l / (r^2 + a^2) (r p_x - a p_y, r p_y + a p_x)
-//   dp_z          = G z r (r^2 + a^2) / Sigma + l^2/2 df/dz + f l p_z / r
-// where G = l^2/2 df/dr + f l d(L.p)/dr collects every term along grad r, and
-// the f derivatives are taken from f itself: df/dr = (f/r)(3 a^2 z^2 - r^4)/Sigma,
-// df/dz = -2 a^2 z f / Sigma.
+//   dp_z          = z/Sigma (G r (r^2 + a^2) - a^2 l (f l)) + f l p_z / r
+// where G = l^2/2 df/dr + f l dl/dr collects every term along grad r.  The f
+// derivatives come from f itself: df/dr = (f/r)(3 a^2 z^2 - r^4)/Sigma, and
+// since Sigma = r^4 + a^2 z^2, (3 a^2 z^2 - r^4)/Sigma = 4 a^2 z^2/Sigma - 1,
+// so G = f l (dl/dr + (l/r)(2 a^2 z^2/Sigma - 1/2)); df/dz = -2 a^2 z f/Sigma.
 // r2_known: this state's ks_r2_f32 when the caller has it, else negative.
 __device__ __forceinline__ void rhs_kerr_f32(const float* s, float pt, float M, float a, float* d,
                                              float r2_known = -1.f) {
@@ -137,32 +141,29 @@ __device__ __forceinline__ void rhs_kerr_f32(const float* s, float pt, float M, 
   r2 = fmaxf(r2, 1e-12f);
   float r, ir;
   r_and_inv(r2, r, ir);
-  const float r3 = r2 * r;
   const float isig = rcp_(fmaf(r2, r2, q));
   const float r2a = r2 + a2;
   const float ira = rcp_(r2a);
   const float A = fmaf(px, x, py * y);
   const float B = fmaf(px, y, -(py * x));
-  const float zpz = z * pz;
-  const float ell = fmaf(fmaf(r, A, a * B), ira, fmaf(zpz, ir, -pt));
-  const float rsig = r3 * isig;
-  const float fl = (2.f * M) * rsig * ell;
+  const float T = fmaf(r, A, a * B) * ira;
+  const float Z = (z * pz) * ir;
+  const float ell = (T + Z) - pt;
+  const float rsig = (r2 * r) * isig;
+  const float fl = ((2.f * M) * rsig) * ell;
   const float Fi = fl * ira;
+  const float Fr = Fi * r, Fa = Fi * a;
   const float flir = fl * ir;
-  d[0] = fmaf(-Fi, fmaf(r, x, a * y), px);
-  d[1] = fmaf(-Fi, fmaf(r, y, -(a * x)), py);
+  d[0] = fmaf(-Fr, x, fmaf(-Fa, y, px));
+  d[1] = fmaf(-Fr, y, fmaf(Fa, x, py));
   d[2] = fmaf(-flir, z, pz);
-  // l^2/2 df/dr = (l/2) (f l / r) (3 a^2 z^2 - r^4) / Sigma, since
-  // df/dr = (f / r) (3 a^2 z^2 - r^4) / Sigma
-  const float hd = (0.5f * ell) * flir * fmaf(3.f, q, -(r2 * r2)) * isig;
-  const float dldr = fmaf(-zpz, ir * ir, fmaf(a2 - r2, A, -((2.f * a) * r * B)) * (ira * ira));
-  const float G = fmaf(fl, dldr, hd);
+  const float dldr = fmaf(fmaf(-2.f * r, T, A), ira, -(Z * ir));
+  const float inner = fmaf(ell * ir, fmaf(q + q, isig, -0.5f), dldr);
+  const float G = fl * inner;
   const float Gr = G * rsig;
-  d[3] = fmaf(Gr, x, Fi * fmaf(r, px, -(a * py)));
-  d[4] = fmaf(Gr, y, Fi * fmaf(r, py, a * px));
-  // G dr/dz + l^2/2 df/dz + f l p_z / r, with dr/dz = z r (r^2 + a^2) / Sigma and
-  // l^2/2 df/dz = -a^2 z l (f l) / Sigma
-  d[5] = fmaf(z, fmaf(G * r, r2a, -((a2 * ell) * fl)) * isig, flir * pz);
+  d[3] = fmaf(Gr, x, fmaf(Fr, px, -(Fa * py)));
+  d[4] = fmaf(Gr, y, fmaf(Fr, py, Fa * px));
+  d[5] = fmaf(z * isig, fmaf(G * r, r2a, -((a2 * ell) * fl)), flir * pz);
 }
 
 // Kerr, src/metal.jl:466-508 (implicit-quartic r, four derivative terms).
