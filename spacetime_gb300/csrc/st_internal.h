@@ -139,6 +139,12 @@ struct TraceParams {
     float vol_sr, vol_sp, vol_sz;
     // blackbody table index scale (lut_size - 1) / (lut_tmax - lut_tmin)
     float lut_sc;
+    // Kerr step shrink: rkill2 / max(rkill2, 1e-6), 0.12 dt, 0.88 dt
+    float rkill_n, dt_lo, dt_span;
+    // gas grid radial coordinate from log2 s: vol_sr ln 2, -ls_in vol_sr, nr - 1
+    float vol_sr2, vol_r0, vol_rmax;
+    // gas emission: 1 / (2M), 100 emis, opac ds_gas log2(e)
+    float inv_2m, emis100, opds_l2;
   } f;
 };
 
@@ -176,6 +182,17 @@ inline void fill_float_copies(TraceParams* p) {
   p->f.vol_sp = (float)(p->nphi / 6.283185307179586);
   p->f.vol_sz = p->zmax > 0.0 ? (float)((p->nz - 1) / (2.0 * p->zmax)) : 0.f;
   p->f.lut_sc = p->lut_tmax > p->lut_tmin ? (float)((p->lut_size - 1) / (p->lut_tmax - p->lut_tmin)) : 0.f;
+  const double rkd = p->rkill2 > 1e-6 ? p->rkill2 : 1e-6;
+  p->f.rkill_n = (float)(p->rkill2 / rkd);
+  p->f.dt_lo = (float)(0.12 * p->dt);
+  p->f.dt_span = (float)(0.88 * p->dt);
+  const double sr = p->ls_out > p->ls_in ? (p->nr - 1) / (p->ls_out - p->ls_in) : 0.0;
+  p->f.vol_sr2 = (float)(sr * 0.6931471805599453);
+  p->f.vol_r0 = (float)(-p->ls_in * sr);
+  p->f.vol_rmax = (float)(p->nr - 1);
+  p->f.inv_2m = (float)(1.0 / (2.0 * p->M));
+  p->f.emis100 = (float)(100.0 * p->emis);
+  p->f.opds_l2 = (float)(p->opac * p->ds_gas * 1.4426950408889634);
 }
 
 // Variant key of the compiled kernels (the reference's Val{...} switches,

@@ -36,6 +36,20 @@ __device__ __forceinline__ float rcp_(float x) {
   return r;
 }
 __device__ __forceinline__ double rcp_(double x) { return 1.0 / x; }
+// MUFU base-2 exponential and logarithm (PTX ex2 / lg2 .approx.ftz), for the
+// float units' emission terms written in base 2
+__device__ __forceinline__ float ex2_(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float lg2_(float x) {
+  float r;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+// log2(e), for the base-2 forms of exp(c x)
+constexpr double kLog2e = 1.4426950408889634;
 __device__ __forceinline__ float exp_(float x) { return expf(x); }
 __device__ __forceinline__ double exp_(double x) { return exp(x); }
 __device__ __forceinline__ float log_(float x) { return logf(x); }
@@ -303,6 +317,7 @@ __device__ __forceinline__ R emitter_opz(R sx, R sy, R psx, R psy, R E, R M, R a
   const R sqM = sqrt_(M), sqr = sqrt_(r), r32 = r * sqr;
   const R delta = r * r - R(2) * M * r + a2;
   R ut, uphi, ur = R(0);
+  R ux, uy;
   if (r >= r_isco) {
     const R den = r32 - R(3) * M * sqr + R(2) * a * sqM;
     if constexpr (IsD<R>::v) {
@@ -315,6 +330,10 @@ __device__ __forceinline__ R emitter_opz(R sx, R sy, R psx, R psy, R E, R M, R a
       ut = (r32 + a * sqM) * inv;
       uphi = sqM * inv;
     }
+    // circular orbit: u^r = 0, so the radial basis vector drops out exactly
+    // (0 * cos(phi) - y u^phi rounds as -y u^phi)
+    ux = -(sy * uphi);
+    uy = sx * uphi;
   } else {
     const R inv_d = R(1) / max_(delta, R(1e-3));
     ut = ((r * r + a2 + R(2) * M * a2 / r) * E_isco - R(2) * M * a * L_isco / r) * inv_d;
@@ -325,12 +344,12 @@ __device__ __forceinline__ R emitter_opz(R sx, R sy, R psx, R psy, R E, R M, R a
     ur = -sqrt_(max_(Rr, R(0))) / (r * r);
     ut += R(2) * M * r * inv_d * ur;
     uphi += a * inv_d * ur;
+    const R inv_s2 = R(1) / max_(s2, R(1e-6));
+    const R cphi = (r * sx + a * sy) * inv_s2;
+    const R sphi = (r * sy - a * sx) * inv_s2;
+    ux = ur * cphi - sy * uphi;
+    uy = ur * sphi + sx * uphi;
   }
-  const R inv_s2 = R(1) / max_(s2, R(1e-6));
-  const R cphi = (r * sx + a * sy) * inv_s2;
-  const R sphi = (r * sy - a * sx) * inv_s2;
-  const R ux = ur * cphi - sy * uphi;
-  const R uy = ur * sphi + sx * uphi;
   const R Es = fabs_(E) > R(1e-6) ? E : R(1e-6);
   return clamp_(ut - (psx * ux + psy * uy) / Es, R(0.1), R(20));
 }
@@ -357,21 +376,27 @@ template <typename R>
 __device__ __forceinline__ R sample_volume(const TraceParams& p, R sc, R phi, R z) {
   const R zmax = PR(zmax);
   if (sc <= R(0) || fabs_(z) >= zmax) return R(0);
-  const R ls = log_(sc);
-  const R lin = PR(ls_in), lout = PR(ls_out);
-  if (ls <= lin || ls >= lout) return R(0);
+  R fr, fp, fz;
+  if constexpr (IsD<R>::v) {
+    const R ls = log_(sc);
+    const R lin = PR(ls_in), lout = PR(ls_out);
+    if (ls <= lin || ls >= lout) return R(0);
+    fr = (ls - lin) / (lout - lin) * R(p.nr - 1);
+  } else {
+    // (ln s - ln s_in) (nr - 1) / (ln s_out - ln s_in) from log2 s, with the
+    // scale and offset from the host; inside the grid iff 0 < fr < nr - 1
+    fr = fmaf(lg2_(sc), p.f.vol_sr2, p.f.vol_r0);
+    if (!(fr > 0.f && fr < p.f.vol_rmax)) return R(0);
+  }
   const int nr = p.nr, nphi = p.nphi, nz = p.nz;
   const R two_pi = R(6.283185307179586);
   // phi comes from atan2, so |phi| <= pi and mod(phi, 2 pi) is one conditional add
   R pm = phi;
   if (pm < R(0)) pm += two_pi;
-  R fr, fp, fz;
   if constexpr (IsD<R>::v) {
-    fr = (ls - lin) / (lout - lin) * R(nr - 1);
     fp = pm / two_pi * R(nphi);
     fz = (z + zmax) / (R(2) * zmax) * R(nz - 1);
-  } else {  // the three scales come from the host: no division per sample
-    fr = (ls - lin) * p.f.vol_sr;
+  } else {  // the scales come from the host: no division per sample
     fp = pm * p.f.vol_sp;
     fz = (z + zmax) * p.f.vol_sz;
   }
@@ -889,18 +914,34 @@ __device__ __forceinline__ bool march_gas(const TraceParams& p, const R* yp, con
         R rho = sample_volume(p, scyl, phi, sz);
         ++st.gas;
         if (rho > R(1e-4)) {
-          const R Rr = max_(scyl, r_isco) / (R(2) * M);
-          const R T_emit = exp_(R(10.034259) - R(0.375) * log_(max_(Rr * Rr, R(1e-6))));
+          R T_emit;
+          if constexpr (IsD<R>::v) {
+            const R Rr = max_(scyl, r_isco) / (R(2) * M);
+            T_emit = exp_(R(10.034259) - R(0.375) * log_(max_(Rr * Rr, R(1e-6))));
+          } else {
+            // base 2: exp(c - 0.375 ln Rr^2) = 2^(c log2(e) - 0.75 log2 Rr)
+            const float Rr = fmaxf(scyl, r_isco) * p.f.inv_2m;
+            T_emit = ex2_(fmaf(-0.75f, lg2_(fmaxf(Rr, 1e-3f)), float(10.034259 * kLog2e)));
+          }
           if (scyl < r_isco) { const R t3 = scyl / r_isco; rho *= t3 * t3 * t3; }
           const R psx = yp[3] + fs * (yn[3] - yp[3]);
           const R psy = yp[4] + fs * (yn[4] - yp[4]);
           const R opz = emitter_opz(sx, sy, psx, psy, -st.pt, M, PR(a), r_isco, PR(E_isco), PR(L_isco));
           const R T_obs = T_emit * st.scam / opz;
-          const R inten = R(100) / (exp_(R(29622.4) / max_(T_obs, R(1))) - R(1));
           const float4 col = lut_color(p, T_obs, false);
-          const R tau = PR(opac) * rho * ds;
-          const R aa = R(1) - exp_(-tau);
-          const R w = st.alpha * aa * inten * PR(emis);
+          R aa, w;
+          if constexpr (IsD<R>::v) {
+            const R inten = R(100) / (exp_(R(29622.4) / max_(T_obs, R(1))) - R(1));
+            const R tau = PR(opac) * rho * ds;
+            aa = R(1) - exp_(-tau);
+            w = st.alpha * aa * inten * PR(emis);
+          } else {
+            // 100 emis / (exp(29622.4 / T) - 1) and 1 - exp(-opac rho ds) in base 2,
+            // the products of constants from the host
+            const float inte = p.f.emis100 * rcp_(ex2_(float(29622.4 * kLog2e) * rcp_(fmaxf(T_obs, 1.f))) - 1.f);
+            aa = 1.f - ex2_(-(rho * p.f.opds_l2));
+            w = st.alpha * aa * inte;
+          }
           st.acc[0] += w * R(col.x); st.acc[1] += w * R(col.y); st.acc[2] += w * R(col.z);
           st.alpha *= (R(1) - aa);
         }
@@ -1106,14 +1147,23 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
   // radius-adaptive step, src/metal.jl:1250-1260
   const R cap = (VOL && r2 < PR(vol_rb2)) ? R(2) : PR(hcap);
   R h;
-  if constexpr (IsD<R>::v) h = PR(dt) * min_(max_(PR(hcoef) * r / M, R(1)), cap);
-  else h = PR(dt) * min_(max_(p.f.hcoef_m * r, R(1)), cap);
-  if constexpr (KERR) {
-    const R rk = PR(rkill2);
-    R fr;
-    if constexpr (IsD<R>::v) fr = clamp_((rk2 - rk) / max_(rk, R(1e-6)), R(0), R(1));
-    else fr = clamp_((rk2 - rk) * p.f.inv_rkill2, R(0), R(1));
-    h *= R(0.12) + R(0.88) * fr;
+  if constexpr (IsD<R>::v) {
+    h = PR(dt) * min_(max_(PR(hcoef) * r / M, R(1)), cap);
+    if constexpr (KERR) {
+      const R rk = PR(rkill2);
+      const R fr = clamp_((rk2 - rk) / max_(rk, R(1e-6)), R(0), R(1));
+      h *= R(0.12) + R(0.88) * fr;
+    }
+  } else {
+    const float hb = fminf(fmaxf(p.f.hcoef_m * r, 1.f), cap);
+    if constexpr (KERR) {
+      // dt (0.12 + 0.88 clamp((rk2 - rkill2) / rkill2, 0, 1)): one saturated
+      // multiply-add, dt folded into the host's 0.12 dt and 0.88 dt
+      const float fr = __saturatef(fmaf(rk2, p.f.inv_rkill2, -p.f.rkill_n));
+      h = hb * fmaf(p.f.dt_span, fr, p.f.dt_lo);
+    } else {
+      h = PR(dt) * hb;
+    }
   }
   if constexpr (SEM == ST_SEM_RENDER) h = min_(h, PR(tspan) - st.lambda);
 
