@@ -245,7 +245,9 @@ int st_context_create(st_context** out, const float* sky_rgb, int sky_w, int sky
  * context starts with Blackbody() defaults: 6500 K white point, 500-30000 K,
  * 1024 entries). */
 int st_context_set_disc(st_context* ctx, const st_disc* disc);
-/* NULL disables the volume; the density grid is copied to HBM. */
+/* NULL disables the volume; the density grid is copied to HBM.  ST_EINVAL for
+ * nr < 2, nphi < 1, nz < 2, log_s_out <= log_s_in, z_max <= 0 or a grid of
+ * 2^31 cells or more. */
 int st_context_set_volume(st_context* ctx, const st_volume* vol);
 /* set_starfield! defaults: strength 1, texture_weight 0, height 1080,
  * fov_factor 0.55, density 384, fill 0.5, flux 0.011, psf_pixels 0.5,

@@ -1239,6 +1239,7 @@ int st_context_set_volume(st_context* ctx, const st_volume* v) {
   if (!v->density || v->nr < 2 || v->nphi < 1 || v->nz < 2) return ST_EINVAL;
   if (!(v->log_s_out > v->log_s_in) || !(v->z_max > 0.0f)) return ST_EINVAL;
   const size_t n = (size_t)v->nr * v->nphi * v->nz;
+  if (n >= ((size_t)1 << 31)) return ST_EINVAL;  // the float sampler indexes the grid in 32 bits
   if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
   if (ctx->d_vol && ctx->vol_bytes != n * sizeof(float)) { cudaFree(ctx->d_vol); ctx->d_vol = nullptr; }
   if (!ctx->d_vol && cudaMalloc(&ctx->d_vol, n * sizeof(float)) != cudaSuccess) return ST_ENOMEM;

@@ -94,6 +94,7 @@ extern "C" int st_render_frames_noalloc(const float* dev_sky_rgba, int sky_w, in
   const int lut_n = (disc && disc->table_size > 0) ? disc->table_size : 1024;
   if (lut_n > NOALLOC_MAX_LUT || lut_n < 2) return ST_ELIMIT;
   if (vol && (!dev_density || vol->nr < 2 || vol->nphi < 1 || vol->nz < 2)) return ST_EINVAL;
+  if (vol && (size_t)vol->nr * vol->nphi * vol->nz >= ((size_t)1 << 31)) return ST_EINVAL;  // 32-bit grid offsets
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return ST_ECUDA;
   // one-time set-up per device (the first call on a device: keep it outside

@@ -374,56 +374,85 @@ __device__ __forceinline__ float4 lut_color(const TraceParams& p, R T, bool rend
 // Trilinear gas density, src/metal.jl:569-610.
 template <typename R>
 __device__ __forceinline__ R sample_volume(const TraceParams& p, R sc, R phi, R z) {
-  const R zmax = PR(zmax);
-  if (sc <= R(0) || fabs_(z) >= zmax) return R(0);
-  R fr, fp, fz;
-  if constexpr (IsD<R>::v) {
+  const int nr = p.nr, nphi = p.nphi, nz = p.nz;
+  const float* v = p.vol;
+  if constexpr (!IsD<R>::v) {
+    // The gas march calls this with sc > 1e-6 and |z| < zmax already checked.
+    // (ln s - ln s_in) (nr - 1) / (ln s_out - ln s_in) from log2 s, with the
+    // scale and offset from the host; inside the grid iff 0 < fr < nr - 1, so
+    // floor(fr) lies in [0, nr - 2] with no clamp.
+    const float fr = fmaf(lg2_(sc), p.f.vol_sr2, p.f.vol_r0);
+    if (!(fr > 0.f && fr < p.f.vol_rmax)) return 0.f;
+    const float flr = floorf(fr);
+    const int i0 = (int)flr;
+    const float tr = fr - flr;
+    // phi comes from atan2: |phi| <= pi, so mod(phi, 2 pi) is one conditional
+    // add, fp lies in [0, nphi] and its floor wraps by one compare
+    const float pm = phi < 0.f ? phi + 6.283185307179586f : phi;
+    const float fp = pm * p.f.vol_sp;
+    const float flp = floorf(fp);
+    const int j0 = (int)flp;
+    const float tp = fp - flp;
+    const int ja = j0 >= nphi ? j0 - nphi : j0;
+    const int jb = ja + 1 >= nphi ? 0 : ja + 1;
+    // z + zmax > 0, so only the upper end needs the clamp
+    const float fz = (z + PR(zmax)) * p.f.vol_sz;
+    const int k0 = min((int)floorf(fz), nz - 2);
+    const float tz = fz - (float)k0;
+    // 32-bit offsets (the context limits the grid to 2^31 cells)
+    const int sk = nr * nphi;
+    const int base = i0 + sk * k0;
+    const float* v00 = v + (base + nr * ja);
+    const float* v10 = v + (base + nr * jb);
+    const float* v01 = v00 + sk;
+    const float* v11 = v10 + sk;
+    const float d000 = __ldg(v00), d100 = __ldg(v00 + 1);
+    const float d010 = __ldg(v10), d110 = __ldg(v10 + 1);
+    const float d001 = __ldg(v01), d101 = __ldg(v01 + 1);
+    const float d011 = __ldg(v11), d111 = __ldg(v11 + 1);
+    const float c00 = d000 + tr * (d100 - d000);
+    const float c10 = d010 + tr * (d110 - d010);
+    const float c01 = d001 + tr * (d101 - d001);
+    const float c11 = d011 + tr * (d111 - d011);
+    const float c0 = c00 + tp * (c10 - c00);
+    const float c1 = c01 + tp * (c11 - c01);
+    return c0 + tz * (c1 - c0);
+  } else {
+    const R zmax = PR(zmax);
+    if (sc <= R(0) || fabs_(z) >= zmax) return R(0);
     const R ls = log_(sc);
     const R lin = PR(ls_in), lout = PR(ls_out);
     if (ls <= lin || ls >= lout) return R(0);
-    fr = (ls - lin) / (lout - lin) * R(p.nr - 1);
-  } else {
-    // (ln s - ln s_in) (nr - 1) / (ln s_out - ln s_in) from log2 s, with the
-    // scale and offset from the host; inside the grid iff 0 < fr < nr - 1
-    fr = fmaf(lg2_(sc), p.f.vol_sr2, p.f.vol_r0);
-    if (!(fr > 0.f && fr < p.f.vol_rmax)) return R(0);
+    const R two_pi = R(6.283185307179586);
+    R pm = phi;
+    if (pm < R(0)) pm += two_pi;
+    const R fr = (ls - lin) / (lout - lin) * R(nr - 1);
+    const R fp = pm / two_pi * R(nphi);
+    const R fz = (z + zmax) / (R(2) * zmax) * R(nz - 1);
+    const int i0 = min(max((int)floor_(fr), 0), nr - 2);
+    const R tr = fr - R(i0);
+    const int j0 = (int)floor_(fp);
+    const R tp = fp - R(j0);
+    const int k0 = min(max((int)floor_(fz), 0), nz - 2);
+    const R tz = fz - R(k0);
+    // j0 is in [0, nphi] (fp < nphi up to rounding): wrap by compare, not by division
+    const int ja = j0 >= nphi ? j0 - nphi : (j0 < 0 ? j0 + nphi : j0);
+    const int jb = ja + 1 >= nphi ? ja + 1 - nphi : ja + 1;
+    const size_t sj = (size_t)nr, sk = (size_t)nr * nphi;
+    const size_t b00 = (size_t)i0 + sj * ja + sk * k0, b10 = (size_t)i0 + sj * jb + sk * k0;
+    const size_t b01 = b00 + sk, b11 = b10 + sk;
+    const R d000 = __ldg(v + b00), d100 = __ldg(v + b00 + 1);
+    const R d010 = __ldg(v + b10), d110 = __ldg(v + b10 + 1);
+    const R d001 = __ldg(v + b01), d101 = __ldg(v + b01 + 1);
+    const R d011 = __ldg(v + b11), d111 = __ldg(v + b11 + 1);
+    const R c00 = d000 + tr * (d100 - d000);
+    const R c10 = d010 + tr * (d110 - d010);
+    const R c01 = d001 + tr * (d101 - d001);
+    const R c11 = d011 + tr * (d111 - d011);
+    const R c0 = c00 + tp * (c10 - c00);
+    const R c1 = c01 + tp * (c11 - c01);
+    return c0 + tz * (c1 - c0);
   }
-  const int nr = p.nr, nphi = p.nphi, nz = p.nz;
-  const R two_pi = R(6.283185307179586);
-  // phi comes from atan2, so |phi| <= pi and mod(phi, 2 pi) is one conditional add
-  R pm = phi;
-  if (pm < R(0)) pm += two_pi;
-  if constexpr (IsD<R>::v) {
-    fp = pm / two_pi * R(nphi);
-    fz = (z + zmax) / (R(2) * zmax) * R(nz - 1);
-  } else {  // the scales come from the host: no division per sample
-    fp = pm * p.f.vol_sp;
-    fz = (z + zmax) * p.f.vol_sz;
-  }
-  const int i0 = min(max((int)floor_(fr), 0), nr - 2);
-  const R tr = fr - R(i0);
-  const int j0 = (int)floor_(fp);
-  const R tp = fp - R(j0);
-  const int k0 = min(max((int)floor_(fz), 0), nz - 2);
-  const R tz = fz - R(k0);
-  // j0 is in [0, nphi] (fp < nphi up to rounding): wrap by compare, not by division
-  const int ja = j0 >= nphi ? j0 - nphi : (j0 < 0 ? j0 + nphi : j0);
-  const int jb = ja + 1 >= nphi ? ja + 1 - nphi : ja + 1;
-  const float* v = p.vol;
-  const size_t sj = (size_t)nr, sk = (size_t)nr * nphi;
-  const size_t b00 = (size_t)i0 + sj * ja + sk * k0, b10 = (size_t)i0 + sj * jb + sk * k0;
-  const size_t b01 = b00 + sk, b11 = b10 + sk;
-  const R d000 = __ldg(v + b00), d100 = __ldg(v + b00 + 1);
-  const R d010 = __ldg(v + b10), d110 = __ldg(v + b10 + 1);
-  const R d001 = __ldg(v + b01), d101 = __ldg(v + b01 + 1);
-  const R d011 = __ldg(v + b11), d111 = __ldg(v + b11 + 1);
-  const R c00 = d000 + tr * (d100 - d000);
-  const R c10 = d010 + tr * (d110 - d010);
-  const R c01 = d001 + tr * (d101 - d001);
-  const R c11 = d011 + tr * (d111 - d011);
-  const R c0 = c00 + tp * (c10 - c00);
-  const R c1 = c01 + tp * (c11 - c01);
-  return c0 + tz * (c1 - c0);
 }
 
 // Bilinear equirectangular sky, src/metal.jl:523-561 / src/raytrace.jl:154-177.

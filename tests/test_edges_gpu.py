@@ -6,8 +6,11 @@
   (radiance p99 <= 1e-5), for both schedules.
 - Arguments the reference rejects come back as ST_EINVAL without touching
   the device: sizes <= 0 or beyond 2^30 pixels, samples <= 0, dt <= 0,
-  |a| > M (src/gr.jl:31), an unknown integrator order.
+  |a| > M (src/gr.jl:31), an unknown integrator order; and a gas grid of
+  2^31 cells or more (the float sampler indexes the grid in 32 bits), which
+  is refused before its density pointer is read.
 """
+import ctypes as C
 import types
 
 import numpy as np
@@ -71,6 +74,11 @@ def test_arguments_the_reference_rejects(built_lib, sky):
         assert code(bh=types.SimpleNamespace(M=1.0, a=1.5)) == _abi.ST_EINVAL   # past the C ABI
         with pytest.raises(ValueError):
             Kerr(1.0, 1.5)                                                    # and in the Python API
+        # a gas grid of 2^31 cells: refused before the (one-cell) buffer is read
+        cell = np.zeros(1, np.float32)
+        big = _abi.StVolume(cell.ctypes.data_as(C.POINTER(C.c_float)), 1 << 16, 1 << 10, 1 << 5,
+                            1.0, 3.0, 1.0, 1.0, 1.0, 2)
+        assert ctx._lib.st_context_set_volume(ctx._h, C.byref(big)) == _abi.ST_EINVAL
         # the context is still usable afterwards
         ok = ctx.render_raw(w.cam, w.bh, ctx.params(_abi.ST_SEM_DRAFT, width=8, height=8))
         assert np.isfinite(ok.image).all()
