@@ -106,7 +106,9 @@ __device__ __forceinline__ void rhs_schw(const R* s, R pt, R M, R* d) {
   const R kap = (x * px + y * py + z * pz) * inv_r;
   const R ell = -pt + kap;
   const R c1 = f * ell * inv_r;
-  const R c2 = f * ell * (R(0.5) * ell + kap) * inv_r * inv_r;
+  R c2;
+  if constexpr (IsD<R>::v) c2 = f * ell * (R(0.5) * ell + kap) * inv_r * inv_r;
+  else c2 = c1 * fmaf(0.5f, ell, kap) * inv_r;  // the same product, sharing c1
   d[0] = px - c1 * x;
   d[1] = py - c1 * y;
   d[2] = pz - c1 * z;
