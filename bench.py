@@ -377,8 +377,8 @@ def fluid_variant(ctx_cls, device: int, steps: int = 200) -> dict:
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum of the 1920x1080 config-1 FP32 launch
-# (26.14 MB read, 0.07 MB written; profiles/trace_fp32_kerr_gas_1080p_dram.md)
-TRACE_1080P_DRAM_BYTES = 26_140_160 + 71_424
+# (26.27 MB read, 0.12 MB written; profiles/trace_fp32_kerr_gas_1080p_dram.md)
+TRACE_1080P_DRAM_BYTES = 26_271_744 + 124_672
 
 
 def run_reference(args):
