@@ -4,6 +4,10 @@
   no multiple of the 16x8 tile or of the 8x4 persistent tile) render every
   pixel and agree with the oracle's FP64 twin at the parity tolerance
   (radiance p99 <= 1e-5), for both schedules.
+- The smallest gas grids (one radial cell, an azimuth of one or two cells that
+  wraps onto itself, one vertical cell) render in FP32 and agree with the
+  oracle's FP64 twin (radiance median <= 1e-4, class mismatches <= 1 %): the
+  float sampler's index math at its limits.
 - Arguments the reference rejects come back as ST_EINVAL without touching
   the device: sizes <= 0 or beyond 2^30 pixels, samples <= 0, dt <= 0,
   |a| > M (src/gr.jl:31), an unknown integrator order; and a gas grid of
@@ -102,3 +106,19 @@ def test_captured_rays_finish_at_launch_without_matter(built_lib, sky):
     c = compare(g.image, g.diag, ref, rays)
     assert c["class_mismatch"] == 0, c
     assert c["dir_median"] <= 1e-9 and c["rad_p99"] <= 1e-5, c
+
+
+@pytest.mark.parametrize("shape", [(2, 1, 2), (3, 2, 3), (5, 3, 2)])
+def test_smallest_gas_grids_fp32(built_lib, sky, shape):
+    nr, nphi, nz = shape
+    w = workloads.config1().scaled(128, 72)
+    w.vol = workloads.volume(nr, nphi, nz, 2.32, 25.0, 0.05)
+    g = gpu_render(w, sky, _abi.ST_PREC_FP32)
+    assert g.stats["gas_samples"] > 0
+    assert np.isfinite(g.image).all()
+    ref, rays = oracle_scene(w, sky, O.INT_RK4).render()
+    c = compare(g.image, g.diag, ref, rays)
+    print(shape, c)
+    assert c["class_mismatch"] <= 0.01 * c["n"], c
+    assert c["rad_median"] <= 1e-4, c   # measured 0.6e-6 .. 3e-6
+
