@@ -434,16 +434,17 @@ int st_context_set_surrogate(st_context* ctx, st_surrogate* s);
 
 /* Allocation-free camera-track render.  No counterpart in the reference.
  * For callers that cannot allocate device memory: a renderer embedded in an
- * engine whose device memory belongs to its own pool, a plug-in invoked
- * inside a CUDA graph capture or stream-ordered region where cudaMalloc would
- * break the capture or synchronise the device, a real-time loop that budgets
- * memory up front.  The caller passes its own device buffers: the sky as
+ * engine whose device memory belongs to its own pool, or a real-time loop
+ * that budgets memory up front and cannot afford the device-wide
+ * synchronisation a cudaMalloc brings.  The caller passes its own device buffers: the sky as
  * float4 texels [sky_h][sky_w] (RGB + unused), the gas density (may be NULL
  * with vol NULL) and the output frames, float4 [nframes][height][width]; the
  * kernel's working memory (ray-queue head, counters, per-frame cameras and the
  * blackbody table) lives in a fixed 80 KiB device array of the library, held on
  * every device that loads it until exit.  Limits: nframes <= 64, blackbody
- * table <= 4096 entries (ST_ELIMIT beyond); DRAFT semantics, samples = 1.
+ * table <= 4096 entries (ST_ELIMIT beyond); DRAFT semantics, samples = 1,
+ * RK4, no surrogate (ST_EUNSUPPORTED otherwise); the disc and volume are
+ * checked as st_context_set_disc / st_context_set_volume check them.
  * The first call on a device resolves the array's address with that device
  * current: make that first call before any stream capture.  All calls share
  * the array (queue head and counters are cleared per call): calls whose GPU

@@ -165,7 +165,7 @@ static double cie_g(double lam, double mu, double s1, double s2) {
   const double t = (lam - mu) / s;
   return std::exp(-0.5 * t * t);
 }
-static void host_blackbody(double T, double* rgb) {
+void host_blackbody(double T, double* rgb) {
   double X = 0, Y = 0, Z = 0;
   for (int i = 0; i <= 80; ++i) {
     const double lam = 380.0 + 5.0 * i, lm = lam * 1e-9;
@@ -1486,6 +1486,8 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
   std::memset(p.U, 0, sizeof p.U);
   p.r_escape = 0.0;
   const long long tiles = (long long)((rp->width + 7) / 8) * ((rp->height + 3) / 4);
+  // the queue counts rays of whole 8x4 tiles in a 32-bit int
+  if (tiles * 32 * nframes > (long long)INT_MAX) return ST_EINVAL;
   p.n_rays = (int)(tiles * 32 * nframes);
   p.chunk_steps = rp->chunk_steps > 0 ? rp->chunk_steps : 32;
   p.budget_iters = ((long long)p.n_rays + 32) * ((long long)nmax_max / p.chunk_steps + 2);

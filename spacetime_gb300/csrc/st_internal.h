@@ -254,6 +254,10 @@ cudaError_t launch_composite(int prec, const TraceParams& p, const lay::CompPara
 // Fill a layer with transparency (0, 0, 0, 1).
 cudaError_t launch_fill_transparent(float4* layer, size_t n, cudaStream_t stream);
 
+// The white-balance-free CIE blackbody colour of temperature T, normalised to
+// its largest channel (src/blackbody.jl:15-35); host, double precision.
+void host_blackbody(double T, double* rgb);
+
 // Launch one trace pass; returns a cudaError_t.
 cudaError_t launch_trace(const Variant& v, const TraceParams& p, int block_x, int block_y,
                          int num_sms, cudaStream_t stream);

@@ -4,13 +4,11 @@
 //
 // Who needs it: code that runs inside another runtime's memory discipline --
 // a renderer embedded in a game engine or compositor whose device memory is
-// all owned by its own pool allocator, a plug-in called from inside a CUDA
-// graph capture or a stream-ordered region where cudaMalloc would break the
-// capture or synchronise the device, or a real-time loop that has budgeted its
-// memory up front and treats any allocation as a stall.  Such a caller already
-// owns the sky texels and the output frames; what it cannot provide is the
-// persistent kernel's own working memory, so that lives here, in a fixed
-// file-scope device array.
+// all owned by its own pool allocator, or a real-time loop that has budgeted
+// its memory up front and treats any allocation (cudaMalloc synchronises the
+// device) as a stall.  Such a caller already owns the sky texels and the
+// output frames; what it cannot provide is the persistent kernel's own
+// working memory, so that lives here, in a fixed file-scope device array.
 //
 // The scratch array (NOALLOC_SCRATCH_BYTES, 80 KiB, held on every device that
 // loads the library until the process exits) holds the ray-queue head, the
@@ -18,10 +16,12 @@
 // table of up to NOALLOC_MAX_LUT entries.  All calls share it, and it keeps
 // the previous call's contents: the queue head and counters are cleared on
 // every call.  Calls whose GPU work overlaps (two streams, or two host threads)
-// race on it and must be serialised by the caller.
+// race on it and must be serialised by the caller.  The call is synchronous:
+// it waits for the caller's stream before it returns.
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -50,29 +50,6 @@ static __device__ __align__(256) unsigned char g_scratch[NOALLOC_SCRATCH_BYTES];
 constexpr int MAX_DEVICES = 64;
 void* g_scratch_addr[MAX_DEVICES] = {nullptr};
 
-double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
-
-// The blackbody table (src/blackbody.jl:15-60), float4 entries.
-void blackbody_rgb(double T, double* rgb) {
-  auto cg = [](double lam, double mu, double s1, double s2) {
-    const double s = lam < mu ? s1 : s2, t = (lam - mu) / s;
-    return std::exp(-0.5 * t * t);
-  };
-  double X = 0, Y = 0, Z = 0;
-  for (int i = 0; i <= 80; ++i) {
-    const double lam = 380.0 + 5.0 * i, lm = lam * 1e-9;
-    const double B = 1.0 / (std::pow(lm, 5) * (std::exp(0.014388 / (lm * T)) - 1.0));
-    X += B * (1.056 * cg(lam, 599.8, 37.9, 31.0) + 0.362 * cg(lam, 442.0, 16.0, 26.7) - 0.065 * cg(lam, 501.1, 20.4, 26.2));
-    Y += B * (0.821 * cg(lam, 568.8, 46.9, 40.5) + 0.286 * cg(lam, 530.9, 16.3, 31.1));
-    Z += B * (1.217 * cg(lam, 437.0, 11.8, 36.0) + 0.681 * cg(lam, 459.0, 26.0, 13.8));
-  }
-  const double r = std::fmax(3.2406 * X - 1.5372 * Y - 0.4986 * Z, 0.0);
-  const double g = std::fmax(-0.9689 * X + 1.8758 * Y + 0.0415 * Z, 0.0);
-  const double b = std::fmax(0.0557 * X - 0.2040 * Y + 1.0570 * Z, 0.0);
-  const double m = std::fmax(std::fmax(r, g), std::fmax(b, 1e-10));
-  rgb[0] = r / m; rgb[1] = g / m; rgb[2] = b / m;
-}
-
 }  // namespace
 
 // Tetrad and rule helpers of the regular path (st_api.cu), reused through a
@@ -90,10 +67,14 @@ extern "C" int st_render_frames_noalloc(const float* dev_sky_rgba, int sky_w, in
   if (!dev_sky_rgba || sky_w < 2 || sky_h < 2 || !cams || !stp || !rp || !dev_out_rgba || nframes <= 0)
     return ST_EINVAL;
   if (nframes > NOALLOC_MAX_FRAMES) return ST_ELIMIT;
-  if (rp->semantics != ST_SEM_DRAFT || rp->samples != 1) return ST_EUNSUPPORTED;
+  // the same rule checks as st_render_frames and the context setters
+  if (rp->semantics != ST_SEM_DRAFT || rp->samples != 1 || rp->surrogate) return ST_EUNSUPPORTED;
+  if (rp->order != 0 && rp->order != 4) return ST_EUNSUPPORTED;  // the persistent kernel integrates with RK4
+  if (disc && disc->emitter != ST_EMIT_KEPLER && disc->emitter != ST_EMIT_KS_EXACT) return ST_EINVAL;
   const int lut_n = (disc && disc->table_size > 0) ? disc->table_size : 1024;
   if (lut_n > NOALLOC_MAX_LUT || lut_n < 2) return ST_ELIMIT;
   if (vol && (!dev_density || vol->nr < 2 || vol->nphi < 1 || vol->nz < 2)) return ST_EINVAL;
+  if (vol && (!(vol->log_s_out > vol->log_s_in) || !(vol->z_max > 0.0f))) return ST_EINVAL;
   if (vol && (size_t)vol->nr * vol->nphi * vol->nz >= ((size_t)1 << 31)) return ST_EINVAL;  // 32-bit grid offsets
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return ST_ECUDA;
@@ -113,7 +94,9 @@ extern "C" int st_render_frames_noalloc(const float* dev_sky_rgba, int sky_w, in
   st::TraceParams p;
   int rc = st::fill_frame_params(&cams[0], stp, rp, &p);
   if (rc != ST_OK) return rc;
-  st::FrameCam fc[NOALLOC_MAX_FRAMES];
+  // host staging (host memory is outside the no-device-allocation contract;
+  // kept off the stack, whose size an embedding thread may limit)
+  std::vector<st::FrameCam> fc(nframes);
   int nmax_max = 0;
   for (int f = 0; f < nframes; ++f) {
     st::TraceParams q;
@@ -130,16 +113,16 @@ extern "C" int st_render_frames_noalloc(const float* dev_sky_rgba, int sky_w, in
     nmax_max = q.nmax > nmax_max ? q.nmax : nmax_max;
   }
   // blackbody table into scratch
-  float4 lut[NOALLOC_MAX_LUT];
+  std::vector<float4> lut(lut_n);
   const double tmin = (disc && disc->table_size > 0) ? disc->table_min : 500.0;
   const double tmax = (disc && disc->table_size > 0) ? disc->table_max : 30000.0;
   if (!(tmax > tmin)) return ST_EINVAL;
   {
     double ref[3];
-    blackbody_rgb(disc && disc->wb_temperature > 0.0 ? disc->wb_temperature : 6500.0, ref);
+    st::host_blackbody(disc && disc->wb_temperature > 0.0 ? disc->wb_temperature : 6500.0, ref);
     for (int i = 0; i < lut_n; ++i) {
       double c[3];
-      blackbody_rgb(std::fmax(tmin + (tmax - tmin) * i / (lut_n - 1), 1.0), c);
+      st::host_blackbody(std::fmax(tmin + (tmax - tmin) * i / (lut_n - 1), 1.0), c);
       lut[i] = make_float4((float)(c[0] / ref[0]), (float)(c[1] / ref[1]), (float)(c[2] / ref[2]), 0.f);
     }
   }
@@ -149,9 +132,10 @@ extern "C" int st_render_frames_noalloc(const float* dev_sky_rgba, int sky_w, in
   float4* dlut = reinterpret_cast<float4*>(base + OFF_LUT);
   if (cudaMemsetAsync(counters, 0, st::CNT_N * sizeof(unsigned long long), s) != cudaSuccess) return ST_ECUDA;
   if (cudaMemsetAsync(queue, 0, sizeof(unsigned int), s) != cudaSuccess) return ST_ECUDA;
-  if (cudaMemcpyAsync(frames, fc, nframes * sizeof(st::FrameCam), cudaMemcpyHostToDevice, s) != cudaSuccess)
+  if (cudaMemcpyAsync(frames, fc.data(), nframes * sizeof(st::FrameCam), cudaMemcpyHostToDevice, s) != cudaSuccess)
     return ST_ECUDA;
-  if (cudaMemcpyAsync(dlut, lut, lut_n * sizeof(float4), cudaMemcpyHostToDevice, s) != cudaSuccess) return ST_ECUDA;
+  if (cudaMemcpyAsync(dlut, lut.data(), lut_n * sizeof(float4), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return ST_ECUDA;
 
   // disc, gas, sky and outputs
   p.disc_on = (disc && disc->inner > 0.0 && disc->outer > disc->inner) ? 1 : 0;
@@ -189,6 +173,8 @@ extern "C" int st_render_frames_noalloc(const float* dev_sky_rgba, int sky_w, in
   p.weight = 1.0f;
   p.first_pass = 1;
   const long long tiles = (long long)((rp->width + 7) / 8) * ((rp->height + 3) / 4);
+  // the queue counts rays of whole 8x4 tiles in a 32-bit int
+  if (tiles * 32 * nframes > (long long)INT_MAX) return ST_EINVAL;
   p.n_rays = (int)(tiles * 32 * nframes);
   p.chunk_steps = rp->chunk_steps > 0 ? rp->chunk_steps : 32;
   p.budget_iters = ((long long)p.n_rays + 32) * ((long long)nmax_max / p.chunk_steps + 2);

@@ -1,6 +1,7 @@
 """st_render_frames_noalloc: the camera-track render for callers that cannot
-allocate device memory (engine-owned memory pools, work issued inside a CUDA
-graph capture, real-time loops with a fixed memory budget).
+allocate device memory (engine-owned memory pools, real-time loops with a
+fixed memory budget that cannot take the device-wide synchronisation of an
+allocation).
 
 The caller owns every buffer it passes (here torch allocates them, as the
 calling application would); the library's working memory is its fixed
@@ -95,3 +96,43 @@ def test_noalloc_rejects_over_capacity(built_lib):
     rc, _ = _noalloc(lib, sky_d, sky.shape[1], sky.shape[0], None, None, None, cams, w.bh, p, out_d)
     assert rc == _abi.ST_ELIMIT
     assert b"scratch" in lib.st_strerror(rc)
+
+
+def test_noalloc_rejects_what_the_context_path_rejects(built_lib):
+    """The argument checks of st_render_frames and the context setters: an
+    unknown emitter or an empty gas extent is ST_EINVAL, the surrogate and the
+    adaptive integrators are ST_EUNSUPPORTED -- all before any device work."""
+    import torch
+    lib = _abi.load()
+    w = workloads.config1(nr=8, nphi=4, nz=4)
+    sky = workloads.sky(512, 256)
+    sky_d, dens_d = _device_inputs(sky, w.vol)
+    out_d = torch.zeros((1, 8, 16, 4), dtype=torch.float32, device="cuda")
+    bb = w.disc.blackbody
+
+    def params(**kw):
+        p = _abi.StRenderParams()
+        lib.st_render_params_default(C.byref(p), _abi.ST_SEM_DRAFT)
+        p.width, p.height, p.samples = 16, 8, 1
+        p.precision = _abi.ST_PREC_FP32
+        for k, v in kw.items():
+            setattr(p, k, v)
+        return p
+
+    def disc(emitter):
+        return _abi.StDisc(0.0, w.disc.outer_radius, 0.0, bb.wb_temperature, bb.table_min, bb.table_max,
+                           bb.table_size, emitter)
+
+    ok = disc(w.emitter)
+    assert _noalloc(lib, sky_d, 512, 256, disc(7), dens_d, w.vol, [w.cam], w.bh, params(), out_d)[0] == _abi.ST_EINVAL
+    assert _noalloc(lib, sky_d, 512, 256, ok, dens_d, w.vol, [w.cam], w.bh, params(surrogate=1),
+                    out_d)[0] == _abi.ST_EUNSUPPORTED
+    assert _noalloc(lib, sky_d, 512, 256, ok, dens_d, w.vol, [w.cam], w.bh, params(order=45),
+                    out_d)[0] == _abi.ST_EUNSUPPORTED
+    bad = w.vol.__class__(**{**w.vol.__dict__, "z_max": 0.0})
+    assert _noalloc(lib, sky_d, 512, 256, ok, dens_d, bad, [w.cam], w.bh, params(), out_d)[0] == _abi.ST_EINVAL
+    bad = w.vol.__class__(**{**w.vol.__dict__, "log_s_out": w.vol.log_s_in})
+    assert _noalloc(lib, sky_d, 512, 256, ok, dens_d, bad, [w.cam], w.bh, params(), out_d)[0] == _abi.ST_EINVAL
+    # and a valid call still works afterwards
+    rc, stats = _noalloc(lib, sky_d, 512, 256, ok, dens_d, w.vol, [w.cam], w.bh, params(), out_d)
+    assert rc == _abi.ST_OK and stats.rays == 16 * 8
