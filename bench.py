@@ -109,6 +109,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def measure_fp32_peak(device: int, iters: int = 100000):
+    """(TFLOP/s, ms) of the library's FP32 FMA-chain ceiling kernel, or (None, 0)."""
+    import ctypes as C
+    from spacetime_gb300 import _abi
+    tf, ms = C.c_double(0.0), C.c_double(0.0)
+    try:
+        rc = _abi.load().st_measure_fp32_peak(device, iters, C.byref(tf), C.byref(ms))
+    except Exception:
+        return None, 0.0
+    return (tf.value, ms.value) if rc == 0 and tf.value > 0 else (None, 0.0)
+
+
 def measured_peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -172,59 +184,115 @@ def cpu_baseline(seconds_target: float = 15.0, threads: int | None = None, gpu_f
     return out
 
 
-def surrogate_variant(ctx_cls, device: int, flush, sigma: float, reps: int = 3) -> dict:
-    """The learned surrogate on the frame it serves: config 1's camera and
-    hole (Kerr a=0.9, r=15 M, i=80 deg, 1920x1080, kernel rules) with no disc
-    or gas, so every ray either escapes or falls in.  Times the same frame
-    three ways -- plain FP32 RK4, FP32 RK4 with FP64 guards, surrogate + FP32
-    (shipped network, gate sigma) -- and scores each against the FP64 oracle
-    (Tsit5 rtol 1e-10) on a 480x270 rendering of the frame."""
+# crops of the 1920x1080 frame the oracle renders for the accuracy figures:
+# (col0, cols, row0, rows) -- the central 240x135 (shadow, photon ring, the
+# densest gas) and a 3x3 grid of 80x45 tiles spread over the frame
+CROPS = [((1920 - 240) // 2, 240, (1080 - 135) // 2, 135)] + [
+    (c, 80, r, 45) for c in (160, 920, 1680) for r in (90, 517, 945)]
+
+
+def _crop_stack(img, diag=None):
+    import numpy as np
+    im = np.concatenate([img[r0:r0 + rh, c0:c0 + cw].reshape(-1, 3) for c0, cw, r0, rh in CROPS])
+    if diag is None:
+        return im
+    return im, np.concatenate([diag[r0:r0 + rh, c0:c0 + cw].reshape(-1) for c0, cw, r0, rh in CROPS])
+
+
+def _errors(img, diag, ref, rays, served=None):
+    """Exit-direction error (rad) over rays both sides call escaped, relative
+    radiance error (L1 over RGB / oracle L1) over all rays; with `served`,
+    the same over the surrogate-served rays alone."""
+    import numpy as np
+    from oracle import oracle as O
+
+    def ang(a, b):
+        return 2 * np.arcsin(np.clip(np.linalg.norm(a - b, axis=-1) / 2, 0, 1))
+
+    esc = ((diag["flags"] & 1) > 0) & ((rays["flags"] & O.RAY_ESCAPED) > 0)
+    d = ang(diag["dir"][esc].astype(np.float64), rays["dir"][esc])
+    rel = np.abs(img.astype(np.float64) - ref).sum(-1) / np.maximum(ref.sum(-1), 1e-6)
+    out = {"rays": int(img.shape[0]), "escaped_both": int(esc.sum()),
+           "dir_median_rad": float(np.median(d)), "dir_p99_rad": float(np.percentile(d, 99)),
+           "radiance_rel_median": float(np.median(rel)), "radiance_rel_p99": float(np.percentile(rel, 99)),
+           "class_mismatch": int((((diag["flags"] & 8) > 0) != ((rays["flags"] & O.RAY_BLACK) > 0)).sum())}
+    if served is not None and served.any():
+        se = served & esc
+        ds = ang(diag["dir"][se].astype(np.float64), rays["dir"][se]) if se.any() else np.zeros(1)
+        out["served"] = {"rays": int(served.sum()), "captured_in_oracle": int((served & ~esc).sum()),
+                         "dir_median_rad": float(np.median(ds)), "dir_p99_rad": float(np.percentile(ds, 99)),
+                         "dir_max_rad": float(ds.max()),
+                         "radiance_rel_median": float(np.median(rel[served])),
+                         "radiance_rel_p99": float(np.percentile(rel[served], 99))}
+    return out
+
+
+def headline_block(ctx_cls, device: int, flush, sigma: float, reps: int = 3) -> dict:
+    """The metric's comparison on one GB300: surrogate + FP32 against the plain
+    FP64-guarded RK4 path and plain FP32 RK4, each frame 1920x1080 with config
+    1's camera and hole (Kerr a=0.9, r=15 M, i=80 deg, Lens(24), kernel rules,
+    exit landing), on three scenes: the gas (config 1 itself), the thin disc
+    (2.32-25 M) and neither.  Each arm: device time per frame (L2 flushed),
+    Mrays/s, surrogate-served fraction, and errors against the FP64 oracle's
+    Tsit5 (rtol 1e-10) on crops of the timed frame itself (CROPS); for the
+    surrogate arm also the served rays alone."""
     import numpy as np
     import torch
     from oracle import oracle as O
     from spacetime_gb300 import _abi, workloads
     from spacetime_gb300.surrogate import load_trained
-    w = workloads.config1_thin()
-    w.disc = None
-    w.params = dict(samples=1, pixel_jitter=0, exit_landing=1)
     sky = workloads.sky()
     sur = load_trained(device)
-    ctx = ctx_cls(sky, disc=None, emitter=w.emitter, device=device)
-    ctx.set_surrogate(sur)
-    small = w.scaled(480, 270)
-    ref, rays = O.scene_for(small, sky, O.INT_TSIT5).render()
+    guards = dict(r_guard=3.0, crit_band=0.05, crit_r=4.0, renorm_every=256)
     arms = {"plain_fp32": dict(precision=_abi.ST_PREC_FP32),
-            "fp32_fp64_guarded": dict(precision=_abi.ST_PREC_FP32_GUARDED, r_guard=3.0, crit_band=0.05,
-                                      crit_r=4.0, renorm_every=256),
+            "fp32_fp64_guarded": dict(precision=_abi.ST_PREC_FP32_GUARDED, **guards),
             "surrogate_fp32": dict(precision=_abi.ST_PREC_FP32, surrogate=1, surrogate_sigma=sigma)}
-    out = {"workload": "config1 camera and hole (Kerr a=0.9, r=15 M, i=80 deg, Lens(24)), 1920x1080, "
-                       "no disc or gas; kernel rules; the shipped surrogate network",
-           "sigma_gate_rad": sigma}
-    for name, kw in arms.items():
-        p = ctx.params(w.semantics, width=1920, height=1080, **w.params, **kw)
-        ctx.render_device(w.cam, w.bh, p)
-        ts = []
-        for _ in range(reps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            _, st = ctx.render_device(w.cam, w.bh, p)
-            ts.append(st["kernel_ms"])
-        ms = float(np.mean(ts))
-        ps = ctx.params(w.semantics, width=480, height=270, **w.params, **kw)
-        r = ctx.render_raw(w.cam, w.bh, ps, diag=True)
-        both = ((r.diag["flags"] & 1) > 0) & ((rays["flags"] & O.RAY_ESCAPED) > 0)
-        d = np.zeros(both.shape)
-        a, b = r.diag["dir"][both], rays["dir"][both]
-        d[both] = 2 * np.arcsin(np.clip(np.linalg.norm(a - b, axis=-1) / 2, 0, 1))
-        rel = np.abs(r.image.astype(np.float64) - ref).sum(-1) / np.maximum(ref.sum(-1), 1e-6)
-        out[name] = {"value": 1920 * 1080 / (ms * 1e-3) / 1e6, "ms_per_step": ms,
-                     "served_fraction": st["surrogate_rays"] / (1920 * 1080),
-                     "dir_median_rad": float(np.median(d)), "dir_p99_rad": float(np.percentile(d, 99)),
-                     "radiance_rel_median": float(np.median(rel)),
-                     "radiance_rel_p99": float(np.percentile(rel, 99))}
-    out["speedup_vs_plain_fp32"] = out["surrogate_fp32"]["value"] / out["plain_fp32"]["value"]
-    out["speedup_vs_fp32_fp64_guarded"] = out["surrogate_fp32"]["value"] / out["fp32_fp64_guarded"]["value"]
-    ctx.close()
+    out = {"frame": "1920x1080, config 1's camera and hole (Kerr a=0.9, r=15 M, i=80 deg, Lens(24)), kernel "
+                    "rules, exit landing; the shipped surrogate network",
+           "sigma_gate_rad": sigma,
+           "errors_on": "crops of the timed frame: central 240x135 + nine 80x45 tiles (64,800 rays), "
+                        "against the FP64 oracle's Tsit5 (rtol 1e-10)"}
+    for wname, make in (("config1_gas", workloads.config1), ("config1_thin_disc", workloads.config1_thin),
+                        ("config1_no_disc_no_gas", workloads.config1_nogas)):
+        w = make()
+        ctx = ctx_cls(sky, disc=w.disc, volume=w.vol, emitter=w.emitter, device=device)
+        ctx.set_surrogate(sur)
+        refs = [O.scene_for(w, sky, O.INT_TSIT5, rect=rect).render() for rect in CROPS]
+        ref = np.concatenate([r[0].reshape(-1, 3) for r in refs]).astype(np.float64)
+        rays = np.concatenate([r[1].reshape(-1) for r in refs])
+        block = {}
+        for name, kw in arms.items():
+            if kw.get("surrogate") and w.vol is not None:
+                # the gate serves no ray of a gas frame (each ray's gas line integral
+                # needs its integrated path), so st_render refuses the combination;
+                # surrogate + FP32 on this frame is the plain FP32 path
+                block[name] = {**block["plain_fp32"], "served_fraction": 0.0,
+                               "note": "st_render refuses the surrogate with gas (ST_EUNSUPPORTED): every ray "
+                                       "starts inside the gas slab and needs its integrated path; the numbers are "
+                                       "the plain FP32 arm's"}
+                continue
+            p = ctx.params(w.semantics, width=1920, height=1080, **w.params, **kw)
+            ctx.render_device(w.cam, w.bh, p)
+            ts = []
+            for _ in range(reps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                _, st = ctx.render_device(w.cam, w.bh, p)
+                ts.append(st["kernel_ms"])
+            ms = float(np.mean(ts))
+            r = ctx.render_raw(w.cam, w.bh, p, diag=True)
+            img, diag = _crop_stack(r.image, r.diag)
+            served = (diag["flags"] & _abi.ST_RAY_SURROGATE) > 0 if kw.get("surrogate") else None
+            block[name] = {"value": 1920 * 1080 / (ms * 1e-3) / 1e6, "ms_per_step": ms,
+                           "served_fraction": st["surrogate_rays"] / (1920 * 1080),
+                           "steps_per_frame": st["steps"], "fp64_steps_per_frame": st["fp64_steps"],
+                           "errors": _errors(img, diag, ref, rays, served)}
+        sv, pl, gd = (block[k]["value"] for k in ("surrogate_fp32", "plain_fp32", "fp32_fp64_guarded"))
+        block["surrogate_vs_fp32_fp64_guarded"] = sv / gd
+        block["surrogate_vs_plain_fp32"] = sv / pl
+        block["plain_fp32_vs_fp32_fp64_guarded"] = pl / gd
+        out[wname] = block
+        ctx.close()
     sur.close()
     return out
 
@@ -460,7 +528,9 @@ def run_track(args):
     achieved = flops / (ms * 1e-3) / 1e12
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     sm_max = measured_peaks().get("sm_max_mhz", 2070.0)
-    fp32_peak = sms * 128 * 2 * sm_max * 1e6 / 1e12
+    fp32_nominal = sms * 128 * 2 * sm_max * 1e6 / 1e12
+    fp32_measured, _ = measure_fp32_peak(local)
+    fp32_peak = fp32_measured or fp32_nominal
     cpu = None
     if not args.no_cpu_baseline:
         try:
@@ -476,7 +546,9 @@ def run_track(args):
                    "gas_samples_per_track": st["gas_samples"], "per_frame_ms": ms / len(w.cams),
                    "l2": "inputs stay L2-resident by design; per-step time is kernel time of the whole track"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak, "traffic": None},
+                     "frac": achieved / fp32_peak, "traffic": None,
+                     "peak_note": "measured FP32 FMA ceiling (st_measure_fp32_peak)" if fp32_measured else
+                     "nominal FP32 FMA rate", "peak_nominal": fp32_nominal},
         "e2e": {"value": rays / (float(np.mean(tot)) * 1e-3) / 1e6, "unit": UNIT,
                 "h2d_bytes_per_step": int(st["h2d_bytes"]), "d2h_bytes_per_step": int(rays * 12)},
         "gpu_launches": args.steps * 2, "clocks": clk, "cpu_baseline": cpu,
@@ -615,10 +687,13 @@ def main(argv=None):
     sms = props.multi_processor_count
     peaks = measured_peaks()
     sm_max = peaks.get("sm_max_mhz", 2070.0)
-    fp32_peak = sms * 128 * 2 * sm_max * 1e6 / 1e12
+    fp32_nominal = sms * 128 * 2 * sm_max * 1e6 / 1e12
+    fp32_measured, fp32_ms = measure_fp32_peak(local)
+    fp32_peak = fp32_measured or fp32_nominal
     if rank != 0:
         return 0
     variants = {}
+    headline = None
     if not args.no_variants and (W, H) == (1920, 1080) and args.workload == "config1":
         # the same frame with FP64 guards (renormalisation every 256 steps, steps
         # inside 3 M, near-critical rays inside 4 M) and all in FP64
@@ -639,9 +714,9 @@ def main(argv=None):
         for name in variants:
             variants[name]["speedup_of_value"] = value / variants[name]["value"]
         try:
-            variants["surrogate_no_gas"] = surrogate_variant(Context, local, flush, args.sigma)
+            headline = headline_block(Context, local, flush, args.sigma)
         except Exception as e:  # report, do not fail the bench
-            variants["surrogate_no_gas"] = {"failed": str(e)}
+            headline = {"failed": str(e)}
         try:
             variants["layered_schwarzschild"] = layered_variant(Context, local, flush)
         except Exception as e:  # report, do not fail the bench
@@ -687,8 +762,8 @@ def main(argv=None):
                           "fp32g": "FP32 RHS, float-float state, FP64 guards"}[args.precision],
             "guards": {"r_guard": args.r_guard, "crit_band": args.crit_band, "renorm_every": args.renorm},
             "surrogate": ("not applied to this frame: every ray starts inside the gas slab, and the gas "
-                          "line integral needs the integrated path; measured on the same camera and hole "
-                          "without gas in variants.surrogate_no_gas")
+                          "line integral needs the integrated path; the surrogate arm on this frame and on "
+                          "the same camera and hole with a thin disc and with neither is in `headline`")
                          if args.workload == "config1" else
                          ({"params": os.path.basename(args.surrogate), "sigma_gate_rad": args.sigma,
                            "served_fraction": served / (W * H)} if args.surrogate else False),
@@ -704,8 +779,12 @@ def main(argv=None):
             "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
             "frac": achieved / fp32_peak, "traffic": traffic,
             "traffic_note": traffic_note,
-            "peak_note": f"nominal FP32 FMA rate: {sms} SMs x 128 lanes x 2 x {sm_max:.0f} MHz "
-                         "(MEASURED_PEAKS.json has no FP32 figure)",
+            "peak_note": (f"measured FP32 FMA ceiling (st_measure_fp32_peak: FMA-chain kernel at full occupancy, "
+                          f"best of 3 launches of {fp32_ms:.1f} ms, CUDA events); MEASURED_PEAKS.json has no FP32 "
+                          "figure" if fp32_measured else
+                          "nominal FP32 FMA rate (the measurement failed)"),
+            "peak_nominal": fp32_nominal,
+            "frac_of_nominal": achieved / fp32_nominal,
             "flops_per_step": flops_per_step(True), "flops_per_gas_sample": FLOPS_GAS_SAMPLE,
         },
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(e2e_stats["h2d_bytes"]),
@@ -713,6 +792,7 @@ def main(argv=None):
         "gpu_launches": args.steps,
         "clocks": clk,
         "cpu_baseline": cpu,
+        "headline": headline,
         "variants": variants,
     }
     print(json.dumps(line))

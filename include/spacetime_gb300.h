@@ -417,6 +417,9 @@ int st_surrogate_get_params(st_surrogate* s, float* host_params);
 int st_surrogate_set_params(st_surrogate* s, const float* host_params);
 /* normalised inputs x[n][6] -> outputs out[n][6] */
 int st_surrogate_forward(st_surrogate* s, const float* x, int n, float* out);
+/* the same, computed by the frame pass's tcgen05 / TMEM kernel (the one
+ * st_render runs); ST_ECUDA if one of its bounded waits ran out */
+int st_surrogate_forward_tc(st_surrogate* s, const float* x, int n, float* out);
 /* loss (total, direction MSE, radius MSE, g MSE) and parameter gradient of
  * targets t[n][8] = (in-plane deflection, out-of-plane tilt, 0, radius, g-1,
  * direction mask, crossing mask, 0) */
@@ -455,6 +458,13 @@ int st_render_frames_noalloc(const float* dev_sky_rgba, int sky_w, int sky_h, co
                              const float* dev_density, const st_volume* vol, int nframes,
                              const st_camera* cams, const st_spacetime* st, const st_render_params* p,
                              float* dev_out_rgba, void* stream, st_stats* stats);
+
+/* Measured FP32 fused-multiply-add ceiling of `device` (TFLOP/s, 2 flops per
+ * FMA; the best of three timed launches of an FMA-chain kernel holding every
+ * SM at full occupancy, `iters` x 128 FMAs per thread; ms_out may be NULL).
+ * No counterpart in the reference: the denominator of the trace kernel's
+ * roofline fraction, whose bound is FP32 issue. */
+int st_measure_fp32_peak(int device, int iters, double* tflops, double* ms_out);
 
 /* The camera's orthonormal Kerr-Schild tetrad (u, Ef, Er, Eu), each a
  * contravariant (t, x, y, z) 4-vector, boosted by the camera velocity. */

@@ -54,6 +54,26 @@ def forward(P, X):
     return out, zs, hs
 
 
+def bf16(x):
+    """Round to bfloat16 (nearest, ties to even), returned as float64."""
+    a = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    r = ((a + 0x7FFF + ((a >> 16) & 1)) & 0xFFFF0000).astype(np.uint32)
+    return r.view(np.float32).astype(np.float64)
+
+
+def forward_bf16(P, X):
+    """The forward pass under the tensor-core kernels' arithmetic contract
+    (st_surrogate.cu): the edge layers in FP32 parameters, the hidden layers'
+    weights and every hidden activation rounded to bf16, sums exact (FP64
+    here; the kernels accumulate in FP32).  Returns the (n, 6) outputs."""
+    w = unpack(P)
+    X = np.asarray(X, dtype=np.float64)
+    h = bf16(_silu(X @ w["W0"].T + w["b0"]))
+    for l in (1, 2, 3):
+        h = bf16(_silu(h @ bf16(w[f"W{l}"]).T + w[f"b{l}"]))
+    return h @ w["W4"].T + w["b4"]
+
+
 def loss_grad(P, X, T):
     """(loss4, grad) with loss4 = (total, direction MSE, radius MSE, g MSE)."""
     w = unpack(P)

@@ -125,12 +125,12 @@ EXPORTS = [
     "st_context_create", "st_context_set_disc", "st_context_set_volume", "st_context_destroy",
     "st_render", "st_render_diag", "st_render_device", "st_render_frames", "st_camera_tetrad",
     "st_surrogate_create", "st_surrogate_destroy", "st_surrogate_num_params", "st_surrogate_get_params",
-    "st_surrogate_set_params", "st_surrogate_forward", "st_surrogate_loss_grad", "st_surrogate_generate",
+    "st_surrogate_set_params", "st_surrogate_forward", "st_surrogate_forward_tc", "st_surrogate_loss_grad", "st_surrogate_generate",
     "st_surrogate_train", "st_render_frames_noalloc", "st_context_set_surrogate",
     "st_starfield_default", "st_context_set_starfield", "st_render_motion",
     "st_save_raw", "st_load_raw_size", "st_load_raw", "st_sky_fan", "st_render_layered",
     "st_render_depth", "st_render_layered_ring", "st_fluid_params_default", "st_fluid_create", "st_fluid_step", "st_fluid_state",
-    "st_fluid_destroy",
+    "st_fluid_destroy", "st_measure_fp32_peak",
 ]
 ST_FAN_N, ST_FAN_FINE = 4096, 1024
 
@@ -182,6 +182,7 @@ def load(path: str | None = None) -> C.CDLL:
     lib.st_surrogate_get_params.argtypes = [C.c_void_p, FP]
     lib.st_surrogate_set_params.argtypes = [C.c_void_p, FP]
     lib.st_surrogate_forward.argtypes = [C.c_void_p, FP, C.c_int, FP]
+    lib.st_surrogate_forward_tc.argtypes = [C.c_void_p, FP, C.c_int, FP]
     lib.st_surrogate_loss_grad.argtypes = [C.c_void_p, FP, FP, C.c_int, FP, FP]
     lib.st_surrogate_generate.argtypes = [C.c_void_p, LL, LL, C.c_double, FP, FP, FP]
     lib.st_surrogate_train.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, FP]
@@ -226,12 +227,14 @@ def load(path: str | None = None) -> C.CDLL:
     lib.st_fluid_state.argtypes = [C.c_void_p, P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_float),
                                    P(C.c_double)]
     lib.st_fluid_state.restype = C.c_int
+    lib.st_measure_fp32_peak.argtypes = [C.c_int, C.c_int, P(C.c_double), P(C.c_double)]
+    lib.st_measure_fp32_peak.restype = C.c_int
     lib.st_fluid_destroy.argtypes = [C.c_void_p]
     lib.st_fluid_destroy.restype = None
     for name in ("st_context_create", "st_context_set_disc", "st_context_set_volume", "st_render",
                  "st_render_diag", "st_render_device", "st_render_frames", "st_camera_tetrad",
                  "st_surrogate_create", "st_surrogate_num_params", "st_surrogate_get_params",
-                 "st_surrogate_set_params", "st_surrogate_forward", "st_surrogate_loss_grad",
+                 "st_surrogate_set_params", "st_surrogate_forward", "st_surrogate_forward_tc", "st_surrogate_loss_grad",
                  "st_surrogate_generate", "st_surrogate_train"):
         getattr(lib, name).restype = C.c_int
     if path is None:

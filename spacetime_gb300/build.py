@@ -31,7 +31,7 @@ UNIT_FLAGS = {
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["st_trace_fp64.cu", "st_trace_fp32.cu", "st_trace_fp32_guarded.cu", "st_api.cu", "st_surrogate.cu", "st_noalloc.cu",
-           "st_layered.cu", "st_rawio.cpp", "st_fluid.cu"]
+           "st_layered.cu", "st_rawio.cpp", "st_fluid.cu", "st_peak.cu"]
 
 
 def nvcc() -> str:

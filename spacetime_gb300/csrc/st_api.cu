@@ -340,6 +340,10 @@ struct st_context {
   int* d_list = nullptr;        // surrogate fallback pixels
   size_t list_cap = 0;
   int* d_count = nullptr;
+  // FP32_GUARDED deferral: saved ray states and their count
+  unsigned char* d_defer = nullptr;
+  size_t defer_cap = 0;  // bytes
+  unsigned* d_defer_count = nullptr;
 };
 
 namespace {
@@ -364,6 +368,30 @@ int ensure(T** ptr, size_t* cap, size_t n) {
 }
 
 double norm3(const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+
+// FP32_GUARDED on the pixel schedule (RK4, no depth buckets), with the
+// environment variable SPACETIME_GB300_GUARD_DEFER=1: space for every ray of
+// one launch to be saved before its first FP64 guard step, so the guard steps
+// run in full warps of a resume kernel.  Off by default: on the 1080p config-1
+// frame the split measured slower than the guard steps inline (103.2 vs
+// 94.5 ms), because the resumed rays' FP64 work no longer overlaps the
+// other warps' FP32 work and their FP64 segments end at different steps.
+int setup_defer(st_context* ctx, TraceParams* p, const st::Variant& v, size_t nrays) {
+  p->defer_state = nullptr;
+  p->defer_count = nullptr;
+  p->defer_cap = 0;
+  if (v.prec != ST_PREC_FP32_GUARDED || v.sched != ST_SCHED_PIXEL || p->order != 4 || p->nb > 0) return ST_OK;
+  const char* e = std::getenv("SPACETIME_GB300_GUARD_DEFER");
+  if (!e || std::strcmp(e, "1") != 0) return ST_OK;
+  if (nrays > (size_t)INT_MAX) return ST_EINVAL;
+  int rc = ensure(&ctx->d_defer, &ctx->defer_cap, nrays * st::guarded_ray_state_bytes());
+  if (rc != ST_OK) return rc;
+  if (!ctx->d_defer_count && cudaMalloc(&ctx->d_defer_count, sizeof(unsigned)) != cudaSuccess) return ST_ENOMEM;
+  p->defer_state = ctx->d_defer;
+  p->defer_count = ctx->d_defer_count;
+  p->defer_cap = (int)nrays;
+  return ST_OK;
+}
 
 // Fill the frame-independent part of TraceParams and the camera of `cam`.
 int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
@@ -623,6 +651,20 @@ __global__ void scale_box_kernel(float4* fb, int W, int c0, int r0, int cols, in
   o.x *= s; o.y *= s; o.z *= s;
 }
 
+// Iteration budget of the persistent kernel's outer loop: enough for every
+// ray of the launch to take its whole step budget in chunk-sized slices.  The
+// environment variable SPACETIME_GB300_QUEUE_BUDGET=<n> lowers it to n, so a
+// test can make the queue run out (the kernel then reports ST_EBUDGET and
+// returns; rays it had not finished are left unwritten).
+long long queue_budget(long long computed) {
+  const char* e = std::getenv("SPACETIME_GB300_QUEUE_BUDGET");
+  if (e) {
+    const long long n = std::atoll(e);
+    if (n > 0 && n < computed) return n;
+  }
+  return computed;
+}
+
 int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
               float* host_rgb, st_ray_diag* host_diag, const float** dev_rgba, st_stats* stats,
               const Motion* mo = nullptr, const Depth* depth = nullptr) {
@@ -669,6 +711,7 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
     if (!ctx->d_box && cudaMalloc(&ctx->d_box, 4 * sizeof(unsigned)) != cudaSuccess) return ST_ENOMEM;
     v.sched = ST_SCHED_PIXEL;  // refinement passes dispatch a box of the pixel grid
   }
+  if ((rc = setup_defer(ctx, &p, v, npix)) != ST_OK) return rc;
   ST_CUDA(cudaMemsetAsync(ctx->d_counters, 0, st::CNT_N * sizeof(unsigned long long), s));
   const std::vector<PassPlan> passes = plan_passes(rp, cam);
   p.weight = (float)(1.0 / passes.size());
@@ -715,7 +758,7 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
       ST_CUDA(cudaMemsetAsync(ctx->d_queue, 0, sizeof(unsigned int), s));
       const long long tiles = (long long)((rp->width + 7) / 8) * ((rp->height + 3) / 4);
       p.n_rays = (int)(tiles * 32);
-      p.budget_iters = ((long long)p.n_rays + 32) * ((long long)p.nmax / std::max(p.chunk_steps, 1) + 2);
+      p.budget_iters = queue_budget(((long long)p.n_rays + 32) * ((long long)p.nmax / std::max(p.chunk_steps, 1) + 2));
     }
     ST_CUDA(st::launch_trace(v, p, rp->block_x, rp->block_y, ctx->num_sms, s));
     ++launches;
@@ -1326,6 +1369,8 @@ void st_context_destroy(st_context* ctx) {
   cudaFree(ctx->d_lut);
   cudaFree(ctx->d_star_lut);
   cudaFree(ctx->d_stat);
+  cudaFree(ctx->d_defer);
+  cudaFree(ctx->d_defer_count);
   cudaFree(ctx->d_buckets);
   cudaFree(ctx->d_box);
   cudaFree(ctx->d_fan);
@@ -1490,9 +1535,10 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
   if (tiles * 32 * nframes > (long long)INT_MAX) return ST_EINVAL;
   p.n_rays = (int)(tiles * 32 * nframes);
   p.chunk_steps = rp->chunk_steps > 0 ? rp->chunk_steps : 32;
-  p.budget_iters = ((long long)p.n_rays + 32) * ((long long)nmax_max / p.chunk_steps + 2);
+  p.budget_iters = queue_budget(((long long)p.n_rays + 32) * ((long long)nmax_max / p.chunk_steps + 2));
   p.nmax = nmax_max;
   v.sched = rp->schedule == ST_SCHED_PIXEL ? ST_SCHED_PIXEL : ST_SCHED_PERSISTENT;
+  if ((rc = setup_defer(ctx, &p, v, npix * nframes)) != ST_OK) return rc;
   // the device work of one call: stage cameras, clear queue and counters,
   // trace all frames in one launch, pack, read the counters
   // Under stream capture a plain event record only orders streams; the

@@ -120,6 +120,13 @@ struct TraceParams {
   // pixel schedule over a compacted list (surrogate fallback rays)
   const int* pix_list;       // optional pixel indices (device)
   const int* n_list;         // their count (device)
+  // FP32_GUARDED pixel schedule: rays stop before their first FP64 guard step
+  // and are saved here (defer_cap states of the trace unit's ray-state size,
+  // in the order their warps reached it); a resume kernel over the saved
+  // rays runs the FP64 steps in full warps.  Null: guard steps inline.
+  void* defer_state;
+  unsigned int* defer_count;
+  int defer_cap;
   // persistent schedule
   const FrameCam* frames;    // optional per-frame cameras (device)
   int n_frames;              // frames in the table (pixel schedule: grid z)
@@ -267,5 +274,8 @@ cudaError_t launch_pack_rgb(const float4* fb, float* rgb, int n, cudaStream_t st
 
 // Number of registers the pixel kernel of a variant uses (for reporting).
 int variant_registers(const Variant& v);
+
+// Bytes of one saved ray state of the FP32_GUARDED deferral (defer_state).
+size_t guarded_ray_state_bytes();
 
 }  // namespace st

@@ -39,7 +39,7 @@ __device__ __forceinline__ void flush_counters(const TraceParams& p, unsigned lo
 
 // One thread per pixel over a 2-D grid of tiles (blockDim.x * blockDim.y a
 // multiple of 32; threads are linearised so a warp covers a compact tile).
-template <int PREC, int KERR, int VOL, int SEM, int ORD = 4, int DEPTH = 0>
+template <int PREC, int KERR, int VOL, int SEM, int ORD = 4, int DEPTH = 0, int DEFER = 0>
 __global__ void __launch_bounds__(128, ORD == 4 ? ST_MINB : ST_MINB_ADAPTIVE) trace_pixel_kernel(const __grid_constant__ TraceParams p) {
   using R = typename RealOf<PREC>::T;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -74,9 +74,51 @@ __global__ void __launch_bounds__(128, ORD == 4 ? ST_MINB : ST_MINB_ADAPTIVE) tr
     st.pix = base + j * p.width + i;
     if (final_at_launch<SEM>(p, st.flags)) st.flags |= ST_RAY_CAPTURED;
     else
-      while (!step_ray<PREC, KERR, VOL, SEM, ORD, DEPTH>(p, st)) {
+      while (!step_ray<PREC, KERR, VOL, SEM, ORD, DEPTH, DEFER>(p, st)) {
       }
-    finish_ray<PREC, KERR, SEM, DEPTH>(p, st, st.pix, p.frames ? st.pix : j * p.width + i);
+    bool deferred = false;
+    if constexpr (DEFER) deferred = (st.flags & ST_RAY_DEFER) != 0;
+    if (!deferred) {
+      finish_ray<PREC, KERR, SEM, DEPTH>(p, st, st.pix, p.frames ? st.pix : j * p.width + i);
+      steps = st.steps; f64 = st.fp64_steps; gas = st.gas; rays = 1;
+    }
+    if constexpr (DEFER) {
+      // save the suspended ray (its counters travel with it); one atomic per
+      // warp, consecutive slots for the warp's deferring lanes
+      const unsigned act = __activemask();
+      const unsigned want = __ballot_sync(act, deferred);
+      if (deferred) {
+        const int leader = __ffs(want) - 1;
+        const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
+        unsigned slot0 = 0;
+        if (lane == leader) slot0 = atomicAdd(p.defer_count, (unsigned)__popc(want));
+        slot0 = __shfl_sync(want, slot0, leader);
+        const unsigned slot = slot0 + __popc(want & ((1u << lane) - 1u));
+        if (slot < (unsigned)p.defer_cap) {
+          st.flags &= ~ST_RAY_DEFER;
+          static_cast<RayState<R>*>(p.defer_state)[slot] = st;
+        } else if (p.counters) {
+          atomicMax(p.counters + CNT_STATUS, (unsigned long long)ST_ECUDA);  // cannot happen: cap >= rays
+        }
+      }
+    }
+  }
+  flush_counters(p, steps, f64, gas, rays);
+}
+
+// FP32_GUARDED: the rays the pixel kernel saved before their first FP64 step,
+// one thread each, so the FP64 steps they start with run in full warps; each
+// continues to its end with the guard steps inline.
+template <int KERR, int VOL, int SEM>
+__global__ void __launch_bounds__(128, ST_MINB) trace_resume_kernel(const __grid_constant__ TraceParams p) {
+  using R = float;
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long steps = 0, f64 = 0, gas = 0, rays = 0;
+  if (t < min(*p.defer_count, (unsigned)p.defer_cap)) {
+    RayState<R> st = static_cast<const RayState<R>*>(p.defer_state)[t];
+    while (!step_ray<ST_PREC_FP32_GUARDED, KERR, VOL, SEM, 4, 0, 0>(p, st)) {
+    }
+    finish_ray<ST_PREC_FP32_GUARDED, KERR, SEM, 0>(p, st, st.pix, st.pix);
     steps = st.steps; f64 = st.fp64_steps; gas = st.gas; rays = 1;
   }
   flush_counters(p, steps, f64, gas, rays);
@@ -174,6 +216,18 @@ cudaError_t launch_variant(const TraceParams& p, int sched, int bx, int by, int 
     if constexpr (SEM == ST_SEM_DRAFT && PREC != ST_PREC_FP32_GUARDED) {
       if (p.order == 45) { trace_pixel_kernel<PREC, KERR, VOL, SEM, 45><<<grid, block, 0, s>>>(p); return cudaGetLastError(); }
       if (p.order == 46) { trace_pixel_kernel<PREC, KERR, VOL, SEM, 46><<<grid, block, 0, s>>>(p); return cudaGetLastError(); }
+    }
+    if constexpr (PREC == ST_PREC_FP32_GUARDED) {
+      if (p.defer_state && p.defer_count && p.defer_cap > 0) {
+        // guard steps gathered into full warps: stop each ray before its first
+        // FP64 step, then resume the saved rays one per thread
+        cudaError_t e = cudaMemsetAsync(p.defer_count, 0, sizeof(unsigned int), s);
+        if (e != cudaSuccess) return e;
+        trace_pixel_kernel<PREC, KERR, VOL, SEM, 4, 0, 1><<<grid, block, 0, s>>>(p);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        trace_resume_kernel<KERR, VOL, SEM><<<(unsigned)((p.defer_cap + 127) / 128), 128, 0, s>>>(p);
+        return cudaGetLastError();
+      }
     }
     trace_pixel_kernel<PREC, KERR, VOL, SEM><<<grid, block, 0, s>>>(p);
   }

@@ -806,8 +806,12 @@ __global__ void __launch_bounds__(FTHREADS, 1)
 // as the unfused forward stores it) run in FP32.
 //
 // Every wait on an mbarrier is bounded; a wait that runs out marks the tile
-// failed (its pixels all go to the integrator, so the frame stays exact), sets
-// the status word, and the CTA still frees its TMEM.
+// failed (its pixels all go to the integrator, so the frame stays exact) and
+// sets the status word.  Before the CTA frees its TMEM and exits, the thread
+// that issued the copies and the MMAs waits again (bounded) for the one
+// operation still outstanding -- the last armed weight copy or the last
+// committed MMA batch -- so that neither lands in shared memory or TMEM the
+// CTA no longer owns.
 constexpr uint32_t TC_ROWS = 128, TC_THREADS = 512;
 constexpr uint32_t TC_A_BYTES = TC_ROWS * NH * 2;  // 64 KB activation tile
 constexpr uint32_t TC_B_BYTES = NH * NH * 2;       // 128 KB weight tile
@@ -963,11 +967,13 @@ __global__ void __launch_bounds__(128) sur_scatter_kernel(const __grid_constant_
 // CTA per 128 rows, 16 warps.  tile_status[t] = 0, or 1 when a bounded wait
 // ran out (the gate then integrates the tile's pixels, and the status word is
 // set).  The weights of hidden layer 1, the packed FP32 parameters and the
-// tile's inputs arrive together on one mbarrier.
+// tile's inputs arrive together on one mbarrier.  wait_limit bounds every
+// mbarrier wait (polls); issue_first = 0 leaves the first copies unissued, so
+// the first wait runs out with nothing in flight -- the failure path's test.
 __global__ void __launch_bounds__(TC_THREADS, 1)
     sur_mlp_tc_kernel(const float* __restrict__ Psmall, const unsigned char* __restrict__ Wsw,
                       const float* __restrict__ X, float* __restrict__ O, int* __restrict__ tile_status,
-                      unsigned long long* counters) {
+                      unsigned long long* counters, uint32_t wait_limit, int issue_first) {
   extern __shared__ unsigned char tsm_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(tsm_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -987,14 +993,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = S.tmem;
-  if (tid == 0) {
+  // thread 0's record of what it has in flight: the phase of bar_w last
+  // armed with copies and of bar_mma last committed to (-1: none)
+  int w_armed = issue_first ? 0 : -1, mma_committed = -1;
+  if (tid == 0 && issue_first) {
     tc::mbar_expect_tx(&S.bar_w, TC_B_BYTES + TC_SMALL_BYTES + TC_X_BYTES);
 #pragma unroll
     for (int c = 0; c < 4; ++c) tc::bulk_g2s(Bs + c * 32768, Wsw + c * 32768, 32768, &S.bar_w);
     tc::bulk_g2s(S.W0, Psmall, TC_SMALL_BYTES, &S.bar_w);
     tc::bulk_g2s(S.X, X + row0 * NIN, TC_X_BYTES, &S.bar_w);
   }
-  if (!tc::mbar_wait(&S.bar_w, 0, TC_WAIT_LIMIT)) S.fail = 1;
+  if (!tc::mbar_wait(&S.bar_w, 0, wait_limit)) S.fail = 1;
   __syncthreads();
   const bool start_ok = S.fail == 0;
   // layer 0 (FP32): thread = hidden unit n over one half of the rows
@@ -1022,7 +1031,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint32_t ph = 0;
   for (int l = 0; l < 3 && start_ok; ++l) {
     if (tid == 0) {
-      if (tc::mbar_wait(&S.bar_w, ph, TC_WAIT_LIMIT)) {
+      if (tc::mbar_wait(&S.bar_w, ph, wait_limit)) {
         tc::fence_after_sync();
 #pragma unroll
         for (int s = 0; s < NH / 16; ++s) {
@@ -1031,13 +1040,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           tc::mma_bf16(tmem, ad, bd, TC_IDESC, s > 0 ? 1u : 0u);
         }
         tc::mma_commit(&S.bar_mma);
+        mma_committed = l;
       } else {
         S.fail = 1;
       }
     }
     __syncthreads();
     if (S.fail) break;
-    if (!tc::mbar_wait(&S.bar_mma, ph, TC_WAIT_LIMIT)) S.fail = 1;
+    if (!tc::mbar_wait(&S.bar_mma, ph, wait_limit)) S.fail = 1;
     ph ^= 1u;
     __syncthreads();
     if (S.fail) break;
@@ -1048,6 +1058,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
       for (int c = 0; c < 4; ++c)
         tc::bulk_g2s(Bs + c * 32768, Wsw + (size_t)(l + 1) * TC_B_BYTES + c * 32768, 32768, &S.bar_w);
+      w_armed = l + 1;
     }
 #pragma unroll 1
     for (int c = 0; c < 2; ++c) {
@@ -1089,6 +1100,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (!failed) {
 #pragma unroll
     for (int o = 0; o < NOUT; ++o) Opart[(cq * TC_ROWS + row) * NOUT + o] = part[o];
+  } else if (tid == 0) {
+    // drain: a parity wait on the last armed / committed phase returns at
+    // once if it has completed and otherwise waits for it (each barrier has
+    // at most one phase outstanding)
+    if (w_armed >= 0) (void)tc::mbar_wait(&S.bar_w, (uint32_t)w_armed & 1u, wait_limit);
+    if (mma_committed >= 0) (void)tc::mbar_wait(&S.bar_mma, (uint32_t)mma_committed & 1u, wait_limit);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -1243,6 +1260,42 @@ int backward(st_surrogate* s, const float* X, int B) {
 
 int pad128(long long n) { return (int)((n + 127) / 128 * 128); }
 
+// Wait bound and first-copy switch of sur_mlp_tc_kernel.  The environment
+// variable SPACETIME_GB300_TC_WAIT_OUT=1 makes every tile's first wait run out
+// (its copies are never issued, short wait bound): the failure path under test.
+struct TcWait {
+  uint32_t limit;
+  int issue_first;
+};
+TcWait tc_wait_mode() {
+  const char* e = std::getenv("SPACETIME_GB300_TC_WAIT_OUT");
+  if (e && std::strcmp(e, "1") == 0) return TcWait{1024u, 0};
+  return TcWait{TC_WAIT_LIMIT, 1};
+}
+
+// Frame-pass buffers for `rows` network rows (a multiple of 128, one tile of
+// the tcgen05 kernel per 128).
+int ensure_frame(st_surrogate* s, long long rows) {
+  if (s->frows >= rows) return ST_OK;
+  cudaFree(s->fX); cudaFree(s->fAux); cudaFree(s->fFl); cudaFree(s->fO); cudaFree(s->fStatus);
+  cudaFree(s->fMask); cudaFree(s->fCount); cudaFree(s->fOff);
+  s->fX = nullptr; s->fAux = nullptr; s->fFl = nullptr; s->fO = nullptr; s->fStatus = nullptr;
+  s->fMask = nullptr; s->fCount = nullptr; s->fOff = nullptr;
+  s->frows = 0;
+  const size_t nw = (size_t)rows / 32, nb = (size_t)rows / TC_ROWS;
+  if (cudaMalloc(&s->fX, rows * NIN * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&s->fAux, rows * sizeof(float4)) != cudaSuccess ||
+      cudaMalloc(&s->fFl, rows * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&s->fO, rows * NOUT * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&s->fStatus, nb * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&s->fMask, nw * sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&s->fCount, nw * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&s->fOff, nw * sizeof(int)) != cudaSuccess)
+    return ST_ENOMEM;
+  s->frows = rows;
+  return ST_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1350,6 +1403,32 @@ int st_surrogate_forward(st_surrogate* s, const float* X, int n, float* out) {
   return ST_OK;
 }
 
+// The same network on the frame pass's tensor-core kernel (tcgen05 / TMEM,
+// sur_mlp_tc_kernel): rows padded to whole 128-row tiles with zeros.
+int st_surrogate_forward_tc(st_surrogate* s, const float* X, int n, float* out) {
+  if (!s || !X || !out || n <= 0) return ST_EINVAL;
+  if (cudaSetDevice(s->device) != cudaSuccess) return ST_ECUDA;
+  const long long B = pad128(n);
+  const int nb = (int)(B / TC_ROWS);
+  int rc = ensure_frame(s, B);
+  if (rc != ST_OK) return rc;
+  cudaStream_t st = s->stream;
+  SC(cudaMemsetAsync(s->fX, 0, (size_t)B * NIN * 4, st));
+  SC(cudaMemcpyAsync(s->fX, X, (size_t)n * NIN * 4, cudaMemcpyHostToDevice, st));
+  SC(cudaFuncSetAttribute(sur_mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+  const TcWait tw = tc_wait_mode();
+  sur_mlp_tc_kernel<<<nb, TC_THREADS, TC_SMEM, st>>>(s->Psmall, s->Wsw, s->fX, s->fO, s->fStatus, nullptr, tw.limit,
+                                                     tw.issue_first);
+  SC(cudaGetLastError());
+  std::vector<int> status(nb);
+  SC(cudaMemcpyAsync(out, s->fO, (size_t)n * NOUT * 4, cudaMemcpyDeviceToHost, st));
+  SC(cudaMemcpyAsync(status.data(), s->fStatus, nb * sizeof(int), cudaMemcpyDeviceToHost, st));
+  SC(cudaStreamSynchronize(st));
+  for (int t = 0; t < nb; ++t)
+    if (status[t]) return ST_ECUDA;  // a bounded wait ran out: that tile has no output
+  return ST_OK;
+}
+
 // Loss and parameter gradient on n rows (rows beyond n are masked padding).
 int st_surrogate_loss_grad(st_surrogate* s, const float* X, const float* T, int n, float* loss4, float* grad) {
   if (!s || !X || !T || n <= 0) return ST_EINVAL;
@@ -1453,31 +1532,17 @@ int surrogate_frame(st_surrogate* s, const TraceParams& p, const Variant& v, con
     k<<<nb, sur::FTHREADS, sur::F_SMEM, stream>>>(p, f, s->P, s->Wb[0], s->Wb[1], s->Wb[2], list, count);
   } else {
     const long long rows = (long long)nb * sur::TC_ROWS;
-    if (s->frows < rows) {
-      cudaFree(s->fX); cudaFree(s->fAux); cudaFree(s->fFl); cudaFree(s->fO); cudaFree(s->fStatus);
-      cudaFree(s->fMask); cudaFree(s->fCount); cudaFree(s->fOff);
-      s->fX = nullptr; s->fAux = nullptr; s->fFl = nullptr; s->fO = nullptr; s->fStatus = nullptr;
-      s->fMask = nullptr; s->fCount = nullptr; s->fOff = nullptr;
-      s->frows = 0;
-      const size_t nw = (size_t)rows / 32;
-      if (cudaMalloc(&s->fX, rows * sur::NIN * sizeof(float)) != cudaSuccess ||
-          cudaMalloc(&s->fAux, rows * sizeof(float4)) != cudaSuccess ||
-          cudaMalloc(&s->fFl, rows * sizeof(int)) != cudaSuccess ||
-          cudaMalloc(&s->fO, rows * sur::NOUT * sizeof(float)) != cudaSuccess ||
-          cudaMalloc(&s->fStatus, (size_t)nb * sizeof(int)) != cudaSuccess ||
-          cudaMalloc(&s->fMask, nw * sizeof(unsigned)) != cudaSuccess ||
-          cudaMalloc(&s->fCount, nw * sizeof(int)) != cudaSuccess ||
-          cudaMalloc(&s->fOff, nw * sizeof(int)) != cudaSuccess)
-        return ST_ENOMEM;
-      s->frows = rows;
-    }
+    const int rc = ensure_frame(s, rows);
+    if (rc != ST_OK) return rc;
     if (v.kerr) sur::sur_inputs_kernel<1><<<nb, 128, 0, stream>>>(p, f, s->fX, s->fAux, s->fFl);
     else sur::sur_inputs_kernel<0><<<nb, 128, 0, stream>>>(p, f, s->fX, s->fAux, s->fFl);
     SC(cudaGetLastError());
     SC(cudaFuncSetAttribute(sur::sur_mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)sur::TC_SMEM));
+    const TcWait tw = tc_wait_mode();
     sur::sur_mlp_tc_kernel<<<nb, sur::TC_THREADS, sur::TC_SMEM, stream>>>(s->Psmall, s->Wsw, s->fX, s->fO,
-                                                                          s->fStatus, p.counters);
+                                                                          s->fStatus, p.counters, tw.limit,
+                                                                          tw.issue_first);
     SC(cudaGetLastError());
     sur::sur_gate_kernel<<<nb, 128, 0, stream>>>(p, f, s->fO, s->fAux, s->fFl, s->fStatus, s->fMask, s->fCount);
     SC(cudaGetLastError());

@@ -182,6 +182,44 @@ __device__ __forceinline__ void rhs_kerr_f32(const float* s, float pt, float M, 
   d[5] = fmaf(z * isig, fmaf(G * r, r2a, -((a2 * ell) * fl)), flir * pz);
 }
 
+// The regrouped Kerr RHS above in double, for the FP32_GUARDED path's FP64
+// guard steps: the same algebra (r from the half-w quartic root, one
+// reciprocal square root for r and 1/r, two reciprocals), so a guard step
+// issues about half the FP64 instructions of the term-by-term form.  On GB300
+// an FP64 instruction costs tens of FP32 ones; the all-FP64 precision keeps
+// the term-by-term form the oracle restates.
+__device__ __forceinline__ void rhs_kerr_rg64(const double* s, double pt, double M, double a, double* d) {
+  const double x = s[0], y = s[1], z = s[2], px = s[3], py = s[4], pz = s[5];
+  const double a2 = a * a, z2 = z * z;
+  const double q = a2 * z2;
+  const double wh = fma(fma(x, x, fma(y, y, z2)), 0.5, -(0.5 * a2));
+  const double r2 = fmax(wh + sqrt(fma(wh, wh, q)), 1e-12);
+  const double ir = rsqrt(r2), r = r2 * ir;
+  const double isig = 1.0 / fma(r2, r2, q);
+  const double r2a = r2 + a2;
+  const double ira = 1.0 / r2a;
+  const double A = fma(px, x, py * y);
+  const double B = fma(px, y, -(py * x));
+  const double T = fma(r, A, a * B) * ira;
+  const double Z = (z * pz) * ir;
+  const double ell = (T + Z) - pt;
+  const double rsig = (r2 * r) * isig;
+  const double fl = ((2.0 * M) * rsig) * ell;
+  const double Fi = fl * ira;
+  const double Fr = Fi * r, Fa = Fi * a;
+  const double flir = fl * ir;
+  d[0] = fma(-Fr, x, fma(-Fa, y, px));
+  d[1] = fma(-Fr, y, fma(Fa, x, py));
+  d[2] = fma(-flir, z, pz);
+  const double dldr = fma(fma(-2.0 * r, T, A), ira, -(Z * ir));
+  const double inner = fma(ell * ir, fma(q + q, isig, -0.5), dldr);
+  const double G = fl * inner;
+  const double Gr = G * rsig;
+  d[3] = fma(Gr, x, fma(Fr, px, -(Fa * py)));
+  d[4] = fma(Gr, y, fma(Fr, py, Fa * px));
+  d[5] = fma(z * isig, fma(G * r, r2a, -((a2 * ell) * fl)), flir * pz);
+}
+
 // Kerr, src/metal.jl:466-508 (implicit-quartic r, four derivative terms).
 template <typename R>
 __device__ __forceinline__ void rhs_kerr(const R* s, R pt, R M, R a, R* d) {
@@ -553,6 +591,10 @@ __device__ __forceinline__ bool final_at_launch(const TraceParams& p, int flags)
 
 // Internal ray flag of the layer pass: the fan proves the ray misses the gate.
 constexpr int ST_RAY_LAYER_CULLED = 1 << 20;
+// Internal ray flag of the guarded schedule: the ray stopped before its first
+// FP64 guard step, its state saved for the resume kernel.
+constexpr int ST_RAY_DEFER = 1 << 21;
+constexpr int ST_RAY_INTERNAL = ST_RAY_LAYER_CULLED | ST_RAY_DEFER;
 
 // Camera tetrad for the current ray; per-frame data lives in TraceParams for
 // single frames and in FrameCam for batched tracks (st_render_frames).
@@ -1090,15 +1132,36 @@ __device__ __forceinline__ R tsit5_adaptive(const R* s0, R pt, R M, R a, R r, R 
   return h_used;
 }
 
-// FP64 guard step on the float-float state.
+// RHS of the guard steps: the regrouped Kerr form in double, Schwarzschild as is.
+template <int KERR>
+__device__ __forceinline__ void rhs_guard(const double* s, double pt, double M, double a, double* d) {
+  if constexpr (KERR) rhs_kerr_rg64(s, pt, M, a, d); else rhs_schw(s, pt, M, d);
+}
+
+// FP64 guard step on the float-float state (classical RK4 in double).
 template <int KERR>
 __device__ __forceinline__ void guard_step_fp64(float* y, float* lo, float pt, double M, double a, float h) {
   double yd[6], k1d[6], inc[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) yd[k] = (double)y[k] + (double)lo[k];
   const double ptd = (double)pt;
-  rhs<KERR>(yd, ptd, M, a, k1d);
-  rk4_inc<KERR>(yd, ptd, M, a, (double)h, k1d, inc);
+  rhs_guard<KERR>(yd, ptd, M, a, k1d);
+  {
+    double t[6], k[6], sum[6];
+    const double hd = (double)h, hh = 0.5 * hd;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) { t[i] = fma(hh, k1d[i], yd[i]); sum[i] = k1d[i]; }
+    rhs_guard<KERR>(t, ptd, M, a, k);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) { sum[i] = fma(2.0, k[i], sum[i]); t[i] = fma(hh, k[i], yd[i]); }
+    rhs_guard<KERR>(t, ptd, M, a, k);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) { sum[i] = fma(2.0, k[i], sum[i]); t[i] = fma(hd, k[i], yd[i]); }
+    rhs_guard<KERR>(t, ptd, M, a, k);
+    const double h6 = hd * (1.0 / 6.0);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) inc[i] = h6 * (sum[i] + k[i]);
+  }
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
     const double v = yd[k] + inc[k];
@@ -1124,8 +1187,12 @@ __device__ __forceinline__ void renorm_fp64(float* y, float* lo, float pt, doubl
 
 // One integration step for the variant; returns true when the ray is done.
 // Mirrors the step loop of src/metal.jl:1201-1572 (DRAFT) and the callback
-// structure of src/raytrace.jl:339-373 (RENDER).
-template <int PREC, int KERR, int VOL, int SEM, int ORD = 4, int DEPTH = 0>
+// structure of src/raytrace.jl:339-373 (RENDER).  DEFER (FP32_GUARDED): a
+// step that would run in FP64 is not taken; the ray returns flagged
+// ST_RAY_DEFER with its state as it entered the call (the only field the
+// call has written, r_prev, is rewritten to the same value when the step is
+// taken again), so the resume kernel can take it in a dense FP64 warp.
+template <int PREC, int KERR, int VOL, int SEM, int ORD = 4, int DEPTH = 0, int DEFER = 0>
 __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename RealOf<PREC>::T>& st) {
   using R = typename RealOf<PREC>::T;
   const R M = PR(M), a = PR(a);
@@ -1219,6 +1286,12 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
   if constexpr (PREC == ST_PREC_FP32_GUARDED) {
     fp64_step = (st.guard_ray && (PR(crit_r2) <= R(0) || rk2 < PR(crit_r2))) ||
                 (!(st.flags & ST_RAY_BCAPT) && rk2 < PR(r_guard2));
+    if constexpr (DEFER) {
+      if (fp64_step) {
+        st.flags |= ST_RAY_DEFER;
+        return true;
+      }
+    }
   }
   if constexpr (ORD == 45 || ORD == 46) {
     // adaptive Tsit5 (src/metal.jl:1278-1381); 45 caps the step at the
@@ -1476,7 +1549,7 @@ __device__ __forceinline__ void finish_ray(const TraceParams& p, RayState<typena
   if (p.diag) {
     st_ray_diag d;
     d.dir[0] = (double)d0; d.dir[1] = (double)d1; d.dir[2] = (double)d2;
-    d.flags = st.flags | (st.guard_ray ? ST_RAY_GUARDED : 0);
+    d.flags = (st.flags & ~ST_RAY_INTERNAL) | (st.guard_ray ? ST_RAY_GUARDED : 0);
     d.r_final = (float)rf;
     d.alpha = (float)st.alpha;
     d.r_cross = st.r_cross;

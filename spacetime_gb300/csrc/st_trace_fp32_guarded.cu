@@ -11,4 +11,6 @@ cudaError_t launch_trace_fp32_guarded(const Variant& v, const TraceParams& p, in
 
 int variant_registers_fp32_guarded(const Variant& v) { return variant_regs_impl<ST_PREC_FP32_GUARDED>(v.kerr, v.vol, v.sem); }
 
+size_t guarded_ray_state_bytes() { return sizeof(RayState<float>); }
+
 }  // namespace st

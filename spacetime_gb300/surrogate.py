@@ -53,6 +53,14 @@ class Surrogate:
         _abi.check(self._lib.st_surrogate_forward(self._h, _fp(X), X.shape[0], _fp(out)), "st_surrogate_forward")
         return out
 
+    def forward_tc(self, X) -> np.ndarray:
+        """The network on the frame pass's tcgen05 / TMEM kernel."""
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        out = np.empty((X.shape[0], NOUT), np.float32)
+        _abi.check(self._lib.st_surrogate_forward_tc(self._h, _fp(X), X.shape[0], _fp(out)),
+                   "st_surrogate_forward_tc")
+        return out
+
     def loss_grad(self, X, T):
         X = np.ascontiguousarray(X, dtype=np.float32)
         T = np.ascontiguousarray(T, dtype=np.float32)

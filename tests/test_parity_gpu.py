@@ -117,3 +117,29 @@ def test_adaptive_tsit5_modes_fp64_vs_twin(built_lib, sky, order, twin):
     ts, ts_rays = oracle_scene(w, sky, O.INT_TSIT5).render()
     c2 = compare(g.image, g.diag, ts, ts_rays)
     assert c2["dir_median"] <= 1e-6, c2
+
+
+def test_guarded_deferral_matches_inline_guards(built_lib, sky, monkeypatch):
+    """FP32_GUARDED on the pixel schedule with SPACETIME_GB300_GUARD_DEFER=1
+    stops each ray before its first FP64 guard step and resumes the saved rays
+    one per thread, so their FP64 steps start in full warps.  Against the
+    default (guard steps inline): the same rays take the same steps, FP64
+    steps included, and the frames agree to the float tolerance of two
+    compilations of one kernel (radiance within 1e-3 on 99 % of pixels)."""
+    w = workloads.config1().scaled(240, 135)
+    kw = dict(r_guard=3.0, crit_band=0.05, crit_r=4.0, renorm_every=256)
+    monkeypatch.setenv("SPACETIME_GB300_GUARD_DEFER", "1")
+    a = gpu_render(w, sky, FP32G, **kw)
+    monkeypatch.delenv("SPACETIME_GB300_GUARD_DEFER")
+    b = gpu_render(w, sky, FP32G, **kw)
+    print("deferred", a.stats, "inline", b.stats)
+    assert a.stats["status"] == _abi.ST_OK and a.stats["rays"] == w.width * w.height
+    assert a.stats["fp64_steps"] > 0
+    assert abs(a.stats["steps"] - b.stats["steps"]) <= 1e-4 * b.stats["steps"]
+    assert abs(a.stats["fp64_steps"] - b.stats["fp64_steps"]) <= 1e-3 * b.stats["fp64_steps"]
+    rel = np.abs(a.image - b.image).sum(-1) / np.maximum(np.abs(b.image).sum(-1), 1e-6)
+    assert (rel > 1e-3).mean() <= 0.01, (rel > 1e-3).mean()
+    c = compare(a.image, a.diag, b.image.astype(np.float64), b.diag)
+    assert c["class_mismatch"] <= 2 and c["dir_median"] <= 1e-6, c
+    # the diag flags carry no internal bits
+    assert not (a.diag["flags"] & ~0x1FF).any()
