@@ -37,6 +37,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Mrays/s 1080p Kerr a=0.9: surrogate+FP32 vs plain RK4, same GB300, ≤1e-4 rad"
 UNIT = "Mrays/s"
+# surrogate gates (max predicted std-dev of the exit angles, rad): the widest
+# that keeps the frame's exit directions inside the 1e-4 / 1e-3 rad target on
+# the no-disc 1080p frame, and a wider one that serves about half of it
+SIGMA_TARGET = 2e-4
+SIGMA_WIDE = 4e-4
 
 # Algorithmic flops, counted from spacetime_gb300/csrc/st_trace.cuh (every
 # add, mul, div, sqrt, rsqrt, rcp, exp, log, atan2 counted as one).
@@ -246,10 +251,15 @@ def headline_block(ctx_cls, device: int, flush, sigma: float, reps: int = 3) -> 
     guards = dict(r_guard=3.0, crit_band=0.05, crit_r=4.0, renorm_every=256)
     arms = {"plain_fp32": dict(precision=_abi.ST_PREC_FP32),
             "fp32_fp64_guarded": dict(precision=_abi.ST_PREC_FP32_GUARDED, **guards),
-            "surrogate_fp32": dict(precision=_abi.ST_PREC_FP32, surrogate=1, surrogate_sigma=sigma)}
+            "surrogate_fp32": dict(precision=_abi.ST_PREC_FP32, surrogate=1, surrogate_sigma=sigma),
+            "surrogate_fp32_wide_gate": dict(precision=_abi.ST_PREC_FP32, surrogate=1,
+                                             surrogate_sigma=SIGMA_WIDE)}
     out = {"frame": "1920x1080, config 1's camera and hole (Kerr a=0.9, r=15 M, i=80 deg, Lens(24)), kernel "
                     "rules, exit landing; the shipped surrogate network",
-           "sigma_gate_rad": sigma,
+           "sigma_gate_rad": sigma, "sigma_gate_wide_rad": SIGMA_WIDE,
+           "gates": "surrogate_fp32: the widest gate that keeps the frame's exit directions inside the target "
+                    "(median 1e-4, p99 1e-3 rad); surrogate_fp32_wide_gate: a gate that serves about half the "
+                    "no-disc frame and misses the target",
            "errors_on": "crops of the timed frame: central 240x135 + nine 80x45 tiles (64,800 rays), "
                         "against the FP64 oracle's Tsit5 (rtol 1e-10)"}
     for wname, make in (("config1_gas", workloads.config1), ("config1_thin_disc", workloads.config1_thin),
@@ -287,9 +297,12 @@ def headline_block(ctx_cls, device: int, flush, sigma: float, reps: int = 3) -> 
                            "served_fraction": st["surrogate_rays"] / (1920 * 1080),
                            "steps_per_frame": st["steps"], "fp64_steps_per_frame": st["fp64_steps"],
                            "errors": _errors(img, diag, ref, rays, served)}
-        sv, pl, gd = (block[k]["value"] for k in ("surrogate_fp32", "plain_fp32", "fp32_fp64_guarded"))
+        sv, sw, pl, gd = (block[k]["value"] for k in ("surrogate_fp32", "surrogate_fp32_wide_gate", "plain_fp32",
+                                                          "fp32_fp64_guarded"))
         block["surrogate_vs_fp32_fp64_guarded"] = sv / gd
         block["surrogate_vs_plain_fp32"] = sv / pl
+        block["surrogate_wide_gate_vs_fp32_fp64_guarded"] = sw / gd
+        block["surrogate_wide_gate_vs_plain_fp32"] = sw / pl
         block["plain_fp32_vs_fp32_fp64_guarded"] = pl / gd
         out[wname] = block
         ctx.close()
@@ -584,7 +597,7 @@ def main(argv=None):
     ap.add_argument("--surrogate", default=None,
                     help="trained surrogate parameters (.npy; 'shipped' = spacetime_gb300/data/surrogate_kerr.npy) "
                          "for config1_thin / config1_nogas")
-    ap.add_argument("--sigma", type=float, default=4e-4, help="surrogate gate: max predicted std-dev (rad)")
+    ap.add_argument("--sigma", type=float, default=SIGMA_TARGET, help="surrogate gate: max predicted std-dev (rad)")
     ap.add_argument("--fluid-only", action="store_true",
                     help="print only the fluid disc timing (DiscFluidSim / step_sim!) as one JSON line")
     args = ap.parse_args(argv)

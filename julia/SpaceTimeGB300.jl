@@ -1,20 +1,34 @@
 # SpaceTimeGB300.jl -- Julia bindings of libspacetime_gb300.so (include/spacetime_gb300.h).
 #
-# Drop-in methods for SpaceTime.jl's GPU entry points:
-#   render(cam, bh, sky; disc, width, height, samples, relativistic)   (src/raytrace.jl:339)
-#   GB300Context(sky, w, h; disc, volume)                             (MetalPreviewContext, src/metal.jl:129)
-#   render_draft_mtl(ctx, cam, st; width, height, samples, dt, ...)   (src/metal.jl:2040)
-#   render_depth_mtl(ctx, cam, st; nbuckets, ...)                     (src/metal.jl:1945)
-#   DiscFluidSim(vol, disc; ...), step_sim!(sim, ctx; dt, jacobi)     (src/disc_sim.jl:45, 287)
+# Methods of SpaceTime.jl's own GPU entry points, selected by this package's
+# context type (no method of SpaceTime's own types is replaced):
+#   render(cam, bh, GB300Sky(sky); disc, width, height, samples, relativistic)
+#                                       render, src/raytrace.jl:339
+#   GB300Context(sky, w, h; disc, volume)
+#                                       MetalPreviewContext, src/metal.jl:129
+#   render_draft_mtl(ctx::GB300Context, cam, st; width, height, samples, dt, ...)
+#                                       src/metal.jl:2040 (Camera), :2244 (ThinLensCamera),
+#                                       and through it the Sampling overload, src/look.jl:248
+#   render_depth_mtl(ctx::GB300Context, cam, st; nbuckets, ...)
+#                                       src/metal.jl:1945
+#   set_starfield!(ctx::GB300Context; ...)
+#                                       src/metal.jl:257
+#   DiscFluidSim(ctx::GB300Context, vol, disc; ...), step_sim!(sim, ctx; dt, jacobi)
+#                                       src/disc_sim.jl:45, 287
 # Images come back as Matrix{RGBf}(width, height), the reference's layout.
 # This file is not exercised in this repository's CI (no Julia toolchain);
 # the same ABI is tested through Python ctypes (tests/test_abi.py and the GPU tests).
 module SpaceTimeGB300
 
 using SpaceTime
-using SpaceTime: AbstractCamera, Camera, Schwarzschild, Kerr, AccretionDisc, DiscVolume, spin
+using SpaceTime: AbstractCamera, AbstractSpacetime, Camera, ThinLensCamera, Schwarzschild, Kerr,
+                 AccretionDisc, DiscVolume, spin
+import SpaceTime: render, render_draft_mtl, render_depth_mtl, set_starfield!, step_sim!, DiscFluidSim
 using Colors: RGB
+using Random
 using StaticArrays
+
+export GB300Context, GB300Sky
 
 const RGBf = RGB{Float32}
 const libst = get(ENV, "SPACETIME_GB300_LIB", joinpath(@__DIR__, "..", "spacetime_gb300", "libspacetime_gb300.so"))
@@ -137,19 +151,34 @@ function st_render!(ctx::GB300Context, cam::StCamera, bh, p::StRenderParams)
     img
 end
 
-"""`render(cam, bh, sky; disc, width, height, samples, relativistic)` on the GPU with the CPU
-renderer's rules (Keplerian disc, horizon at 2.00001, r_max = max(5|pos|, 100))."""
-function render_gb300(cam::Camera, bh::Schwarzschild, sky; disc=AccretionDisc(), width::Int=400,
-                      height::Int=200, samples::Int=1, relativistic::Bool=false, precision::Int=ST_PREC_FP64)
-    ctx = GB300Context(sky, width, height; disc=disc, emitter=ST_EMIT_KEPLER)
+"""The sky of a `render` call, marking it for the GB300: `render(cam, bh, GB300Sky(sky); ...)`."""
+struct GB300Sky{T}
+    background::T
+end
+
+"""`render(cam, bh, GB300Sky(sky); disc, width, height, samples, jittered, rng, relativistic)`:
+SpaceTime's CPU renderer (src/raytrace.jl:339) on the GPU, with its rules (Keplerian disc,
+horizon at 2.00001, r_max = max(5|pos|, 100)).  `solver` is accepted and ignored (the GPU
+integrates with RK4 in FP64 by default); `dust`, `volume` and `starfield` are not provided."""
+function render(cam::Camera, spacetime::Schwarzschild, sky::GB300Sky;
+                disc::Union{AccretionDisc,Nothing}=AccretionDisc(), dust=nothing, volume=nothing,
+                width::Int=400, height::Int=200, solver=nothing, samples::Int=1, jittered::Bool=true,
+                rng::Random.AbstractRNG=Random.default_rng(), progress::Union{Function,Nothing}=nothing,
+                relativistic::Bool=false, starfield=nothing, precision::Int=ST_PREC_FP64)
+    (dust === nothing && volume === nothing && starfield === nothing) ||
+        throw(ArgumentError("the GB300 render path takes the thin disc only"))
+    ctx = GB300Context(sky.background, width, height; disc=disc, emitter=ST_EMIT_KEPLER)
     p = default_params(ST_SEM_RENDER)
     p.width = width; p.height = height; p.samples = samples
+    p.pixel_jitter = jittered; p.seed = rand(rng, UInt64)
     p.relativistic = relativistic; p.precision = precision
-    st_render!(ctx, st_camera(cam), bh, p)
+    img = st_render!(ctx, st_camera(cam), spacetime, p)
+    progress === nothing || progress(1.0)
+    img
 end
 
 """`set_starfield!(ctx; ...)` (src/metal.jl:257-295), same keywords and defaults."""
-function set_starfield_gb300!(ctx::GB300Context; strength::Real=1.0, texture_weight::Real=0.0,
+function set_starfield!(ctx::GB300Context; strength::Real=1.0, texture_weight::Real=0.0,
                               height::Union{Int,Nothing}=nothing, fov_factor::Real=0.55, density::Real=384,
                               fill::Real=0.5, flux::Real=0.011, psf_pixels::Real=0.5,
                               galactic::NTuple{3,Real}=(0.0, 0.0, 1.0), concentration::Real=3.0,
@@ -166,20 +195,26 @@ end
 keywords (src/metal.jl:2040-2054) including `refine`; with `camera_at` (a function of the
 shutter fraction s in [0, 1) returning a Camera) it renders motion blur, midpoint or
 per-pixel shutter, through st_render_motion."""
-function render_draft_gb300(ctx::GB300Context, cam::Camera, bh; width::Int=1920, height::Int=1080,
-                            samples::Int=2, dt::Real=0.02, fisheye_deg::Real=0.0, aperture_world::Real=0.0,
-                            focus_dist::Real=1.0, relativistic::Bool=false, precision::Int=ST_PREC_FP32,
-                            pixel_jitter::Bool=true, camera_at::Union{Function,Nothing}=nothing,
-                            per_pixel_shutter::Bool=false, order::Int=4, tol::Real=1e-4,
-                            refine::Int=1, refine_var::Real=0.35, refine_graze::Real=0.05,
-                            refine_margin::Int=8)
+function render_draft_mtl(ctx::GB300Context, cam::Camera, bh::AbstractSpacetime; width::Int=1920,
+                          height::Int=1080, samples::Int=2, dt::Real=0.02,
+                          rng::Random.AbstractRNG=Random.default_rng(),
+                          progress::Union{Function,Nothing}=nothing, fisheye_deg::Real=0.0,
+                          aperture_world::Real=0.0, focus_dist::Real=1.0, relativistic::Bool=false,
+                          camera_at::Union{Function,Nothing}=nothing, per_pixel_shutter::Bool=false,
+                          refine::Int=1, refine_var::Real=0.35, refine_graze::Real=0.05,
+                          refine_margin::Int=8, pixel_jitter::Bool=true, order::Int=4, tol::Real=1e-4,
+                          precision::Int=ST_PREC_FP32)
     p = default_params(ST_SEM_DRAFT)
-    p.width = width; p.height = height; p.samples = samples; p.dt = dt
+    p.width = width; p.height = height; p.samples = samples; p.dt = dt; p.seed = rand(rng, UInt64)
     p.relativistic = relativistic; p.precision = precision; p.pixel_jitter = pixel_jitter
     p.order = order; p.tol = tol
     p.refine = refine; p.refine_var = refine_var; p.refine_graze = refine_graze; p.refine_margin = refine_margin
     c = st_camera(cam; fisheye_deg, aperture_world, focus_dist)
-    camera_at === nothing && return st_render!(ctx, c, bh, p)
+    if camera_at === nothing
+        img = st_render!(ctx, c, bh, p)
+        progress === nothing || progress(1.0)
+        return img
+    end
     n = samples^2
     fracs = per_pixel_shutter ? [m / n for m in 0:n] : [(m + 0.5) / n for m in 0:(n - 1)]
     poses = [st_camera(camera_at(s); fisheye_deg, aperture_world, focus_dist) for s in fracs]
@@ -190,13 +225,23 @@ function render_draft_gb300(ctx::GB300Context, cam::Camera, bh; width::Int=1920,
                  Ptr{Float32}, Ptr{Cvoid}, Ptr{Cvoid}),
                 ctx.handle, Ref(c), poses, length(poses), per_pixel_shutter, st, p, out, C_NULL, C_NULL),
           "st_render_motion")
+    progress === nothing || progress(1.0)
     [RGBf(out[1, i, j], out[2, i, j], out[3, i, j]) for i in 1:width, j in 1:height]
+end
+
+"""`render_draft_mtl(ctx, cam::ThinLensCamera, st; ...)` (src/metal.jl:2244-2252): the lens
+as a pinhole camera plus its world-space aperture and focus distance."""
+function render_draft_mtl(ctx::GB300Context, cam::ThinLensCamera, bh::AbstractSpacetime; kwargs...)
+    fov = (cam.sensor_width / 2.0) / cam.focal_length
+    pinhole = Camera(cam.pos, cam.pos + cam.fwd, cam.up_local, fov)
+    ap = cam.aperture * cam.focus_distance / cam.focal_length
+    return render_draft_mtl(ctx, pinhole, bh; kwargs..., aperture_world=ap, focus_dist=cam.focus_distance)
 end
 
 """`render_depth_mtl(ctx, cam, st; width, height, samples, dt, nbuckets, fisheye_deg, relativistic)`
 (src/metal.jl:1935-1990): the (3*nbuckets, width, height) Float32 array of emission binned by path
 length, the last bucket the sky."""
-function render_depth_gb300(ctx::GB300Context, cam::Camera, bh; width::Int=1920, height::Int=1080,
+function render_depth_mtl(ctx::GB300Context, cam::Camera, bh::AbstractSpacetime; width::Int=1920, height::Int=1080,
                             samples::Int=2, dt::Real=0.02, nbuckets::Int=10, fisheye_deg::Real=0.0,
                             relativistic::Bool=false, precision::Int=ST_PREC_FP32)
     nbuckets >= 3 || throw(ArgumentError("nbuckets must be ≥ 3"))
@@ -221,10 +266,10 @@ mutable struct GB300FluidSim
     ctx::GB300Context
 end
 
-"""`DiscFluidSim(vol, disc; M, forcing, drag, relax)` (src/disc_sim.jl:38-91) on the context's gas grid;
-`vol` is the DiscVolume the context was built with."""
-function GB300FluidSim(ctx::GB300Context, vol::DiscVolume, disc::AccretionDisc; M::Real=1.0,
-                       forcing::Real=6.0, drag::Real=0.15, relax::Real=0.05)
+"""`DiscFluidSim(vol, disc; M, forcing, drag, relax)` (src/disc_sim.jl:38-91) on the context's gas
+grid, as `DiscFluidSim(ctx, vol, disc; ...)`; `vol` is the DiscVolume the context was built with."""
+function DiscFluidSim(ctx::GB300Context, vol::DiscVolume, disc::AccretionDisc; M::Real=1.0,
+                      forcing::Real=6.0, drag::Real=0.15, relax::Real=0.05)
     h = Ref{Ptr{Cvoid}}(C_NULL)
     fp = Ref(StFluidParams(M, forcing, drag, relax, vol.scale_height))
     check(ccall((:st_fluid_create, libst), Cint, (Ptr{Ptr{Cvoid}}, Ptr{Cvoid}, Ref{StDisc}, Ref{StFluidParams}),
@@ -236,7 +281,7 @@ end
 
 """`step_sim!(sim, ctx; dt, jacobi)` (src/disc_sim.jl:287-320): one step, queued on the context's
 stream, written into its gas texture."""
-function step_sim_gb300!(sim::GB300FluidSim, ctx::GB300Context; dt::Real=0.05, jacobi::Int=8)
+function step_sim!(sim::GB300FluidSim, ctx::GB300Context; dt::Real=0.05, jacobi::Int=8)
     ctx === sim.ctx || throw(ArgumentError("the solver writes into the context it was built on"))
     check(ccall((:st_fluid_step, libst), Cint, (Ptr{Cvoid}, Cdouble, Cint, Cint, Cint, Ptr{Cfloat}),
                 sim.handle, dt, jacobi, 1, 1, C_NULL), "st_fluid_step")

@@ -69,6 +69,7 @@ struct TraceParams {
   double disc_inner, disc_outer, disc_falloff;
   const float4* lut;         // [lut_size] RGB_
   int lut_size;
+  int lut_stage;             // pixel kernel: copy the table to shared memory first
   double lut_tmin, lut_tmax;
   // volume
   int vol_on;

@@ -2,6 +2,8 @@
 // and their launchers, instantiated per precision in st_trace_*.cu.
 #pragma once
 
+#include <cstdlib>
+
 #include "st_trace.cuh"
 
 // Minimum resident blocks per SM requested from ptxas (register budget);
@@ -42,6 +44,13 @@ __device__ __forceinline__ void flush_counters(const TraceParams& p, unsigned lo
 template <int PREC, int KERR, int VOL, int SEM, int ORD = 4, int DEPTH = 0, int DEFER = 0>
 __global__ void __launch_bounds__(128, ORD == 4 ? ST_MINB : ST_MINB_ADAPTIVE) trace_pixel_kernel(const __grid_constant__ TraceParams p) {
   using R = typename RealOf<PREC>::T;
+  if (p.lut_stage) {
+    // the blackbody table into shared memory, once per block (16 KiB for the
+    // default 1024 entries), before any thread takes a ray
+    const int lin = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+    for (int k = lin; k < p.lut_size; k += nthr) st_lut_smem[k] = __ldg(p.lut + k);
+    __syncthreads();
+  }
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (p.box_cols > 0) {  // a refinement pass over its box only
@@ -193,6 +202,13 @@ __global__ void __launch_bounds__(128, ST_MINB) trace_persistent_kernel(const __
   if (!done && lane == 0 && p.counters) atomicMax(p.counters + CNT_STATUS, (unsigned long long)ST_EBUDGET);
 }
 
+// SPACETIME_GB300_LUT_SMEM=1: the plain pixel kernels stage the blackbody
+// table in shared memory instead of reading it through L1.
+inline bool lut_staging() {
+  const char* e = std::getenv("SPACETIME_GB300_LUT_SMEM");
+  return e && e[0] == '1';
+}
+
 template <int PREC, int KERR, int VOL, int SEM>
 cudaError_t launch_variant(const TraceParams& p, int sched, int bx, int by, int num_sms, cudaStream_t s) {
   if (sched == ST_SCHED_PERSISTENT) {
@@ -228,6 +244,13 @@ cudaError_t launch_variant(const TraceParams& p, int sched, int bx, int by, int 
         trace_resume_kernel<KERR, VOL, SEM><<<(unsigned)((p.defer_cap + 127) / 128), 128, 0, s>>>(p);
         return cudaGetLastError();
       }
+    }
+    if (lut_staging() && p.lut && p.lut_size > 0 && p.lut_size <= 3072 && (p.vol_on || p.disc_on)) {
+      // the blackbody table read from shared memory (at most 48 KiB)
+      TraceParams q = p;
+      q.lut_stage = 1;
+      trace_pixel_kernel<PREC, KERR, VOL, SEM><<<grid, block, (size_t)p.lut_size * sizeof(float4), s>>>(q);
+      return cudaGetLastError();
     }
     trace_pixel_kernel<PREC, KERR, VOL, SEM><<<grid, block, 0, s>>>(p);
   }

@@ -395,6 +395,10 @@ __device__ __forceinline__ R emitter_opz(R sx, R sy, R psx, R psy, R E, R M, R a
 }
 
 // LUT colour; RENDER rounds half to even (Julia round), DRAFT truncates x+0.5.
+// The blackbody table staged in the pixel kernel's dynamic shared memory
+// (TraceParams::lut_stage; the kernel copies it there before its first ray).
+extern __shared__ float4 st_lut_smem[];
+
 template <typename R>
 __device__ __forceinline__ float4 lut_color(const TraceParams& p, R T, bool render_rule) {
   const R tmin = PR(lut_tmin), tmax = PR(lut_tmax);
@@ -408,6 +412,7 @@ __device__ __forceinline__ float4 lut_color(const TraceParams& p, R T, bool rend
     idx = render_rule ? (int)rintf(x) : (int)(x + R(0.5));
   }
   idx = min(max(idx, 0), p.lut_size - 1);
+  if (p.lut_stage) return st_lut_smem[idx];
   return __ldg(p.lut + idx);
 }
 

@@ -87,8 +87,14 @@ def make_sky(width=2048, height=1024, n_stars=20000, seed=1234, mu=-6.0, sigma=0
 # array of shape (nz, nphi, nr) C-order (the same bytes).
 # ---------------------------------------------------------------------------
 
+def _lat(lat, i, j, k):
+    """Lattice value at integer cell (i, j, k), periodic in 64 (_lat,
+    src/disc_volume.jl:287-288)."""
+    return lat[np.mod(i, 64), np.mod(j, 64), np.mod(k, 64)]
+
+
 def _value_noise(lat, x, y, z):
-    n = lat.shape[0]
+    """Trilinear value noise with smoothstep weights (src/disc_volume.jl:290-307)."""
     ix, iy, iz = np.floor(x).astype(np.int64), np.floor(y).astype(np.int64), np.floor(z).astype(np.int64)
     fx, fy, fz = x - ix, y - iy, z - iz
     fx = fx * fx * (3 - 2 * fx)
@@ -96,7 +102,7 @@ def _value_noise(lat, x, y, z):
     fz = fz * fz * (3 - 2 * fz)
 
     def L(i, j, k):
-        return lat[i % n, j % n, k % n]
+        return _lat(lat, i, j, k)
 
     c00 = L(ix, iy, iz) + fx * (L(ix + 1, iy, iz) - L(ix, iy, iz))
     c10 = L(ix, iy + 1, iz) + fx * (L(ix + 1, iy + 1, iz) - L(ix, iy + 1, iz))
@@ -108,14 +114,68 @@ def _value_noise(lat, x, y, z):
 
 
 def _fbm(lat, x, y, z, octaves=4, gain=0.5, lacunarity=2.1):
-    w = np.array([0.5 * gain ** k for k in range(octaves)])
-    w = w / w.sum()
-    out = np.zeros_like(x)
-    f = 1.0
-    for k in range(octaves):
-        out += w[k] * _value_noise(lat, x * f + 17.0 * k, y * f + 31.0 * k, z * f + 7.0 * k)
-        f *= lacunarity
-    return out
+    """Octaves of value noise, each `lacunarity` finer and `gain` weaker,
+    normalised by the sum of amplitudes (_fbm, src/disc_volume.jl:336-347)."""
+    amp, freq, total, norm = 0.5, 1.0, 0.0, 0.0
+    for _ in range(octaves):
+        total = total + amp * _value_noise(lat, x * freq, y * freq, z * freq)
+        norm += amp
+        amp *= gain
+        freq *= lacunarity
+    return total / norm
+
+
+VEIN_SCALE = 2.5  # src/disc_volume.jl:350
+
+
+def _worley(lat, x, y, z, ridge=True):
+    """Cellular noise over the 3x3x3 neighbourhood, one feature point per
+    lattice cell drawn from the lattice at three offsets: F2 - F1 (scaled by
+    VEIN_SCALE) for ridge, else 1 - F1, clamped to [0, 1] (_worley,
+    src/disc_volume.jl:373-399)."""
+    ix, iy, iz = np.floor(x).astype(np.int64), np.floor(y).astype(np.int64), np.floor(z).astype(np.int64)
+    f1 = np.full(np.shape(x), np.inf)
+    f2 = np.full(np.shape(x), np.inf)
+    for dk in (-1, 0, 1):
+        for dj in (-1, 0, 1):
+            for di in (-1, 0, 1):
+                cx, cy, cz = ix + di, iy + dj, iz + dk
+                px = cx + _lat(lat, cx, cy, cz)
+                py = cy + _lat(lat, cx + 17, cy + 31, cz + 7)
+                pz = cz + _lat(lat, cx + 43, cy + 11, cz + 29)
+                d = (px - x) ** 2 + (py - y) ** 2 + (pz - z) ** 2
+                closer = d < f1
+                f2 = np.where(closer, f1, np.where(d < f2, d, f2))
+                f1 = np.where(closer, d, f1)
+    f1, f2 = np.sqrt(f1), np.sqrt(f2)
+    return np.clip(VEIN_SCALE * (f2 - f1), 0.0, 1.0) if ridge else np.clip(1.0 - f1, 0.0, 1.0)
+
+
+def _worley_fbm(lat, x, y, z, octaves, gain=0.5, lacunarity=2.0, ridge=True):
+    """Octaves of Worley noise, normalised (_worley_fbm, src/disc_volume.jl:410-422)."""
+    amp, freq, total, norm = 0.5, 1.0, 0.0, 0.0
+    for _ in range(octaves):
+        total = total + amp * _worley(lat, x * freq, y * freq, z * freq, ridge=ridge)
+        norm += amp
+        amp *= gain
+        freq *= lacunarity
+    return total / norm
+
+
+def _shape_coverage(lat, ls, u, zh, octaves, gain, lac, erosion, escale, eoct, eridge):
+    """Base fBm on (10 ln s, 6 u, zh), carved by the Worley detail field with
+    the cloud remap (base - e w) / (1 - e w) when erosion > 0
+    (_shape_coverage, src/disc_volume.jl:454-464)."""
+    n = _fbm(lat, 10.0 * ls, 6.0 * u, zh, octaves, gain, lac)
+    if erosion <= 0.0:
+        return n
+    w = _worley_fbm(lat, escale * 10.0 * ls, escale * 6.0 * u, escale * zh, eoct, ridge=eridge)
+    ew = erosion * w
+    return np.clip((n - ew) / (1.0 - ew), 0.0, 1.0)
+
+
+WRAP_BLEND = math.radians(18.0)  # src/disc_volume.jl:164
+HAZE_WINDOW = 0.6                # src/disc_volume.jl:173
 
 
 @dataclass
@@ -148,14 +208,27 @@ def disc_radial_profile(s, inner, outer, M=1.0, falloff=0.0):
 
 def make_volume(inner=3.0, outer=20.0, M=1.0, nr=192, nphi=256, nz=48, scale_height=0.08,
                 turbulence=0.8, spiral_twist=4.0, seed=7, falloff=0.0,
-                emission_scale=0.8, opacity_scale=1.2, march_stride=2) -> Volume:
-    """Gas grid in the form of DiscVolume (src/disc_volume.jl:175-271): radial
-    profile x Gaussian slab exp(-z^2/2H^2), H = scale_height*s, times the
-    log-normal turbulence exp(6 t (n - 1/2)) of a seeded value-noise fBm n on
-    sheared (log s, phi + twist log(s/s_in), z/H) coordinates; log-spaced s,
-    periodic phi, z in +-3 H(s_out); peak-normalised."""
+                emission_scale=0.8, opacity_scale=1.2, march_stride=2, noise_octaves=4, noise_gain=0.5,
+                noise_lacunarity=2.1, haze=0.0, haze_height=4.0, erosion=0.0, erosion_scale=4.0,
+                erosion_octaves=3, erosion_mode="billow") -> Volume:
+    """The gas grid of DiscVolume(disc; ...) (src/disc_volume.jl:175-271),
+    restated in numpy with the same keywords and defaults: radial profile x
+    Gaussian slab exp(-z^2/2H^2), H = scale_height s (plus the windowed haze
+    envelope when haze > 0), times the log-normal turbulence
+    exp(6 turbulence (n - 1/2)) of the coverage field n -- value-noise fBm on
+    sheared coordinates (10 ln s, 6 (phi + spiral_twist ln(s/s_in)), 2 z/H),
+    optionally carved by Worley noise -- with the last 18 deg of azimuth
+    crossfaded onto the phi - 2 pi branch; log-spaced s, periodic phi, z in
+    +-3 H(s_out); peak-normalised.  The 64^3 noise lattice is uniform [0, 1)
+    float32 from a seeded numpy generator (the reference draws it from its
+    `rng` argument, a Julia stream this cannot reproduce), so the field has the
+    reference's construction and statistics, not its bytes."""
+    if erosion_mode not in ("vein", "billow"):
+        raise ValueError(f"erosion_mode must be 'vein' or 'billow', got {erosion_mode!r}")
+    eridge = erosion_mode == "vein"
+    ero = min(max(float(erosion), 0.0), 0.95)
     rng = np.random.default_rng(seed)
-    lat = rng.random((64, 64, 64))
+    lat = rng.random((64, 64, 64), dtype=np.float32)
     z_max = 3.0 * scale_height * outer
     log_in, log_out = math.log(inner), math.log(outer)
     k = np.arange(nz)[:, None, None]
@@ -167,26 +240,33 @@ def make_volume(inner=3.0, outer=20.0, M=1.0, nr=192, nphi=256, nz=48, scale_hei
     H = scale_height * s
     rho0 = disc_radial_profile(s, inner, outer, M, falloff)
     slab = np.exp(-z ** 2 / (2 * H ** 2))
-    u = phi + spiral_twist * np.log(s / inner)
+    if haze > 0.0:
+        Hh = haze_height * H
+        t = np.clip((np.abs(z / z_max) - HAZE_WINDOW) / (1.0 - HAZE_WINDOW), 0.0, 1.0)
+        slab = slab + haze * np.exp(-z ** 2 / (2 * Hh ** 2)) * (1.0 - t * t * (3.0 - 2.0 * t))
     shape = np.broadcast_shapes(z.shape, phi.shape, s.shape)
-    X = np.broadcast_to(8.0 * np.log(s), shape)
-    Y = np.broadcast_to(u * (64 / (2 * math.pi)) / 4.0, shape)
-    Zc = np.broadcast_to(2.0 * z / H, shape)
-    n = _fbm(lat, X, Y, Zc)
-    # close the azimuthal seam: crossfade the last 18 deg onto the phi - 2 pi branch
-    blend = math.radians(18.0)
-    Y2 = np.broadcast_to((u - 2 * math.pi) * (64 / (2 * math.pi)) / 4.0, shape)
-    n2 = _fbm(lat, X, Y2, Zc)
-    wphi = np.clip((phi - (2 * math.pi - blend)) / blend, 0.0, 1.0)
-    wphi = wphi * wphi * (3 - 2 * wphi)
-    n = (1 - wphi) * n + wphi * n2
+    u = phi + spiral_twist * np.log(s / inner)
+    ls = np.broadcast_to(np.log(s), shape)
+    U = np.broadcast_to(u, shape)
+    ZH = np.broadcast_to(2.0 * z / H, shape)
+    args = (noise_octaves, noise_gain, noise_lacunarity, ero, erosion_scale, erosion_octaves, eridge)
+    n = _shape_coverage(lat, ls, U, ZH, *args)
+    # the wrap sector: crossfade onto the phi - 2 pi branch of the noise
+    jw = np.nonzero(phi[0, :, 0] > 2 * math.pi - WRAP_BLEND)[0]
+    if jw.size:
+        n2 = _shape_coverage(lat, ls[:, jw, :], U[:, jw, :] - 2 * math.pi, ZH[:, jw, :], *args)
+        w = (phi[:, jw, :] - (2 * math.pi - WRAP_BLEND)) / WRAP_BLEND
+        w = w * w * (3.0 - 2.0 * w)
+        n = np.array(n)
+        n[:, jw, :] = (1.0 - w) * n[:, jw, :] + w * n2
     turb = np.exp(6.0 * turbulence * (n - 0.5))
     dens = (rho0 * slab * turb).astype(np.float32)
     peak = dens.max()
     if peak > 0:
         dens /= peak
     return Volume(np.ascontiguousarray(dens), float(np.float32(log_in)), float(np.float32(log_out)),
-                  float(np.float32(z_max)), scale_height, emission_scale, opacity_scale, march_stride)
+                  float(np.float32(z_max)), float(np.float32(scale_height)), emission_scale, opacity_scale,
+                  march_stride)
 
 
 # ---------------------------------------------------------------------------

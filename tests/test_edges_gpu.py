@@ -122,3 +122,26 @@ def test_smallest_gas_grids_fp32(built_lib, sky, shape):
     assert c["class_mismatch"] <= 0.01 * c["n"], c
     assert c["rad_median"] <= 1e-4, c   # measured 0.6e-6 .. 3e-6
 
+
+
+@pytest.mark.parametrize("prec", [_abi.ST_PREC_FP64, _abi.ST_PREC_FP32])
+def test_non_finite_rays_end_black(built_lib, prec):
+    """The NaN guard (src/metal.jl:1414-1421): a ray whose state stops being
+    finite is captured and painted black, as the reference does, instead of
+    running to its step budget.  A NaN field of view (fov_factor) makes every
+    ray of the frame non-finite from launch (the host does not reject it, as
+    the reference's camera block does not): each ray takes one step, is caught
+    by the guard and ends black, the launch finishes with status OK, and the
+    oracle's twin (which restates the same guard) agrees."""
+    w = workloads.config1_thin().scaled(32, 18)
+    w.params = dict(samples=1, pixel_jitter=0, exit_landing=1)
+    w.cam.fov_factor = float("nan")
+    sky = workloads.sky(512, 256)
+    g = gpu_render(w, sky, prec)
+    assert g.stats["status"] == _abi.ST_OK and g.stats["rays"] == 32 * 18
+    assert g.stats["steps"] == 32 * 18          # one step each: the guard stops them
+    assert (g.image == 0).all()
+    assert ((g.diag["flags"] & _abi.ST_RAY_CAPTURED) > 0).all()
+    assert ((g.diag["flags"] & _abi.ST_RAY_BLACK) > 0).all()
+    ref, rays = oracle_scene(w, sky, O.INT_RK4).render()
+    assert (ref == 0).all() and ((rays["flags"] & O.RAY_BLACK) > 0).all()

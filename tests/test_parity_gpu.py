@@ -143,3 +143,16 @@ def test_guarded_deferral_matches_inline_guards(built_lib, sky, monkeypatch):
     assert c["class_mismatch"] <= 2 and c["dir_median"] <= 1e-6, c
     # the diag flags carry no internal bits
     assert not (a.diag["flags"] & ~0x1FF).any()
+
+
+def test_blackbody_table_in_shared_memory(built_lib, sky, monkeypatch):
+    """SPACETIME_GB300_LUT_SMEM=1 stages the blackbody table in each block's
+    shared memory before the pixel kernel takes rays; the lookups read the same
+    entries, so the frame is bit-identical to the L1 path (gas and thin disc)."""
+    for w in (workloads.config1().scaled(160, 90), workloads.config1_thin().scaled(160, 90)):
+        a = gpu_render(w, sky, FP32, diag=False)
+        monkeypatch.setenv("SPACETIME_GB300_LUT_SMEM", "1")
+        b = gpu_render(w, sky, FP32, diag=False)
+        monkeypatch.delenv("SPACETIME_GB300_LUT_SMEM")
+        np.testing.assert_array_equal(a.image, b.image)
+        assert a.stats["steps"] == b.stats["steps"]
