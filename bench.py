@@ -218,7 +218,8 @@ def _errors(img, diag, ref, rays, served=None):
     d = ang(diag["dir"][esc].astype(np.float64), rays["dir"][esc])
     rel = np.abs(img.astype(np.float64) - ref).sum(-1) / np.maximum(ref.sum(-1), 1e-6)
     out = {"rays": int(img.shape[0]), "escaped_both": int(esc.sum()),
-           "dir_median_rad": float(np.median(d)), "dir_p99_rad": float(np.percentile(d, 99)),
+           "dir_median_rad": float(np.median(d)) if d.size else None,
+           "dir_p99_rad": float(np.percentile(d, 99)) if d.size else None,
            "radiance_rel_median": float(np.median(rel)), "radiance_rel_p99": float(np.percentile(rel, 99)),
            "class_mismatch": int((((diag["flags"] & 8) > 0) != ((rays["flags"] & O.RAY_BLACK) > 0)).sum())}
     if served is not None and served.any():
@@ -488,6 +489,107 @@ def run_reference(args):
     return 0
 
 
+def track_accuracy(ctx, w, p, track_img, workload: str) -> dict:
+    """Errors of timed track frames against the FP64 oracle's Tsit5 (rtol
+    1e-10) on crops of those frames: config 4, frame 0 -- the central 480x270
+    and a 3x3 grid of 160x90 tiles of the 3840x2160 frame; config 2, frames
+    0, 120 and 239 (r = 30 M, mid-fall, inside the horizon) -- the central
+    320x180 of each.  Radiance from the track's own output; exit directions
+    from a single-frame render of the same camera with per-ray records (the
+    same kernel; tracks and single frames are tested equal).  Each frame is
+    also scored against the oracle's fixed-step FP64 twin of the kernel's
+    rules: from inside the horizon the backward rays approach the horizon
+    asymptotically in ingoing Kerr-Schild coordinates, which the kernel's
+    fixed RK4 step crosses (as the reference's Metal kernel does) and Tsit5
+    at rtol 1e-10 does not, so there the twin is the reference's result."""
+    import numpy as np
+    from oracle import oracle as O
+    from spacetime_gb300 import workloads
+    W, H = w.width, w.height
+    sky = workloads.sky()
+    if workload == "config4":
+        frames = [0]
+        crops = [((W - 480) // 2, 480, (H - 270) // 2, 270)] + [
+            (c, 160, r, 90) for c in (320, 1840, 3360) for r in (180, 1035, 1890)]
+    else:
+        frames = [0, len(w.cams) // 2, len(w.cams) - 1]
+        crops = [((W - 320) // 2, 320, (H - 180) // 2, 180)]
+    out = {"oracle": "Tsit5 rtol 1e-10", "frames": {}}
+    for f in frames:
+        wf = w.scaled(W, H)
+        wf.cam = w.cams[f]
+        pd = ctx.params(w.semantics, width=W, height=H, precision=p.precision, r_guard=p.r_guard,
+                        crit_band=p.crit_band, crit_r=p.crit_r, renorm_every=p.renorm_every, **w.params)
+        d = ctx.render_raw(w.cams[f], w.bh, pd, diag=True).diag
+        refs = [O.scene_for(wf, sky, O.INT_TSIT5, rect=rect).render() for rect in crops]
+        ref = np.concatenate([x[0].reshape(-1, 3) for x in refs]).astype(np.float64)
+        rays = np.concatenate([x[1].reshape(-1) for x in refs])
+        img = np.concatenate([track_img[f][r0:r0 + rh, c0:c0 + cw].reshape(-1, 3) for c0, cw, r0, rh in crops])
+        dg = np.concatenate([d[r0:r0 + rh, c0:c0 + cw].reshape(-1) for c0, cw, r0, rh in crops])
+        e = _errors(img, dg, ref, rays)
+        tw = [O.scene_for(wf, sky, O.INT_RK4, rect=rect).render() for rect in crops]
+        e["vs_fp64_twin"] = _errors(img, dg, np.concatenate([x[0].reshape(-1, 3) for x in tw]).astype(np.float64),
+                                    np.concatenate([x[1].reshape(-1) for x in tw]))
+        e["camera_r"] = float(np.linalg.norm(w.cams[f].pos))
+        e["crops"] = [list(c) for c in crops]
+        out["frames"][str(f)] = e
+    return out
+
+
+def run_training(args):
+    """config 3, the learned surrogate's training: FP64 labels generated on the
+    GPU (Sobol-sampled rays, the integrator's own rules), then AdamW steps of
+    the 6 -> 256x4 -> 6 BF16 network at batch 16384, the hidden-layer GEMMs on
+    tcgen05 (default) and on mma.sync (SPACETIME_GB300_TRAIN_MMA=sync), timed
+    with CUDA-synchronised wall clock, each path from the same starting
+    parameters.  Tensor work per step: three hidden layers x (forward, input
+    gradient, weight gradient) x 2 x 16384 x 256 x 256 flops."""
+    import numpy as np
+    import torch
+    from spacetime_gb300.surrogate import Surrogate
+    torch.cuda.set_device(0)
+    batch, steps, warm = 16384, max(args.steps, 1) * 50, max(args.warmup, 3) * 10
+    n_labels = 1 << 21
+    out, t_lab = {}, None
+    for mode in ("tcgen05", "mma_sync"):
+        if mode == "mma_sync":
+            os.environ["SPACETIME_GB300_TRAIN_MMA"] = "sync"
+        sur = Surrogate(0, seed=1)
+        t0 = time.perf_counter()
+        sur.generate(n_labels, offset=0, copy=False)
+        torch.cuda.synchronize()
+        t_lab = t_lab or time.perf_counter() - t0
+        sur.train(warm, batch=batch, lr=1e-3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hist = sur.train(steps, batch=batch, lr=1e-3)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        sur.close()
+        os.environ.pop("SPACETIME_GB300_TRAIN_MMA", None)
+        flops = 3 * 3 * 2.0 * batch * 256 * 256
+        out[mode] = {"ms_per_step": dt / steps * 1e3, "samples_per_s": batch * steps / dt,
+                     "hidden_gemm_tflops": flops * steps / dt / 1e12, "loss_last": float(np.mean(hist[-50:]))}
+    bf16 = measured_peaks().get("bf16_tflops")
+    line = {
+        "metric": "surrogate training samples/s (config3: batch 16384, BF16 6-256x4-6 MLP, AdamW)",
+        "value": out["tcgen05"]["samples_per_s"], "unit": "samples/s", "n_gpus": 1, "steps": steps,
+        "warmup": warm, "ms_per_step": out["tcgen05"]["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": "config3: surrogate training, FP64 labels of Sobol-sampled rays",
+                   "labels": n_labels, "label_rate_per_s": n_labels / t_lab, "batch": batch},
+        "roofline": {"bound": "tensor", "achieved": out["tcgen05"]["hidden_gemm_tflops"], "peak": bf16,
+                     "unit": "TFLOP/s",
+                     "frac": out["tcgen05"]["hidden_gemm_tflops"] / bf16 if bf16 else None, "traffic": None,
+                     "note": "hidden-layer GEMM flops over the whole step time (edge layers, loss, "
+                             "transposes and AdamW included in the time)"},
+        "paths": out,
+        "tcgen05_vs_mma_sync": out["mma_sync"]["ms_per_step"] / out["tcgen05"]["ms_per_step"],
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_track(args):
     """config2 (240 frames 1280x720 free fall, Schwarzschild, thin disc) or
     config4 (8 frames 3840x2160, Kerr a=0.99, boosted 0.3c, gas 512x128x64):
@@ -545,11 +647,16 @@ def run_track(args):
     fp32_measured, _ = measure_fp32_peak(local)
     fp32_peak = fp32_measured or fp32_nominal
     cpu = None
+    accuracy = None
     if not args.no_cpu_baseline:
         try:
             cpu = cpu_baseline(workload=args.workload, frame_size=(w.width, w.height))
         except Exception as e:
             cpu = {"value": None, "sample": f"failed: {e}"}
+        try:
+            accuracy = track_accuracy(ctx, w, p, r.image, args.workload)
+        except Exception as e:  # report, do not fail the bench
+            accuracy = {"failed": str(e)}
     line = {
         "metric": f"Mrays/s {args.workload} track", "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -565,6 +672,7 @@ def run_track(args):
         "e2e": {"value": rays / (float(np.mean(tot)) * 1e-3) / 1e6, "unit": UNIT,
                 "h2d_bytes_per_step": int(st["h2d_bytes"]), "d2h_bytes_per_step": int(rays * 12)},
         "gpu_launches": args.steps * 2, "clocks": clk, "cpu_baseline": cpu,
+        "accuracy_vs_oracle": accuracy,
         "variants": variants,
     }
     print(json.dumps(line))
@@ -592,7 +700,7 @@ def main(argv=None):
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--clocks-csv", default=None)
     ap.add_argument("--workload", default="config1",
-                    choices=["config1", "config1_thin", "config1_nogas", "config2", "config4"],
+                    choices=["config1", "config1_thin", "config1_nogas", "config2", "config3", "config4"],
                     help="config1 is the headline; the others are the remaining benchmark configurations")
     ap.add_argument("--surrogate", default=None,
                     help="trained surrogate parameters (.npy; 'shipped' = spacetime_gb300/data/surrogate_kerr.npy) "
@@ -612,6 +720,8 @@ def main(argv=None):
         return 0
     if args.workload in ("config2", "config4"):
         return run_track(args)
+    if args.workload == "config3":
+        return run_training(args)
 
     import numpy as np
     import torch

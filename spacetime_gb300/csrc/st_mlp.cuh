@@ -168,6 +168,20 @@ struct EpiHidden {
     if (Z) *reinterpret_cast<float2*>(Z + (size_t)m * ldc + n) = make_float2(z0, z1);
     *reinterpret_cast<__nv_bfloat162*>(H + (size_t)m * ldc + n) = __floats2bfloat162_rn(silu(z0), silu(z1));
   }
+  // one element (the tcgen05 GEMM's row-coalesced epilogue): pre() is read
+  // for a whole block before its stores, so no store orders a later load;
+  // store() returns the stored value for the transposed copy T (optional,
+  // [ldc][ldt]: H^T for the weight gradient)
+  __nv_bfloat16* T = nullptr;
+  int ldt = 0;
+  __device__ float pre(int, int) const { return 0.f; }
+  __device__ float store(int m, int n, float v, float) const {
+    const float z = v + bias[n];
+    if (Z) Z[(size_t)m * ldc + n] = z;
+    const __nv_bfloat16 h = __float2bfloat16_rn(silu(z));
+    H[(size_t)m * ldc + n] = h;
+    return __bfloat162float(h);
+  }
 };
 
 // Backward through a hidden layer's input: dZ_prev = (dZ W) * silu'(Z_prev), bf16.
@@ -180,6 +194,14 @@ struct EpiBackDX {
     *reinterpret_cast<__nv_bfloat162*>(dZprev + (size_t)m * ldc + n) =
         __floats2bfloat162_rn(v0 * dsilu(z.x), v1 * dsilu(z.y));
   }
+  __nv_bfloat16* T = nullptr;  // optional transposed copy [ldc][ldt] (dZ^T for the weight gradient)
+  int ldt = 0;
+  __device__ float pre(int m, int n) const { return Zprev[(size_t)m * ldc + n]; }
+  __device__ float store(int m, int n, float v, float z) const {
+    const __nv_bfloat16 d = __float2bfloat16_rn(v * dsilu(z));
+    dZprev[(size_t)m * ldc + n] = d;
+    return __bfloat162float(d);
+  }
 };
 
 // Weight gradient (split-K over the batch): dW[m][n] += acc.
@@ -189,6 +211,13 @@ struct EpiAccum {
   __device__ void operator()(int m, int n, float v0, float v1) const {
     atomicAdd(dW + (size_t)m * ldc + n, v0);
     atomicAdd(dW + (size_t)m * ldc + n + 1, v1);
+  }
+  __nv_bfloat16* T = nullptr;  // (no transposed copy)
+  int ldt = 0;
+  __device__ float pre(int, int) const { return 0.f; }
+  __device__ float store(int m, int n, float v, float) const {
+    atomicAdd(dW + (size_t)m * ldc + n, v);
+    return 0.f;
   }
 };
 

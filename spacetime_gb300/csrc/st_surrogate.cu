@@ -40,6 +40,7 @@
 #include "st_internal.h"
 #include "st_mlp.cuh"
 #include "st_tc.cuh"
+#include "st_tcgemm.cuh"
 #include "st_trace.cuh"
 
 namespace st {
@@ -161,12 +162,14 @@ __global__ void l4_bwd_dx(const float* __restrict__ dout, const float* __restric
 }
 
 // dW4[j][k] += sum_b dout[b][j] H3[b][k], db4[j] += sum_b dout[b][j]; a block
-// of 256 threads (one per k) sweeps ROWS rows.
-constexpr int RED_ROWS = 256;
+// of 256 threads (one per k) sweeps RED_ROWS rows (32: a batch of 16384 gives
+// 512 blocks, enough to cover the GPU's SMs, for one atomic per output per block).
+constexpr int RED_ROWS = 32;
 __global__ void l4_bwd_w(const float* __restrict__ dout, const __nv_bfloat16* __restrict__ H3, float* G, int B) {
   const int k = threadIdx.x;
   const int b0 = blockIdx.x * RED_ROWS, b1 = min(B, b0 + RED_ROWS);
   float acc[NOUT] = {0, 0, 0, 0, 0, 0}, db[NOUT] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 8
   for (int b = b0; b < b1; ++b) {
     const float h = __bfloat162float(H3[(size_t)b * NH + k]);
 #pragma unroll
@@ -188,6 +191,7 @@ __global__ void colsum_bf16(const __nv_bfloat16* __restrict__ D, float* G, size_
   const int n = threadIdx.x;
   const int b0 = blockIdx.x * RED_ROWS, b1 = min(B, b0 + RED_ROWS);
   float s = 0.f;
+#pragma unroll 8
   for (int b = b0; b < b1; ++b) s += __bfloat162float(D[(size_t)b * NH + n]);
   atomicAdd(G + off + n, s);
 }
@@ -197,6 +201,7 @@ __global__ void l0_bwd(const __nv_bfloat16* __restrict__ dZ0, const float* __res
   const int n = threadIdx.x;
   const int b0 = blockIdx.x * RED_ROWS, b1 = min(B, b0 + RED_ROWS);
   float acc[NIN] = {0, 0, 0, 0, 0, 0}, db = 0.f;
+#pragma unroll 8
   for (int b = b0; b < b1; ++b) {
     const float d = __bfloat162float(dZ0[(size_t)b * NH + n]);
     db += d;
@@ -1141,6 +1146,12 @@ struct st_surrogate {
   cudaStream_t stream = nullptr;
   float *P = nullptr, *G = nullptr, *Mm = nullptr, *Vv = nullptr;
   __nv_bfloat16* Wb[3] = {nullptr, nullptr, nullptr};
+  __nv_bfloat16* Wt[3] = {nullptr, nullptr, nullptr};  // W^T (bf16) for the tcgen05 input-gradient GEMM
+  // [256][cap] transposes for the weight gradient: H_0..H_2 (written by the
+  // forward epilogues) and dZ (ping-pong, written by the input-gradient epilogues)
+  __nv_bfloat16* HT[3] = {nullptr, nullptr, nullptr};
+  __nv_bfloat16* dZT[2] = {nullptr, nullptr};
+  int* d_status = nullptr;                              // tcgen05 GEMM: a bounded wait ran out
   unsigned char* Wsw = nullptr;  // hidden layers as swizzled bf16 images for the tcgen05 frame kernel
   float* Psmall = nullptr;       // FP32 edge layers and biases packed for the same kernel
   // frame-pass buffers, rows in tile order: inputs, launch data, outputs, per-tile status
@@ -1180,6 +1191,8 @@ int ensure_work(st_surrogate* s, int rows) {
   cudaFree(s->X);
   for (int l = 0; l < 4; ++l) { cudaFree(s->Z[l]); cudaFree(s->H[l]); }
   cudaFree(s->dZa); cudaFree(s->dZb); cudaFree(s->out); cudaFree(s->dout); cudaFree(s->T);
+  for (int l = 0; l < 3; ++l) { cudaFree(s->HT[l]); s->HT[l] = nullptr; }
+  for (int l = 0; l < 2; ++l) { cudaFree(s->dZT[l]); s->dZT[l] = nullptr; }
   s->cap = 0;
   const size_t R = rows;
   if (cudaMalloc(&s->X, R * NIN * 4) != cudaSuccess) return ST_ENOMEM;
@@ -1192,6 +1205,10 @@ int ensure_work(st_surrogate* s, int rows) {
   if (cudaMalloc(&s->out, R * NOUT * 4) != cudaSuccess || cudaMalloc(&s->dout, R * NOUT * 4) != cudaSuccess ||
       cudaMalloc(&s->T, R * NT * 4) != cudaSuccess)
     return ST_ENOMEM;
+  for (int l = 0; l < 3; ++l)
+    if (cudaMalloc(&s->HT[l], R * NH * 2) != cudaSuccess) return ST_ENOMEM;
+  for (int l = 0; l < 2; ++l)
+    if (cudaMalloc(&s->dZT[l], R * NH * 2) != cudaSuccess) return ST_ENOMEM;
   s->cap = rows;
   return ST_OK;
 }
@@ -1199,6 +1216,8 @@ int ensure_work(st_surrogate* s, int rows) {
 int sync_bf16(st_surrogate* s) {
   for (int l = 0; l < 3; ++l) {
     to_bf16<<<(NH * NH + 255) / 256, 256, 0, s->stream>>>(s->P + OWH[l], s->Wb[l], NH * NH);
+    SC(cudaGetLastError());
+    st::tcg::transpose_bf16<<<dim3(NH / 32, NH / 32), 256, 0, s->stream>>>(s->Wb[l], s->Wt[l], NH, NH);
     SC(cudaGetLastError());
   }
   pack_sw128<<<(3 * NH * NH + 255) / 256, 256, 0, s->stream>>>(s->P, s->Wsw);
@@ -1208,12 +1227,50 @@ int sync_bf16(st_surrogate* s) {
   return ST_OK;
 }
 
+// The hidden-layer GEMMs of training and of st_surrogate_forward run on
+// tcgen05 (st_tcgemm.cuh) unless SPACETIME_GB300_TRAIN_MMA=sync selects the
+// mma.sync kernels (st_mlp.cuh), the same computation on the warp-level path.
+bool train_on_tcgen05() {
+  const char* e = std::getenv("SPACETIME_GB300_TRAIN_MMA");
+  return !(e && std::strcmp(e, "sync") == 0);
+}
+
+// C[M][256] = A[M][K] B[256][K]^T on tcgen05, K split over gridDim.z.
+template <class Epi>
+int gemm_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int M, int K, int splits, Epi epi,
+            int* status, cudaStream_t st) {
+  static bool attr = false;  // one instantiation per epilogue
+  if (!attr) {
+    SC(cudaFuncSetAttribute(st::tcg::gemm_tc_kernel<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)st::tcg::SMEM));
+    attr = true;
+  }
+  st::tcg::gemm_tc_kernel<Epi><<<dim3(1, M / st::tcg::TILE_M, splits), st::tcg::THREADS, st::tcg::SMEM, st>>>(
+      A, lda, B, ldb, K, epi, status);
+  SC(cudaGetLastError());
+  return ST_OK;
+}
+
 // forward of B rows (B multiple of 128) from s->X-like input pointer
 int forward(st_surrogate* s, const float* X, int B, bool keep_z, cudaStream_t st) {
   l0_fwd<<<(B * NH + 255) / 256, 256, 0, st>>>(X, s->P, keep_z ? s->Z[0] : nullptr, s->H[0], B);
   SC(cudaGetLastError());
+  const bool tc5 = train_on_tcgen05();
+  if (tc5 && keep_z) {
+    // training: H_0^T for the first layer's weight gradient (the GEMM
+    // epilogues write H_1^T and H_2^T themselves)
+    st::tcg::transpose_bf16<<<dim3(NH / 32, B / 32), 256, 0, st>>>(s->H[0], s->HT[0], B, NH);
+    SC(cudaGetLastError());
+  }
   for (int l = 1; l <= 3; ++l) {
     EpiHidden e{s->P + OBH[l - 1], keep_z ? s->Z[l] : nullptr, s->H[l], NH};
+    if (tc5) {
+      // Z = H W^T: A = H [B][256], B = W [256 out][256 in], both K-major
+      if (keep_z && l < 3) { e.T = s->HT[l]; e.ldt = B; }
+      const int rc = gemm_tc(s->H[l - 1], NH, s->Wb[l - 1], NH, B, NH, 1, e, s->d_status, st);
+      if (rc != ST_OK) return rc;
+      continue;
+    }
     st::mlp::gemm_bf16_kernel<true, true, EpiHidden>
         <<<dim3(NH / st::mlp::TN, B / st::mlp::TM, 1), st::mlp::GEMM_THREADS, 0, st>>>(s->H[l - 1], NH, s->Wb[l - 1],
                                                                                       NH, NH, e);
@@ -1236,6 +1293,33 @@ int backward(st_surrogate* s, const float* X, int B) {
   __nv_bfloat16* dZ = s->dZa;
   __nv_bfloat16* dZn = s->dZb;
   const int splits = std::max(1, std::min(64, B / 1024));
+  if (train_on_tcgen05()) {
+    // both weight-gradient operands K-major over the batch: dZ^T and H^T
+    // (written transposed by the forward and input-gradient epilogues; dZ_3,
+    // from the FP32 output layer, transposed here); K = 1024 per split keeps
+    // the atomics few and the pipeline full
+    st::tcg::transpose_bf16<<<dim3(NH / 32, B / 32), 256, 0, st>>>(dZ, s->dZT[0], B, NH);
+    SC(cudaGetLastError());
+    int cur = 0;
+    for (int l = 3; l >= 1; --l) {
+      // dW_l[o][i] = sum_b dZ[b][o] H_{l-1}[b][i]: A = dZ^T [256][B], B = H^T [256][B]
+      EpiAccum ea{s->G + OWH[l - 1], NH};
+      int rc = gemm_tc(s->dZT[cur], B, s->HT[l - 1], B, NH, B, splits, ea, s->d_status, st);
+      if (rc != ST_OK) return rc;
+      colsum_bf16<<<nred, NH, 0, st>>>(dZ, s->G, OBH[l - 1], B);
+      SC(cudaGetLastError());
+      // dZ_{l-1}[b][i] = (sum_o dZ[b][o] W[o][i]) silu'(Z_{l-1}): A = dZ [B][256], B = W^T [256 in][256 out]
+      EpiBackDX eb{s->Z[l - 1], dZn, NH};
+      if (l > 1) { eb.T = s->dZT[cur ^ 1]; eb.ldt = B; }
+      rc = gemm_tc(dZ, NH, s->Wt[l - 1], NH, B, NH, 1, eb, s->d_status, st);
+      if (rc != ST_OK) return rc;
+      std::swap(dZ, dZn);
+      cur ^= 1;
+    }
+    l0_bwd<<<nred, NH, 0, st>>>(dZ, X, s->G, B);
+    SC(cudaGetLastError());
+    return ST_OK;
+  }
   for (int l = 3; l >= 1; --l) {
     // dW_l = dZ_l^T H_{l-1}
     EpiAccum ea{s->G + OWH[l - 1], NH};
@@ -1259,6 +1343,18 @@ int backward(st_surrogate* s, const float* X, int B) {
 }
 
 int pad128(long long n) { return (int)((n + 127) / 128 * 128); }
+
+// After a sync: ST_ECUDA (and the flag cleared) when a tcgen05 GEMM's bounded
+// wait ran out since the last check.
+int gemm_status(st_surrogate* s) {
+  int h = 0;
+  SC(cudaMemcpy(&h, s->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    SC(cudaMemset(s->d_status, 0, sizeof(int)));
+    return ST_ECUDA;
+  }
+  return ST_OK;
+}
 
 // Wait bound and first-copy switch of sur_mlp_tc_kernel.  The environment
 // variable SPACETIME_GB300_TC_WAIT_OUT=1 makes every tile's first wait run out
@@ -1318,7 +1414,10 @@ int st_surrogate_create(st_surrogate** out, int device, unsigned long long seed)
       cudaMalloc(&s->loss, 16 * 4) != cudaSuccess)
     return fail(ST_ENOMEM);
   for (int l = 0; l < 3; ++l)
-    if (cudaMalloc(&s->Wb[l], NH * NH * 2) != cudaSuccess) return fail(ST_ENOMEM);
+    if (cudaMalloc(&s->Wb[l], NH * NH * 2) != cudaSuccess || cudaMalloc(&s->Wt[l], NH * NH * 2) != cudaSuccess)
+      return fail(ST_ENOMEM);
+  if (cudaMalloc(&s->d_status, sizeof(int)) != cudaSuccess || cudaMemset(s->d_status, 0, sizeof(int)) != cudaSuccess)
+    return fail(ST_ENOMEM);
   if (cudaMalloc(&s->Wsw, 3 * (size_t)TC_B_BYTES) != cudaSuccess) return fail(ST_ENOMEM);
   if (cudaMalloc(&s->Psmall, TC_SMALL_BYTES) != cudaSuccess) return fail(ST_ENOMEM);
   // He-style uniform initialisation from a splitmix64 stream (host)
@@ -1358,7 +1457,10 @@ void st_surrogate_destroy(st_surrogate* s) {
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
   cudaFree(s->P); cudaFree(s->G); cudaFree(s->Mm); cudaFree(s->Vv); cudaFree(s->loss);
-  for (int l = 0; l < 3; ++l) cudaFree(s->Wb[l]);
+  for (int l = 0; l < 3; ++l) { cudaFree(s->Wb[l]); cudaFree(s->Wt[l]); }
+  cudaFree(s->d_status);
+  for (int l = 0; l < 3; ++l) cudaFree(s->HT[l]);
+  for (int l = 0; l < 2; ++l) cudaFree(s->dZT[l]);
   cudaFree(s->Wsw);
   cudaFree(s->Psmall);
   cudaFree(s->fX); cudaFree(s->fAux); cudaFree(s->fFl); cudaFree(s->fO); cudaFree(s->fStatus);
@@ -1400,7 +1502,7 @@ int st_surrogate_forward(st_surrogate* s, const float* X, int n, float* out) {
   if ((rc = forward(s, s->X, B, false, s->stream)) != ST_OK) return rc;
   SC(cudaMemcpyAsync(out, s->out, (size_t)n * NOUT * 4, cudaMemcpyDeviceToHost, s->stream));
   SC(cudaStreamSynchronize(s->stream));
-  return ST_OK;
+  return gemm_status(s);
 }
 
 // The same network on the frame pass's tensor-core kernel (tcgen05 / TMEM,
@@ -1451,7 +1553,7 @@ int st_surrogate_loss_grad(st_surrogate* s, const float* X, const float* T, int 
   if (loss4) SC(cudaMemcpyAsync(loss4, s->loss, 4 * 4, cudaMemcpyDeviceToHost, st));
   if (grad) SC(cudaMemcpyAsync(grad, s->G, NPARAM * 4, cudaMemcpyDeviceToHost, st));
   SC(cudaStreamSynchronize(st));
-  return ST_OK;
+  return gemm_status(s);
 }
 
 // Generate n labelled samples (Sobol indices offset..offset+n-1) on the
@@ -1510,6 +1612,7 @@ int st_surrogate_train(st_surrogate* s, int steps, int batch, float lr, float we
     if (loss_hist) SC(cudaMemcpyAsync(&lh[k], s->loss, 4, cudaMemcpyDeviceToHost, st));
   }
   SC(cudaStreamSynchronize(st));
+  if ((rc = gemm_status(s)) != ST_OK) return rc;
   if (loss_hist) std::memcpy(loss_hist, lh.data(), steps * sizeof(float));
   return ST_OK;
 }

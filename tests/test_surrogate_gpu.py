@@ -136,3 +136,32 @@ def test_training_reduces_loss(sur):
     assert np.isfinite(hist).all()
     first, last = hist[:10].mean(), hist[-10:].mean()
     assert last < first - 1.0, (first, last)
+
+
+def test_tcgen05_training_gemms_match_mma_sync(sur, monkeypatch):
+    """The training passes' hidden-layer GEMMs run on tcgen05 with TMEM
+    accumulators (forward H W^T, input gradient dZ W, weight gradient
+    dZ^T H split over the batch); SPACETIME_GB300_TRAIN_MMA=sync runs the same
+    computation on mma.sync.  Same bf16 contract, another FP32 summation
+    order: the forward agrees to 2e-3 of the output scale and every parameter
+    tensor's gradient to relative L2 1e-2 (cosine >= 0.9999); both are checked
+    against the FP64 oracle above."""
+    rng = np.random.default_rng(7)
+    X, T = _random_batch(4096, rng)
+    out_tc = sur.forward(X)
+    loss_tc, g_tc = sur.loss_grad(X, T)
+    monkeypatch.setenv("SPACETIME_GB300_TRAIN_MMA", "sync")
+    out_sy = sur.forward(X)
+    loss_sy, g_sy = sur.loss_grad(X, T)
+    monkeypatch.delenv("SPACETIME_GB300_TRAIN_MMA")
+    assert np.abs(out_tc - out_sy).max() <= 2e-3 * np.abs(out_sy).max()
+    assert abs(loss_tc[0] - loss_sy[0]) <= 1e-3 * abs(loss_sy[0])
+    o = 0
+    for name, shape in MO.SIZES:
+        n = int(np.prod(shape))
+        a, b = g_tc[o:o + n].astype(np.float64), g_sy[o:o + n].astype(np.float64)
+        o += n
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        cos = a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30)
+        print(name, rel, cos)
+        assert rel <= 1e-2 and cos >= 0.9999, (name, rel, cos)
