@@ -252,6 +252,7 @@ def headline_block(ctx_cls, device: int, flush, sigma: float, reps: int = 3) -> 
     guards = dict(r_guard=3.0, crit_band=0.05, crit_r=4.0, renorm_every=256)
     arms = {"plain_fp32": dict(precision=_abi.ST_PREC_FP32),
             "fp32_fp64_guarded": dict(precision=_abi.ST_PREC_FP32_GUARDED, **guards),
+            "fp32_df_guarded": dict(precision=_abi.ST_PREC_FP32_GUARDED_DF, **guards),
             "surrogate_fp32": dict(precision=_abi.ST_PREC_FP32, surrogate=1, surrogate_sigma=sigma),
             "surrogate_fp32_wide_gate": dict(precision=_abi.ST_PREC_FP32, surrogate=1,
                                              surrogate_sigma=SIGMA_WIDE)}
@@ -305,6 +306,7 @@ def headline_block(ctx_cls, device: int, flush, sigma: float, reps: int = 3) -> 
         block["surrogate_wide_gate_vs_fp32_fp64_guarded"] = sw / gd
         block["surrogate_wide_gate_vs_plain_fp32"] = sw / pl
         block["plain_fp32_vs_fp32_fp64_guarded"] = pl / gd
+        block["plain_fp32_vs_fp32_df_guarded"] = pl / block["fp32_df_guarded"]["value"]
         out[wname] = block
         ctx.close()
     sur.close()
@@ -602,7 +604,8 @@ def run_track(args):
     from spacetime_gb300 import _abi, autotune, workloads
     from spacetime_gb300.api import Context
     w = workloads.config2() if args.workload == "config2" else workloads.config4()
-    prec = {"fp64": _abi.ST_PREC_FP64, "fp32": _abi.ST_PREC_FP32, "fp32g": _abi.ST_PREC_FP32_GUARDED}[args.precision]
+    prec = {"fp64": _abi.ST_PREC_FP64, "fp32": _abi.ST_PREC_FP32, "fp32g": _abi.ST_PREC_FP32_GUARDED,
+            "fp32gdf": _abi.ST_PREC_FP32_GUARDED_DF}[args.precision]
     ctx = Context(workloads.sky(), disc=w.disc, volume=w.vol, emitter=w.emitter, device=local)
     p = ctx.params(w.semantics, width=w.width, height=w.height, precision=prec, r_guard=args.r_guard,
                    crit_band=args.crit_band, crit_r=args.crit_r, renorm_every=args.renorm, **w.params)
@@ -639,6 +642,17 @@ def run_track(args):
         variants["fp32_fp64_guarded"] = {"value": rays / (msg * 1e-3) / 1e6, "ms_per_step": msg,
                                          "fp64_steps_per_track": rg.stats["fp64_steps"],
                                          "speedup_of_value": (rays / (ms * 1e-3)) / (rays / (msg * 1e-3))}
+        # the same guards with the guard steps in double-float on the FP32 pipe
+        pd = ctx.params(w.semantics, width=w.width, height=w.height, precision=_abi.ST_PREC_FP32_GUARDED_DF,
+                        r_guard=3.0, crit_band=0.05, crit_r=4.0, renorm_every=256, **w.params)
+        autotune.apply(pd, tuned)
+        pd.graph = 1
+        ctx.render_frames_raw(w.cams, w.bh, pd)
+        rd = ctx.render_frames_raw(w.cams, w.bh, pd)
+        msd = rd.stats["kernel_ms"]
+        variants["fp32_df_guarded"] = {"value": rays / (msd * 1e-3) / 1e6, "ms_per_step": msd,
+                                       "guard_steps_per_track": rd.stats["fp64_steps"],
+                                       "speedup_of_value": msd / ms}
     flops = st["steps"] * flops_per_step(kerr) + st["gas_samples"] * FLOPS_GAS_SAMPLE
     achieved = flops / (ms * 1e-3) / 1e12
     sms = torch.cuda.get_device_properties(local).multi_processor_count
@@ -686,7 +700,7 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "fp32g"])
+    ap.add_argument("--precision", default="fp32", choices=["fp64", "fp32", "fp32g", "fp32gdf"])
     ap.add_argument("--no-variants", action="store_true", help="skip the FP32G / FP64 comparison runs")
     ap.add_argument("--schedule", default="pixel", choices=["pixel", "persistent"])
     ap.add_argument("--size", default="1920x1080", help="frame WxH (profiling uses a smaller case)")
@@ -738,7 +752,8 @@ def main(argv=None):
          "config1_nogas": workloads.config1_nogas}[args.workload]()
     W, H = (int(x) for x in args.size.lower().split("x"))
     w = w.scaled(W, H)
-    prec = {"fp64": _abi.ST_PREC_FP64, "fp32": _abi.ST_PREC_FP32, "fp32g": _abi.ST_PREC_FP32_GUARDED}[args.precision]
+    prec = {"fp64": _abi.ST_PREC_FP64, "fp32": _abi.ST_PREC_FP32, "fp32g": _abi.ST_PREC_FP32_GUARDED,
+            "fp32gdf": _abi.ST_PREC_FP32_GUARDED_DF}[args.precision]
     sched = _abi.ST_SCHED_PERSISTENT if args.schedule == "persistent" else _abi.ST_SCHED_PIXEL
     ctx = Context(workloads.sky(), disc=w.disc, volume=w.vol, emitter=w.emitter, device=local)
     sur = None
@@ -821,6 +836,7 @@ def main(argv=None):
         # the same frame with FP64 guards (renormalisation every 256 steps, steps
         # inside 3 M, near-critical rays inside 4 M) and all in FP64
         for name, kw, reps in (("fp32_fp64_guarded", dict(precision=_abi.ST_PREC_FP32_GUARDED), 3),
+                               ("fp32_df_guarded", dict(precision=_abi.ST_PREC_FP32_GUARDED_DF), 3),
                                ("fp64", dict(precision=_abi.ST_PREC_FP64), 1)):
             pv = ctx.params(w.semantics, width=W, height=H, schedule=sched, r_guard=3.0, crit_band=0.05,
                             crit_r=4.0, renorm_every=256, **w.params, **kw)
@@ -882,7 +898,8 @@ def main(argv=None):
                         if args.workload == "config1" else
                         f"{w.name}: config1's camera and hole, {W}x{H}, sky 2048x1024, kernel rules, samples=1",
             "precision": {"fp64": "FP64", "fp32": "FP32 (MUFU sqrt/rcp/exp/log)",
-                          "fp32g": "FP32 RHS, float-float state, FP64 guards"}[args.precision],
+                          "fp32g": "FP32 RHS, float-float state, FP64 guards",
+                          "fp32gdf": "FP32 RHS, float-float state, double-float guards"}[args.precision],
             "guards": {"r_guard": args.r_guard, "crit_band": args.crit_band, "renorm_every": args.renorm},
             "surrogate": ("not applied to this frame: every ray starts inside the gas slab, and the gas "
                           "line integral needs the integrated path; the surrogate arm on this frame and on "

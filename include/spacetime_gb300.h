@@ -94,7 +94,13 @@ enum {
                                 FP64 for steps inside r_guard, for rays in the
                                 critical band, and for the null-constraint
                                 renormalisation */
-  ST_PREC_FP32 = 2           /* plain FP32, as the reference's Metal kernel */
+  ST_PREC_FP32 = 2,          /* plain FP32, as the reference's Metal kernel */
+  ST_PREC_FP32_GUARDED_DF = 3  /* ST_PREC_FP32_GUARDED with the guard steps and
+                                the null renormalisation in double-float
+                                arithmetic (pairs of floats, about 47-bit
+                                significands) on the FP32 pipe instead of
+                                FP64, whose rate on GB300 is a small fraction
+                                of FP32's */
 };
 /* launch schedule */
 enum {

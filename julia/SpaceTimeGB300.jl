@@ -41,6 +41,7 @@ const ST_EMIT_KS_EXACT = 1
 const ST_PREC_FP64 = 0
 const ST_PREC_FP32_GUARDED = 1
 const ST_PREC_FP32 = 2
+const ST_PREC_FP32_GUARDED_DF = 3
 
 struct StCamera
     pos::NTuple{3,Float64}; fwd::NTuple{3,Float64}; right::NTuple{3,Float64}; up::NTuple{3,Float64}

@@ -16,7 +16,7 @@ ST_OK, ST_EINVAL, ST_ECUDA, ST_EBUDGET, ST_ENOMEM, ST_EUNSUPPORTED, ST_ESTATE, S
 ST_PROJ_PINHOLE, ST_PROJ_FISHEYE = 0, 1
 ST_EMIT_KEPLER, ST_EMIT_KS_EXACT = 0, 1
 ST_SEM_RENDER, ST_SEM_DRAFT = 0, 1
-ST_PREC_FP64, ST_PREC_FP32_GUARDED, ST_PREC_FP32 = 0, 1, 2
+ST_PREC_FP64, ST_PREC_FP32_GUARDED, ST_PREC_FP32, ST_PREC_FP32_GUARDED_DF = 0, 1, 2, 3
 ST_SCHED_PIXEL, ST_SCHED_PERSISTENT = 0, 1
 
 ST_RAY_ESCAPED = 1

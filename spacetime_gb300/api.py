@@ -337,7 +337,8 @@ class Context:
 
 
 _PREC = {"fp64": _abi.ST_PREC_FP64, "fp32": _abi.ST_PREC_FP32, "fp32g": _abi.ST_PREC_FP32_GUARDED,
-         "fp32_guarded": _abi.ST_PREC_FP32_GUARDED}
+         "fp32_guarded": _abi.ST_PREC_FP32_GUARDED, "fp32g_df": _abi.ST_PREC_FP32_GUARDED_DF,
+         "fp32_guarded_df": _abi.ST_PREC_FP32_GUARDED_DF}
 
 
 def _prec(x):

@@ -401,7 +401,7 @@ int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, 
   if (!(M > 0.0) || !(std::fabs(a) <= M)) return ST_EINVAL;
   if (rp->width <= 0 || rp->height <= 0 || rp->samples <= 0 || !(rp->dt > 0.0)) return ST_EINVAL;
   if ((long long)rp->width * rp->height > (1ll << 30)) return ST_EINVAL;
-  if (rp->precision < ST_PREC_FP64 || rp->precision > ST_PREC_FP32) return ST_EINVAL;
+  if (rp->precision < ST_PREC_FP64 || rp->precision > ST_PREC_FP32_GUARDED_DF) return ST_EINVAL;
   if (rp->semantics != ST_SEM_RENDER && rp->semantics != ST_SEM_DRAFT) return ST_EINVAL;
   const double rpos = norm3(cam->pos);
   if (!(rpos > 0.0) || !std::isfinite(rpos)) return ST_EINVAL;
@@ -413,6 +413,7 @@ int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, 
   const int order = rp->order == 0 ? 4 : rp->order;
   if (order != 4 && order != 45 && order != 46) return ST_EINVAL;
   if (order != 4 && (rp->semantics != ST_SEM_DRAFT || rp->precision == ST_PREC_FP32_GUARDED ||
+                     rp->precision == ST_PREC_FP32_GUARDED_DF ||
                      rp->schedule == ST_SCHED_PERSISTENT))
     return ST_EUNSUPPORTED;
   if (rp->surrogate) {
@@ -532,7 +533,9 @@ int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, 
   p->counters = ctx->d_counters;
   p->queue = ctx->d_queue;
   p->chunk_steps = rp->chunk_steps > 0 ? rp->chunk_steps : 32;
-  v->prec = rp->precision;
+  // double-float guards run in the FP32_GUARDED kernels
+  v->prec = rp->precision == ST_PREC_FP32_GUARDED_DF ? ST_PREC_FP32_GUARDED : rp->precision;
+  p->guard_df = rp->precision == ST_PREC_FP32_GUARDED_DF ? 1 : 0;
   v->kerr = (a != 0.0) ? 1 : 0;
   v->vol = p->vol_on;
   v->sem = rp->semantics;
@@ -1627,7 +1630,7 @@ int fill_frame_params(const st_camera* cam, const st_spacetime* stp, const st_re
   const double M = stp->M, a = stp->a;
   if (!(M > 0.0) || !(std::fabs(a) <= M)) return ST_EINVAL;
   if (rp->width <= 0 || rp->height <= 0 || !(rp->dt > 0.0)) return ST_EINVAL;
-  if (rp->precision < ST_PREC_FP64 || rp->precision > ST_PREC_FP32) return ST_EINVAL;
+  if (rp->precision < ST_PREC_FP64 || rp->precision > ST_PREC_FP32_GUARDED_DF) return ST_EINVAL;
   const double rpos = norm3(cam->pos);
   if (!(rpos > 0.0) || !std::isfinite(rpos)) return ST_EINVAL;
   std::memset(p, 0, sizeof(*p));
@@ -1669,6 +1672,7 @@ int fill_frame_params(const st_camera* cam, const st_spacetime* stp, const st_re
   p->crit_r2 = rp->crit_r > 0.0 ? rp->crit_r * rp->crit_r : 0.0;
   p->b_crit = 3.0 * std::sqrt(3.0) * M;
   p->renorm_every = rp->renorm_every;
+  p->guard_df = rp->precision == ST_PREC_FP32_GUARDED_DF ? 1 : 0;
   p->chunk_steps = rp->chunk_steps > 0 ? rp->chunk_steps : 32;
   return ST_OK;
 }

@@ -64,6 +64,7 @@ struct TraceParams {
   // FP32_GUARDED policy
   double r_guard2, crit_band, b_crit, crit_r2;
   int renorm_every;
+  int guard_df;              // guard steps in double-float on the FP32 pipe (ST_PREC_FP32_GUARDED_DF)
   // thin disc
   int disc_on, emitter;
   double disc_inner, disc_outer, disc_falloff;
@@ -139,6 +140,9 @@ struct TraceParams {
   // float variant never converts from double inside its loop (on GB300 every
   // double -> float conversion issues on the FP64 pipe)
   struct Flt {
+    // M and a as double-float pairs (hi + lo = the double) for the
+    // double-float guard steps
+    float M_lo, a_lo;
     float M, a, rkill2, vol_rb2, hcap, dt, hcoef, tspan, ds_gas, zmax, r_isco, E_isco, L_isco, opac, emis, disc_inner, disc_outer, disc_falloff, lut_tmin, lut_tmax, ls_in, ls_out, crit_r2, r_guard2, tol, layer_gate;
     // float step rule without per-step divisions: hcoef / M and 1 / max(rkill2, 1e-6)
     float hcoef_m, inv_rkill2;
@@ -160,6 +164,8 @@ struct TraceParams {
 inline void fill_float_copies(TraceParams* p) {
   p->f.M = (float)p->M;
   p->f.a = (float)p->a;
+  p->f.M_lo = (float)(p->M - (double)p->f.M);
+  p->f.a_lo = (float)(p->a - (double)p->f.a);
   p->f.rkill2 = (float)p->rkill2;
   p->f.vol_rb2 = (float)p->vol_rb2;
   p->f.hcap = (float)p->hcap;

@@ -180,7 +180,7 @@ extern "C" int st_render_frames_noalloc(const float* dev_sky_rgba, int sky_w, in
   p.budget_iters = ((long long)p.n_rays + 32) * ((long long)nmax_max / p.chunk_steps + 2);
   p.nmax = nmax_max;
   st::Variant v;
-  v.prec = rp->precision;
+  v.prec = rp->precision == ST_PREC_FP32_GUARDED_DF ? ST_PREC_FP32_GUARDED : rp->precision;
   v.kerr = stp->a != 0.0 ? 1 : 0;
   v.vol = p.vol_on;
   v.sem = ST_SEM_DRAFT;

@@ -1176,6 +1176,198 @@ __device__ __forceinline__ void guard_step_fp64(float* y, float* lo, float pt, d
   }
 }
 
+// ---------------------------------------------------------------------------
+// Double-float arithmetic on the FP32 pipe (ST_PREC_FP32_GUARDED_DF): a value
+// is hi + lo, two floats with |lo| <= ulp(hi) / 2, about 48 significant bits.
+// Sums by Knuth's TwoSum and Dekker's FastTwoSum, products by the exact FMA
+// residual, reciprocal and (reciprocal) square roots by one Newton-Raphson
+// step from the float value (which doubles its ~23 correct bits).  Every
+// operation is a rounded intrinsic, so neither contraction nor fast-math
+// flags of the translation unit change the error-free transformations.
+// ---------------------------------------------------------------------------
+struct df2 {
+  float hi, lo;
+};
+__device__ __forceinline__ df2 dfq(float a) { return df2{a, 0.f}; }
+__device__ __forceinline__ df2 df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return df2{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+// |a| >= |b| (or a = 0)
+__device__ __forceinline__ df2 df_fast(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return df2{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+// x + y with one TwoSum on the high parts and the low parts added in float
+// (Dekker's add): the error is about 2^-47 of max(|x|, |y|) -- an absolute
+// bound at the operands' scale, which is what a guard step's state needs --
+// for half the instructions of the form that also bounds it relative to the
+// sum under cancellation
+__device__ __forceinline__ df2 df_add(df2 x, df2 y) {
+  const df2 s = df_two_sum(x.hi, y.hi);
+  return df_fast(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+__device__ __forceinline__ df2 df_neg(df2 x) { return df2{-x.hi, -x.lo}; }
+__device__ __forceinline__ df2 df_sub(df2 x, df2 y) { return df_add(x, df_neg(y)); }
+__device__ __forceinline__ df2 df_mul(df2 x, df2 y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -p);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  return df_fast(p, e);
+}
+__device__ __forceinline__ df2 df_mulf(df2 x, float f) {
+  const float p = __fmul_rn(x.hi, f);
+  return df_fast(p, __fmaf_rn(x.lo, f, __fmaf_rn(x.hi, f, -p)));
+}
+// x y + z
+__device__ __forceinline__ df2 df_fma(df2 x, df2 y, df2 z) { return df_add(df_mul(x, y), z); }
+// 1 / x: r0 + r0 (1 - x r0)
+__device__ __forceinline__ df2 df_rcp(df2 x) {
+  const float r0 = __frcp_rn(x.hi);
+  const df2 e = df_sub(dfq(1.f), df_mulf(x, r0));
+  return df_fast(r0, __fmul_rn(r0, e.hi));
+}
+// sqrt(x), x > 0: s0 + (x - s0^2) / (2 s0)
+__device__ __forceinline__ df2 df_sqrt(df2 x) {
+  if (!(x.hi > 0.f)) return dfq(0.f);
+  const float s0 = __fsqrt_rn(x.hi);
+  const float p = __fmul_rn(s0, s0);
+  const df2 d = df_sub(x, df2{p, __fmaf_rn(s0, s0, -p)});
+  return df_fast(s0, __fmul_rn(d.hi, __frcp_rn(__fmul_rn(2.f, s0))));
+}
+// 1 / sqrt(x), x > 0: r0 + r0 (1 - x r0^2) / 2
+__device__ __forceinline__ df2 df_rsqrt(df2 x) {
+  const float r0 = __frsqrt_rn(x.hi);
+  const float p = __fmul_rn(r0, r0);
+  const df2 e = df_sub(dfq(1.f), df_mul(x, df2{p, __fmaf_rn(r0, r0, -p)}));
+  return df_fast(r0, __fmul_rn(__fmul_rn(0.5f, r0), e.hi));
+}
+
+// The guard RHS in double-float: the regrouped Kerr form of rhs_kerr_f32 /
+// rhs_kerr_rg64, and the Schwarzschild form of rhs_schw.
+template <int KERR>
+__device__ __forceinline__ void rhs_df(const df2* s, df2 pt, df2 M, df2 a, df2* d) {
+  const df2 x = s[0], y = s[1], z = s[2], px = s[3], py = s[4], pz = s[5];
+  if constexpr (KERR) {
+    const df2 a2 = df_mul(a, a), z2 = df_mul(z, z);
+    const df2 q = df_mul(a2, z2);
+    const df2 wh = df_sub(df_mulf(df_add(df_add(df_mul(x, x), df_mul(y, y)), z2), 0.5f), df_mulf(a2, 0.5f));
+    df2 r2 = df_add(wh, df_sqrt(df_add(df_mul(wh, wh), q)));
+    if (!(r2.hi > 1e-12f)) r2 = dfq(1e-12f);
+    const df2 ir = df_rsqrt(r2), r = df_mul(r2, ir);
+    const df2 isig = df_rcp(df_add(df_mul(r2, r2), q));
+    const df2 r2a = df_add(r2, a2);
+    const df2 ira = df_rcp(r2a);
+    const df2 A = df_add(df_mul(px, x), df_mul(py, y));
+    const df2 B = df_sub(df_mul(px, y), df_mul(py, x));
+    const df2 T = df_mul(df_add(df_mul(r, A), df_mul(a, B)), ira);
+    const df2 Z = df_mul(df_mul(z, pz), ir);
+    const df2 ell = df_sub(df_add(T, Z), pt);
+    const df2 rsig = df_mul(df_mul(r2, r), isig);
+    const df2 fl = df_mul(df_mul(df_mulf(M, 2.f), rsig), ell);
+    const df2 Fi = df_mul(fl, ira);
+    const df2 Fr = df_mul(Fi, r), Fa = df_mul(Fi, a);
+    const df2 flir = df_mul(fl, ir);
+    d[0] = df_sub(df_sub(px, df_mul(Fr, x)), df_mul(Fa, y));
+    d[1] = df_add(df_sub(py, df_mul(Fr, y)), df_mul(Fa, x));
+    d[2] = df_sub(pz, df_mul(flir, z));
+    const df2 dldr = df_sub(df_mul(df_sub(A, df_mul(df_mulf(r, 2.f), T)), ira), df_mul(Z, ir));
+    const df2 inner = df_add(df_mul(df_mul(ell, ir), df_sub(df_mul(df_mulf(q, 2.f), isig), dfq(0.5f))), dldr);
+    const df2 G = df_mul(fl, inner);
+    const df2 Gr = df_mul(G, rsig);
+    d[3] = df_sub(df_add(df_mul(Gr, x), df_mul(Fr, px)), df_mul(Fa, py));
+    d[4] = df_add(df_add(df_mul(Gr, y), df_mul(Fr, py)), df_mul(Fa, px));
+    d[5] = df_add(df_mul(df_mul(z, isig), df_sub(df_mul(df_mul(G, r), r2a), df_mul(df_mul(a2, ell), fl))),
+                  df_mul(flir, pz));
+  } else {
+    const df2 r2 = df_add(df_add(df_mul(x, x), df_mul(y, y)), df_mul(z, z));
+    const df2 ir = df_rsqrt(r2);
+    const df2 f = df_mul(df_mulf(M, 2.f), ir);
+    const df2 kap = df_mul(df_add(df_add(df_mul(x, px), df_mul(y, py)), df_mul(z, pz)), ir);
+    const df2 ell = df_sub(kap, pt);
+    const df2 c1 = df_mul(df_mul(f, ell), ir);
+    const df2 c2 = df_mul(df_mul(c1, df_add(df_mulf(ell, 0.5f), kap)), ir);
+    d[0] = df_sub(px, df_mul(c1, x));
+    d[1] = df_sub(py, df_mul(c1, y));
+    d[2] = df_sub(pz, df_mul(c1, z));
+    d[3] = df_sub(df_mul(c1, px), df_mul(c2, x));
+    d[4] = df_sub(df_mul(c1, py), df_mul(c2, y));
+    d[5] = df_sub(df_mul(c1, pz), df_mul(c2, z));
+  }
+}
+
+// Guard step in double-float on the float-float state (classical RK4).
+template <int KERR>
+__device__ __forceinline__ void guard_step_df(float* y, float* lo, float pt, const TraceParams& p, float h) {
+  df2 Y[6], k1[6], k[6], sum[6], t[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) Y[i] = df2{y[i], lo[i]};
+  const df2 PT = dfq(pt), M = df2{p.f.M, p.f.M_lo}, A = df2{p.f.a, p.f.a_lo};
+  const df2 hd = dfq(h), hh = dfq(0.5f * h);
+  rhs_df<KERR>(Y, PT, M, A, k1);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) { t[i] = df_fma(hh, k1[i], Y[i]); sum[i] = k1[i]; }
+  rhs_df<KERR>(t, PT, M, A, k);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) { sum[i] = df_add(sum[i], df_mulf(k[i], 2.f)); t[i] = df_fma(hh, k[i], Y[i]); }
+  rhs_df<KERR>(t, PT, M, A, k);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) { sum[i] = df_add(sum[i], df_mulf(k[i], 2.f)); t[i] = df_fma(hd, k[i], Y[i]); }
+  rhs_df<KERR>(t, PT, M, A, k);
+  const df2 h6 = df_mul(hd, df_rcp(dfq(6.f)));
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const df2 v = df_add(Y[i], df_mul(h6, df_add(sum[i], k[i])));
+    y[i] = v.hi;
+    lo[i] = v.lo;
+  }
+}
+
+// The null renormalisation (null_renorm) in double-float, for the guarded
+// path's double-float mode.
+template <int KERR>
+__device__ __forceinline__ void renorm_df(float* y, float* lo, float pt, const TraceParams& p) {
+  df2 Y[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) Y[i] = df2{y[i], lo[i]};
+  const df2 M = df2{p.f.M, p.f.M_lo}, PT = dfq(pt);
+  df2 f, L[3];
+  if constexpr (KERR) {
+    const df2 a = df2{p.f.a, p.f.a_lo};
+    const df2 a2 = df_mul(a, a), z2 = df_mul(Y[2], Y[2]), q = df_mul(a2, z2);
+    const df2 wh = df_sub(df_mulf(df_add(df_add(df_mul(Y[0], Y[0]), df_mul(Y[1], Y[1])), z2), 0.5f), df_mulf(a2, 0.5f));
+    df2 r2 = df_add(wh, df_sqrt(df_add(df_mul(wh, wh), q)));
+    if (!(r2.hi > 1e-12f)) r2 = dfq(1e-12f);
+    const df2 ir = df_rsqrt(r2), r = df_mul(r2, ir);
+    const df2 ira = df_rcp(df_add(r2, a2));
+    L[0] = df_mul(df_add(df_mul(r, Y[0]), df_mul(a, Y[1])), ira);
+    L[1] = df_mul(df_sub(df_mul(r, Y[1]), df_mul(a, Y[0])), ira);
+    L[2] = df_mul(Y[2], ir);
+    f = df_mul(df_mul(df_mulf(M, 2.f), df_mul(r2, r)), df_rcp(df_add(df_mul(r2, r2), q)));
+  } else {
+    const df2 ir = df_rsqrt(df_add(df_add(df_mul(Y[0], Y[0]), df_mul(Y[1], Y[1])), df_mul(Y[2], Y[2])));
+    L[0] = df_mul(Y[0], ir); L[1] = df_mul(Y[1], ir); L[2] = df_mul(Y[2], ir);
+    f = df_mul(df_mulf(M, 2.f), ir);
+  }
+  const df2 kap = df_add(df_add(df_mul(L[0], Y[3]), df_mul(L[1], Y[4])), df_mul(L[2], Y[5]));
+  const df2 pp = df_add(df_add(df_mul(Y[3], Y[3]), df_mul(Y[4], Y[4])), df_mul(Y[5], Y[5]));
+  const df2 A = df_sub(pp, df_mul(f, df_mul(kap, kap)));
+  const df2 B = df_mulf(df_mul(df_mul(f, PT), kap), 2.f);
+  const df2 C = df_neg(df_mul(df_add(dfq(1.f), f), df_mul(PT, PT)));
+  const df2 disc = df_sub(df_mul(B, B), df_mulf(df_mul(A, C), 4.f));
+  if (!(A.hi > 0.f) || !(disc.hi >= 0.f)) return;
+  const df2 lam = df_mul(df_sub(df_sqrt(disc), B), df_rcp(df_mulf(A, 2.f)));
+  if (!(lam.hi > 0.9f && lam.hi < 1.1f)) return;
+#pragma unroll
+  for (int i = 3; i < 6; ++i) {
+    const df2 v = df_mul(Y[i], lam);
+    y[i] = v.hi;
+    lo[i] = v.lo;
+  }
+}
+
 template <int KERR>
 __device__ __forceinline__ void renorm_fp64(float* y, float* lo, float pt, double M, double a) {
   double yd[6];
@@ -1313,7 +1505,9 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
     st.k1_valid = true;
   } else if (fp64_step) {
     if constexpr (PREC == ST_PREC_FP32_GUARDED) {
-      guard_step_fp64<KERR>(y, st.lo, st.pt, p.M, p.a, h);
+      // the guard step: FP64, or double-float on the FP32 pipe (counted alike)
+      if (p.guard_df) guard_step_df<KERR>(y, st.lo, st.pt, p, h);
+      else guard_step_fp64<KERR>(y, st.lo, st.pt, p.M, p.a, h);
       ++st.fp64_steps;
     }
   } else {
@@ -1335,7 +1529,10 @@ __device__ __forceinline__ bool step_ray(const TraceParams& p, RayState<typename
   }
   ++st.steps;
   if constexpr (PREC == ST_PREC_FP32_GUARDED) {
-    if (p.renorm_every > 0 && (st.steps % p.renorm_every) == 0) renorm_fp64<KERR>(y, st.lo, st.pt, p.M, p.a);
+    if (p.renorm_every > 0 && (st.steps % p.renorm_every) == 0) {
+      if (p.guard_df) renorm_df<KERR>(y, st.lo, st.pt, p);
+      else renorm_fp64<KERR>(y, st.lo, st.pt, p.M, p.a);
+    }
   }
   if (!(y[0] == y[0]) || !(y[2] == y[2]) || !(y[3] == y[3])) { st.flags |= ST_RAY_CAPTURED; return true; }
 

@@ -6,7 +6,8 @@ renders crops of that same frame: the central 240x135 (shadow, photon ring,
 the densest gas) and a 3x3 grid of 80x45 tiles spread over the frame (mostly
 escaping rays, so the direction statistics see the whole field).
 
-Targets, FP32 and FP32 + FP64 guards, against the oracle's Tsit5 (rtol 1e-10):
+Targets, FP32 and FP32 + guards (FP64, or double-float on the FP32 pipe),
+against the oracle's Tsit5 (rtol 1e-10):
   exit direction median <= 1e-4 rad, p99 <= 1e-3 rad, over rays both sides
   call escaped; radiance relative error (L1 over RGB / oracle L1) median
   <= 1e-3; no more than 0.5 % of rays classified differently.
@@ -38,7 +39,7 @@ from .helpers import angle, compare, gpu_render, oracle_scene
 
 pytestmark = pytest.mark.gpu
 
-FP32, FP32G = _abi.ST_PREC_FP32, _abi.ST_PREC_FP32_GUARDED
+FP32, FP32G, FP32GDF = _abi.ST_PREC_FP32, _abi.ST_PREC_FP32_GUARDED, _abi.ST_PREC_FP32_GUARDED_DF
 GUARDS = dict(r_guard=3.0, crit_band=0.05, crit_r=4.0, renorm_every=256)
 W, H = 1920, 1080
 # (col0, cols, row0, rows): the central 240x135 and nine 80x45 tiles
@@ -76,10 +77,10 @@ def oracle_config1(sky):
     return {"tsit5": _oracle_crops(w, sky, O.INT_TSIT5), "twin": _oracle_crops(w, sky, O.INT_RK4)}
 
 
-@pytest.mark.parametrize("prec", [FP32, FP32G], ids=["fp32", "fp32_guarded"])
+@pytest.mark.parametrize("prec", [FP32, FP32G, FP32GDF], ids=["fp32", "fp32_guarded", "fp32_guarded_df"])
 def test_config1_1080p_against_the_oracle(built_lib, sky, oracle_config1, prec):
     w = workloads.config1()
-    kw = GUARDS if prec == FP32G else {}
+    kw = GUARDS if prec in (FP32G, FP32GDF) else {}
     g = gpu_render(w, sky, prec, **kw)
     assert g.image.shape == (H, W, 3) and np.isfinite(g.image).all()
     gi, gd = _crops(g.image, g.diag)
