@@ -393,6 +393,16 @@ int setup_defer(st_context* ctx, TraceParams* p, const st::Variant& v, size_t nr
   return ST_OK;
 }
 
+// Rays a persistent warp takes from the queue at a time: one 8x4 tile (the
+// measured best of 32, 128 and 512 on the 1080p config-1 frame: 39.3, 41.3,
+// 56.5 ms; larger windows leave long rays in a few warps' windows at the end);
+// SPACETIME_GB300_REFILL_WINDOW=<n> (a multiple of 32) for A/B.
+int refill_window() {
+  const char* e = std::getenv("SPACETIME_GB300_REFILL_WINDOW");
+  const int n = e ? std::atoi(e) : 0;
+  return n >= 32 ? n & ~31 : 32;
+}
+
 // Fill the frame-independent part of TraceParams and the camera of `cam`.
 int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
                 TraceParams* p, st::Variant* v) {
@@ -533,6 +543,7 @@ int fill_params(st_context* ctx, const st_camera* cam, const st_spacetime* stp, 
   p->counters = ctx->d_counters;
   p->queue = ctx->d_queue;
   p->chunk_steps = rp->chunk_steps > 0 ? rp->chunk_steps : 32;
+  p->refill_window = refill_window();
   // double-float guards run in the FP32_GUARDED kernels
   v->prec = rp->precision == ST_PREC_FP32_GUARDED_DF ? ST_PREC_FP32_GUARDED : rp->precision;
   p->guard_df = rp->precision == ST_PREC_FP32_GUARDED_DF ? 1 : 0;
@@ -1673,6 +1684,7 @@ int fill_frame_params(const st_camera* cam, const st_spacetime* stp, const st_re
   p->b_crit = 3.0 * std::sqrt(3.0) * M;
   p->renorm_every = rp->renorm_every;
   p->guard_df = rp->precision == ST_PREC_FP32_GUARDED_DF ? 1 : 0;
+  p->refill_window = 32;
   p->chunk_steps = rp->chunk_steps > 0 ? rp->chunk_steps : 32;
   return ST_OK;
 }

@@ -134,6 +134,7 @@ struct TraceParams {
   int n_frames;              // frames in the table (pixel schedule: grid z)
   int n_rays;                // rays in the queue (frames x pixels)
   int chunk_steps;
+  int refill_window;         // rays a warp takes from the queue at a time (multiple of 32)
   unsigned int* queue;       // queue head (device)
   long long budget_iters;    // per-warp loop bound of the persistent kernel
   // single-precision copies of the parameters the per-step code reads, so a

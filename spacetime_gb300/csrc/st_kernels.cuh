@@ -136,7 +136,11 @@ __global__ void __launch_bounds__(128, ST_MINB) trace_resume_kernel(const __grid
 // Persistent schedule: each warp pulls rays from a device queue; a lane whose
 // ray retires is refilled at the next chunk boundary (warp-ballot refill), so
 // short escaping rays do not idle lanes while photon-ring rays run on.  Queue
-// indices are ordered in 8x4 pixel tiles so a warp's first rays are coherent.
+// indices are ordered in 8x4 pixel tiles.  A warp takes the queue in windows of
+// refill_window consecutive indices (whole tiles: a strip of neighbouring
+// tiles) and refills its lanes from its own window before it takes the next,
+// so a refilled lane traces a neighbour of the rays still running beside it
+// (refill_window = 32: every refill from the global queue, as one tile).
 // The outer loop is bounded by budget_iters; on exhaustion the kernel records
 // ST_EBUDGET in the status counter and returns.
 template <int PREC, int KERR, int VOL, int SEM>
@@ -151,17 +155,35 @@ __global__ void __launch_bounds__(128, ST_MINB) trace_persistent_kernel(const __
   bool active = false, exhausted = false, done = false;
   int out_idx = 0;
   unsigned long long steps = 0, f64 = 0, gas = 0, rays = 0;
+  const unsigned nr = (unsigned)p.n_rays;
+  const unsigned win = p.refill_window >= 32 ? (unsigned)(p.refill_window & ~31) : 32u;
+  unsigned w_next = 0, w_end = 0;  // this warp's window of the queue (warp-uniform)
   for (long long it = 0; it < p.budget_iters; ++it) {
     const unsigned idle = __ballot_sync(FULL, !active);
     if (idle && !exhausted) {
-      unsigned base = 0;
-      if (lane == 0) base = atomicAdd(p.queue, (unsigned)__popc(idle));
-      base = __shfl_sync(FULL, base, 0);
-      if (base >= (unsigned)p.n_rays) exhausted = true;
+      const unsigned need = (unsigned)__popc(idle);
+      const unsigned rank = __popc(idle & ((1u << lane) - 1u));
+      unsigned idx = 0xffffffffu;
+      // first from the window, then from a fresh one
+      const unsigned take = min(need, w_end - w_next);
+      if (!active && rank < take) idx = w_next + rank;
+      w_next += take;
+      if (take < need) {
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(p.queue, win);
+        base = __shfl_sync(FULL, base, 0);
+        if (base >= nr) {
+          exhausted = true;
+        } else {
+          w_next = base;
+          w_end = min(base + win, nr);
+          const unsigned t2 = min(need - take, w_end - w_next);
+          if (!active && rank >= take && rank - take < t2) idx = w_next + (rank - take);
+          w_next += t2;
+        }
+      }
       if (!active) {
-        const unsigned rank = __popc(idle & ((1u << lane) - 1u));
-        const unsigned idx = base + rank;
-        if (idx < (unsigned)p.n_rays) {
+        if (idx < nr) {
           const int frame = (int)idx / per_frame;
           const int w = (int)idx - frame * per_frame;
           const int tile = w >> 5, within = w & 31;
