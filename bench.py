@@ -114,6 +114,11 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def config1_workload(W: int = 1920, H: int = 1080) -> str:
+    return (f"config1: Kerr a=0.9 M=1, static camera r=15 M i=80 deg, Lens(24), {W}x{H}, "
+            "gas 256x64x32 ISCO-25M h=0.05r, sky 2048x1024, kernel rules, samples=1")
+
+
 def measure_fp32_peak(device: int, iters: int = 100000):
     """(TFLOP/s, ms) of the library's FP32 FMA-chain ceiling kernel, or (None, 0)."""
     import ctypes as C
@@ -141,12 +146,31 @@ def dist_env():
     return rank, world, local
 
 
+def _strided_dirs(w, FW: int, FH: int, n_rays: int):
+    """Camera-frame directions (cf, cr, cu) of a strided pixel sample of the
+    whole frame, about n_rays of them, as the pinhole camera maps pixel centres
+    (src/metal.jl:863-872, 907-949): a sample of rays of every length."""
+    import numpy as np
+    stride = max(1, math.ceil(math.sqrt(FW * FH / max(n_rays, 1))))
+    i = np.arange(stride // 2, FW, stride)
+    j = np.arange(stride // 2, FH, stride)
+    I, J = np.meshgrid(i, j)
+    u = (I + 0.5 - FW / 2.0) / (FH / 2.0) * w.cam.fov_factor
+    v = (J + 0.5 - FH / 2.0) / (FH / 2.0) * w.cam.fov_factor
+    nu = np.sqrt(u * u + v * v + 1.0)
+    return np.stack([1.0 / nu, u / nu, v / nu], -1).reshape(-1, 3), stride
+
+
 def cpu_baseline(seconds_target: float = 15.0, threads: int | None = None, gpu_frame=None,
-                 gpu_diag=None, workload: str = "config1", frame_size=(1920, 1080)) -> dict:
-    """The FP64 oracle (Tsit5 rtol 1e-10, kernel rules) on a central crop of
-    the workload, sized for ~10-30 s of host work.  When the GPU frame and its
-    per-ray records are given, the same crop also yields the GPU path's
-    exit-direction and radiance error against the oracle."""
+                 gpu_diag=None, workload: str = "config1", frame_size=(1920, 1080), rate_hint=None) -> dict:
+    """The CPU path timed on the host cores: the oracle's restatement of the
+    reference's CPU renderer loop -- DifferentialEquations-style Tsit5 at the
+    reference's own tolerances (reltol = abstol = 1e-6, src/raytrace.jl:369-373)
+    under the kernel's rules -- on a strided pixel sample of the whole frame,
+    sized for ~10-30 s of host work, so the rate covers rays of every length.  When the
+    GPU frame and its per-ray records are given, a central crop rendered by the
+    oracle at rtol 1e-10 also yields the GPU path's exit-direction and radiance
+    error against it."""
     from oracle import oracle as O
     from spacetime_gb300 import workloads
     FW, FH = frame_size
@@ -155,25 +179,31 @@ def cpu_baseline(seconds_target: float = 15.0, threads: int | None = None, gpu_f
          "config2": lambda: workloads.config2(nframes=240), "config4": workloads.config4}[workload]()
     w = w.scaled(FW, FH)
     threads = threads or os.cpu_count() or 1
-    cw, ch = 48, 27
-    sc = O.scene_for(w, workloads.sky(), O.INT_TSIT5, rect=((FW - cw) // 2, cw, (FH - ch) // 2, ch))
-    t0 = time.perf_counter()
-    sc.render(nthreads=threads, records=False)
-    dt = time.perf_counter() - t0
-    rate = cw * ch / max(dt, 1e-6)
-    n = int(min(max(rate * seconds_target, 2000), 200000))
-    cw = int(min(FW, max(48, round(math.sqrt(n * 16 / 9)))))
-    ch = int(min(FH, max(27, round(cw * 9 / 16))))
-    c0, r0 = (FW - cw) // 2, (FH - ch) // 2
-    sc = O.scene_for(w, workloads.sky(), O.INT_TSIT5, rect=(c0, cw, r0, ch))
-    t0 = time.perf_counter()
-    ref, rays = sc.render(nthreads=threads, records=gpu_frame is not None)
-    dt = time.perf_counter() - t0
-    out = {"value": cw * ch / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-           "sample": f"central {cw}x{ch} crop of the {FW}x{FH} frame ({workload}), FP64 Tsit5 rtol 1e-10, "
-                     f"{dt:.1f} s on {threads} threads"}
+    sky = workloads.sky()
+    tol = dict(rtol=1e-6, atol=1e-6)
+
+    sc = O.scene_for(w, sky, O.INT_TSIT5, **tol)
+
+    def run(n):
+        dirs, stride = _strided_dirs(w, FW, FH, n)
+        t0 = time.perf_counter()
+        sc.trace_dirs(dirs, nthreads=threads)
+        return dirs.shape[0], stride, time.perf_counter() - t0
+
+    if rate_hint:
+        rate = rate_hint
+    else:
+        n0, _, t0 = run(4000)
+        rate = n0 / max(t0, 1e-6)
+    n, stride, dt = run(int(min(max(rate * seconds_target, 2000), 400000)))
+    out = {"value": n / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port", "rate_rays_per_s": n / dt,
+           "sample": f"pixels on a stride-{stride} grid over the whole {FW}x{FH} frame ({workload}; {n} rays), "
+                     f"FP64 Tsit5 reltol = abstol = 1e-6 (the reference renderer's), {dt:.1f} s on {threads} threads"}
     if gpu_frame is not None:
         import numpy as np
+        cw, ch = 596, 335
+        c0, r0 = (FW - cw) // 2, (FH - ch) // 2
+        ref, rays = O.scene_for(w, sky, O.INT_TSIT5, rect=(c0, cw, r0, ch)).render(nthreads=threads)
         g = gpu_frame[r0:r0 + ch, c0:c0 + cw].astype(np.float64)
         d = gpu_diag[r0:r0 + ch, c0:c0 + cw]
         both = ((d["flags"] & 1) > 0) & ((rays["flags"] & O.RAY_ESCAPED) > 0)
@@ -182,6 +212,7 @@ def cpu_baseline(seconds_target: float = 15.0, threads: int | None = None, gpu_f
         ang = 2 * np.arcsin(np.clip(np.linalg.norm(a - b, axis=-1) / 2, 0, 1))
         rel = np.abs(g - ref).sum(-1) / np.maximum(ref.sum(-1), 1e-6)
         out["accuracy_vs_oracle"] = {
+            "oracle": f"Tsit5 rtol 1e-10 on the central {cw}x{ch} crop",
             "rays": int(cw * ch), "escaped_both": int(both.sum()),
             "dir_median_rad": float(np.median(ang)), "dir_p99_rad": float(np.percentile(ang, 99)),
             "radiance_rel_median": float(np.median(rel)), "radiance_rel_p99": float(np.percentile(rel, 99)),
@@ -472,8 +503,12 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     per_step = []
     base = None
+    # each step a bounded sample: the whole run stays near two minutes of host work
+    secs = max(1.0, min(args.ref_seconds, 120.0 / max(args.warmup + args.steps, 1)))
+    rate = None
     for k in range(args.warmup + args.steps):
-        b = cpu_baseline(seconds_target=args.ref_seconds, threads=threads)
+        b = cpu_baseline(seconds_target=secs, threads=threads, rate_hint=rate)
+        rate = b["rate_rays_per_s"]
         if k >= args.warmup:
             per_step.append(b["value"])
             base = b
@@ -482,8 +517,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "config1: Kerr a=0.9 r=15 i=80 1920x1080, gas 256x64x32, kernel rules",
-                   "sample": base["sample"]},
+        "config": {"workload": config1_workload(1920, 1080), "sample": base["sample"]},
         "cpu_baseline": {**base, "value": value},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -893,8 +927,7 @@ def main(argv=None):
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if args.precision != "fp64" else "f64", "data": "synthetic",
         "config": {
-            "workload": (f"config1: Kerr a=0.9 M=1, static camera r=15 M i=80 deg, Lens(24), {W}x{H}, "
-                         "gas 256x64x32 ISCO-25M h=0.05r, sky 2048x1024, kernel rules, samples=1")
+            "workload": config1_workload(W, H)
                         if args.workload == "config1" else
                         f"{w.name}: config1's camera and hole, {W}x{H}, sky 2048x1024, kernel rules, samples=1",
             "precision": {"fp64": "FP64", "fp32": "FP32 (MUFU sqrt/rcp/exp/log)",
