@@ -797,63 +797,127 @@ __global__ void __launch_bounds__(FTHREADS, 1)
 // The same frame pass on the 5th-generation tensor cores (tcgen05 + TMEM)
 // ---------------------------------------------------------------------------
 //
-// One CTA = one 16 x 8 pixel tile = 128 network rows; 8 warps.  Hidden layer
-// l: its weights (a 128 KB K-major 128-byte-swizzled bf16 image, packed once
-// per parameter update by pack_sw128) arrive by bulk copy into shared memory;
-// one thread issues 16 tcgen05.mma (M = 128, N = 256, K = 16) reading the
-// activation tile and the weights straight from shared memory into a 128-lane
-// x 256-column FP32 accumulator in TMEM, and commits to an mbarrier; the
-// epilogue reads the accumulator back (tcgen05.ld, warp w: TMEM lanes
-// 32 (w mod 4).., columns 128 (w / 4)..), adds the bias, applies SiLU and
-// writes bf16 activations back into the swizzled tile for the next layer.
-// The next layer's weights are copied while the epilogue runs.  Layer 0
-// (6 -> 256) and layer 4 (256 -> 6, from the last accumulator, rounded to bf16
-// as the unfused forward stores it) run in FP32.
+// The network pass on the tensor cores (sur_mlp_tc_kernel): a persistent CTA
+// per SM takes 128-row tiles in turn, 16 warps.  All five layers are
+// tcgen05.mma (M = 128, FP32 accumulator of 256 TMEM columns) with both
+// operands K-major, 128-byte-swizzled bf16 in shared memory:
+//  - layer 0 (6 -> 256, FP32 in the unfused forward) as one K = 32 product in
+//    split bf16: A row = (x_hi, x_lo, x_hi, 1, 1), B row n = (w_hi, w_hi, w_lo,
+//    b_hi, b_lo), so x.w + b is carried to ~2^-16 relative (x_lo.w_lo dropped);
+//  - hidden layers 1-3 (256 -> 256, bf16 in the unfused forward too);
+//  - layer 4 (256 -> 6, FP32 weights on the bf16-rounded last activations) as
+//    N = 16: rows 0-5 w_hi, rows 8-13 w_lo, summed in the epilogue.
+// Each layer's weights come by bulk copy into one 128 KB buffer, the next
+// layer's while the current epilogue runs (tcgen05.ld, warp w: TMEM lanes
+// 32 (w mod 4).., columns 64 (w / 4)..; bias, SiLU, bf16 into the activation
+// tile for the next MMA).  Layer 4's 8 KB image stays resident, so the next
+// tile's layer-0 weights and inputs are copied as soon as layer 3's MMAs are
+// done, behind layer 3's epilogue and layer 4.  The epilogue and the MMAs run
+// in turn, not overlapped: schedules that ran the next layer's MMAs under the
+// epilogue (two accumulators, the activations handed over by halves or by
+// quarters) measured slower.
 //
-// Every wait on an mbarrier is bounded; a wait that runs out marks the tile
-// failed (its pixels all go to the integrator, so the frame stays exact) and
-// sets the status word.  Before the CTA frees its TMEM and exits, the thread
-// that issued the copies and the MMAs waits again (bounded) for the one
-// operation still outstanding -- the last armed weight copy or the last
-// committed MMA batch -- so that neither lands in shared memory or TMEM the
-// CTA no longer owns.
+// Every wait on an mbarrier is bounded; a wait that runs out leaves the CTA's
+// current and remaining tiles marked failed (the host sets every tile status
+// to -1 before the launch, a finished tile writes 0), so their pixels all go
+// to the integrator and the frame stays exact, and sets the status word.
+// Before the CTA frees its TMEM and exits, the thread that issued the copies
+// and the MMAs waits again (bounded) for the one operation of each barrier
+// still outstanding -- the last armed copy and the last committed MMA batch --
+// so that neither lands in shared memory or TMEM the CTA no longer owns.
 constexpr uint32_t TC_ROWS = 128, TC_THREADS = 512;
 constexpr uint32_t TC_A_BYTES = TC_ROWS * NH * 2;  // 64 KB activation tile
-constexpr uint32_t TC_B_BYTES = NH * NH * 2;       // 128 KB weight tile
+constexpr uint32_t TC_B_BYTES = NH * NH * 2;       // 128 KB hidden-layer weights
+constexpr uint32_t TC_W0_BYTES = NH * 128;         // layer 0: 256 rows x one K-block of 64
+constexpr uint32_t TC_W4_ROWS = 16;
+constexpr uint32_t TC_W4_BYTES = TC_W4_ROWS * NH * 2;  // layer 4: 16 rows x K = 256
+constexpr size_t TC_WSW_BYTES = TC_W0_BYTES + 3 * (size_t)TC_B_BYTES + TC_W4_BYTES;
 constexpr uint32_t TC_TMEM_COLS = 256;
 constexpr uint32_t TC_WAIT_LIMIT = 1u << 22;
 constexpr uint32_t TC_IDESC = tc::idesc_bf16_f32(128, 256);
+constexpr uint32_t TC_IDESC4 = tc::idesc_bf16_f32(128, TC_W4_ROWS);
 
 struct TcSmall {
-  float X[TC_ROWS * NIN];     // this tile's inputs (bulk copy)
-  // the FP32 edge-layer parameters and hidden biases, in the order of the
-  // packed device image Psmall (bulk copy)
-  float W0[NH * NIN];
-  float b0[NH];
+  // hidden biases and the output bias (FP32), in the order of the packed
+  // device image Psmall (bulk copy)
   float bh[3][NH];
-  float W4[NOUT * NH];
   float b4[8];
+  float X[TC_ROWS * NIN];  // this tile's inputs (bulk copy)
   uint64_t bar_w, bar_mma;
   uint32_t tmem;
   int fail;
 };
-constexpr uint32_t TC_SMALL_BYTES = (NH * NIN + NH + 3 * NH + NOUT * NH + 8) * 4;
-static_assert(TC_SMALL_BYTES % 16 == 0 && offsetof(TcSmall, W0) % 16 == 0, "bulk-copy alignment");
-static_assert(offsetof(TcSmall, b4) + 8 * 4 - offsetof(TcSmall, W0) == TC_SMALL_BYTES, "packed layout");
+constexpr uint32_t TC_SMALL_BYTES = (3 * NH + 8) * 4;
 constexpr uint32_t TC_X_BYTES = TC_ROWS * NIN * 4;
-constexpr size_t TC_SMEM = 1024 + TC_A_BYTES + TC_B_BYTES + sizeof(TcSmall);
+static_assert(TC_SMALL_BYTES % 16 == 0 && offsetof(TcSmall, X) == TC_SMALL_BYTES && TC_X_BYTES % 16 == 0,
+              "bulk-copy sizes and alignment");
+constexpr size_t TC_SMEM = 1024 + TC_A_BYTES + TC_B_BYTES + TC_W4_BYTES + sizeof(TcSmall);
 static_assert(TC_SMEM <= 227 * 1024, "tensor-core surrogate tile exceeds shared memory");
 
-// P (FP32 master weights) -> the three hidden layers' swizzled bf16 images.
+// SiLU of two pre-activations on the packed FP32x2 path:
+// z / (1 + 2^(-z log2 e)), with the hardware base-2 exponential and reciprocal
+// approximations (ex2.approx / rcp.approx, relative error ~2^-22), a finite z
+// giving a finite result (-0 when 2^(-z log2 e) overflows).  (A reciprocal by
+// Newton steps on the FMA pipe, one MUFU operation per value instead of two,
+// measured slower: the epilogue is bound by issue, not by the MUFU pipe.)
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float2 silu2(float2 z) {
+  const float2 t = __fmul2_rn(z, make_float2(-1.4426950408889634f, -1.4426950408889634f));
+  const float2 d = __fadd2_rn(make_float2(ex2_approx(t.x), ex2_approx(t.y)), make_float2(1.f, 1.f));
+  return __fmul2_rn(z, make_float2(rcp_approx(d.x), rcp_approx(d.y)));
+}
+
+// bf16 pair (hi, lo) of an FP32 value: v = hi + lo to ~2^-16 relative.
+__device__ __forceinline__ void split_bf16(float v, __nv_bfloat16* hi, __nv_bfloat16* lo) {
+  *hi = __float2bfloat16_rn(v);
+  *lo = __float2bfloat16_rn(v - __bfloat162float(*hi));
+}
+
+// P (FP32 master weights) -> the weight images of the tcgen05 network pass:
+// [layer 0, 32 KB][hidden layers 1-3, 128 KB each][layer 4, 8 KB].
 __global__ void pack_sw128(const float* __restrict__ P, unsigned char* __restrict__ Wsw) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= 3 * NH * NH) return;
-  const int l = idx / (NH * NH), rem = idx - l * NH * NH;
-  const int n = rem / NH, k = rem - n * NH;
-  const size_t off = l == 0 ? OW1 : l == 1 ? OW2 : OW3;
-  *reinterpret_cast<__nv_bfloat16*>(Wsw + (size_t)l * TC_B_BYTES + tc::sw128_off(n, k, NH)) =
-      __float2bfloat16_rn(P[off + (size_t)n * NH + k]);
+  constexpr int nh = 3 * NH * NH, n0 = NH * 64, n4 = TC_W4_ROWS * NH;
+  if (idx < nh) {
+    const int l = idx / (NH * NH), rem = idx - l * NH * NH;
+    const int n = rem / NH, k = rem - n * NH;
+    *reinterpret_cast<__nv_bfloat16*>(Wsw + TC_W0_BYTES + (size_t)l * TC_B_BYTES + tc::sw128_off(n, k, NH)) =
+        __float2bfloat16_rn(P[(l == 0 ? OW1 : l == 1 ? OW2 : OW3) + (size_t)n * NH + k]);
+  } else if (idx < nh + n0) {
+    // layer 0, row n: k 0-5 w_hi, 6-11 w_hi, 12-17 w_lo, 18 b_hi, 19 b_lo, then 0
+    const int n = (idx - nh) >> 6, k = (idx - nh) & 63;
+    __nv_bfloat16 hi, lo, v = __float2bfloat16_rn(0.f);
+    if (k < 18) {
+      split_bf16(P[OW0 + n * NIN + k % 6], &hi, &lo);
+      v = k < 12 ? hi : lo;
+    } else if (k < 20) {
+      split_bf16(P[OB0 + n], &hi, &lo);
+      v = k == 18 ? hi : lo;
+    }
+    *reinterpret_cast<__nv_bfloat16*>(Wsw + tc::sw128_off(n, k, NH)) = v;
+  } else if (idx < nh + n0 + n4) {
+    // layer 4, row n: 0-5 w_hi of output n, 8-13 w_lo of output n - 8, else 0
+    const int n = (idx - nh - n0) / NH, k = (idx - nh - n0) % NH;
+    __nv_bfloat16 hi, lo, v = __float2bfloat16_rn(0.f);
+    const int o = n & 7;
+    if (o < NOUT) {
+      split_bf16(P[OW4 + o * NH + k], &hi, &lo);
+      v = n < 8 ? hi : lo;
+    }
+    *reinterpret_cast<__nv_bfloat16*>(Wsw + TC_W0_BYTES + 3 * (size_t)TC_B_BYTES + tc::sw128_off(n, k, TC_W4_ROWS)) =
+        v;
+  }
 }
+constexpr int TC_PACK_N = 3 * NH * NH + NH * 64 + TC_W4_ROWS * NH;
 
 // Pixel of row `r` (0..127) of tile `t`: each 32-row group is an 8 x 4 block
 // of the 16 x 8 tile, the warp shape of the trace kernel; -1 off the frame.
@@ -865,23 +929,18 @@ __device__ __forceinline__ int tile_pixel(const TraceParams& p, int t, int r) {
   return (i < p.width && j < p.height) ? j * p.width + i : -1;
 }
 
-// Network inputs of every pixel, row-ordered by tile (one thread per pixel).
-// The FP32 edge layers and hidden biases packed as TcSmall holds them.
+// The hidden and output biases packed as TcSmall holds them.
 __global__ void pack_small(const float* __restrict__ P, float* __restrict__ S) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  constexpr int n0 = NH * NIN, n1 = n0 + NH, n2 = n1 + 3 * NH, n3 = n2 + NOUT * NH, n4 = n3 + 8;
-  if (i >= n4) return;
+  constexpr int n1 = 3 * NH, n2 = n1 + 8;
+  if (i >= n2) return;
   float v;
-  if (i < n0) v = P[OW0 + i];
-  else if (i < n1) v = P[OB0 + (i - n0)];
-  else if (i < n2) {
-    const int l = (i - n1) / NH, k = (i - n1) % NH;
-    v = P[(l == 0 ? OB1 : l == 1 ? OB2 : OB3) + k];
-  } else if (i < n3) v = P[OW4 + (i - n2)];
-  else v = (i - n3) < NOUT ? P[OB4 + (i - n3)] : 0.f;
+  if (i < n1) v = P[(i < NH ? OB1 : i < 2 * NH ? OB2 : OB3) + i % NH];
+  else v = (i - n1) < NOUT ? P[OB4 + (i - n1)] : 0.f;
   S[i] = v;
 }
 
+// Network inputs of every pixel, row-ordered by tile (one thread per pixel).
 template <int KERR>
 __global__ void __launch_bounds__(128) sur_inputs_kernel(const __grid_constant__ TraceParams p,
                                                           const __grid_constant__ SurFrame f, float* __restrict__ X,
@@ -968,25 +1027,24 @@ __global__ void __launch_bounds__(128) sur_scatter_kernel(const __grid_constant_
   list[woff[row >> 5] + __popc(m & ((1u << lane) - 1u))] = tile_pixel(p, blockIdx.x, threadIdx.x);
 }
 
-// The network on the tensor cores: X[tiles*128][6] -> O[tiles*128][6]; one
-// CTA per 128 rows, 16 warps.  tile_status[t] = 0, or 1 when a bounded wait
-// ran out (the gate then integrates the tile's pixels, and the status word is
-// set).  The weights of hidden layer 1, the packed FP32 parameters and the
-// tile's inputs arrive together on one mbarrier.  wait_limit bounds every
-// mbarrier wait (polls); issue_first = 0 leaves the first copies unissued, so
-// the first wait runs out with nothing in flight -- the failure path's test.
+// The network on the tensor cores: X[ntiles*128][6] -> O[ntiles*128][6].
+// Persistent: CTA b takes tiles b, b + gridDim.x, ...; a finished tile writes
+// tile_status[t] = 0 (the host sets -1 before the launch).  wait_limit bounds
+// every mbarrier wait (polls); issue_first = 0 leaves the first copies
+// unissued, so the first wait runs out with nothing in flight -- the failure
+// path's test.
 __global__ void __launch_bounds__(TC_THREADS, 1)
     sur_mlp_tc_kernel(const float* __restrict__ Psmall, const unsigned char* __restrict__ Wsw,
-                      const float* __restrict__ X, float* __restrict__ O, int* __restrict__ tile_status,
+                      const float* __restrict__ X, float* __restrict__ O, int* __restrict__ tile_status, int ntiles,
                       unsigned long long* counters, uint32_t wait_limit, int issue_first) {
   extern __shared__ unsigned char tsm_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(tsm_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  unsigned char* As = base;
-  unsigned char* Bs = base + TC_A_BYTES;
-  TcSmall& S = *reinterpret_cast<TcSmall*>(Bs + TC_B_BYTES);
+  unsigned char* As = base;                // activations, 128 x 256
+  unsigned char* Bs = base + TC_A_BYTES;   // the current layer's weights
+  unsigned char* W4s = Bs + TC_B_BYTES;    // layer 4, resident
+  TcSmall& S = *reinterpret_cast<TcSmall*>(W4s + TC_W4_BYTES);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const size_t row0 = (size_t)blockIdx.x * TC_ROWS;
   if (tid == 0) {
     tc::mbar_init(&S.bar_w, 1);
     tc::mbar_init(&S.bar_mma, 1);
@@ -998,119 +1056,177 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = S.tmem;
-  // thread 0's record of what it has in flight: the phase of bar_w last
-  // armed with copies and of bar_mma last committed to (-1: none)
-  int w_armed = issue_first ? 0 : -1, mma_committed = -1;
-  if (tid == 0 && issue_first) {
-    tc::mbar_expect_tx(&S.bar_w, TC_B_BYTES + TC_SMALL_BYTES + TC_X_BYTES);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) tc::bulk_g2s(Bs + c * 32768, Wsw + c * 32768, 32768, &S.bar_w);
-    tc::bulk_g2s(S.W0, Psmall, TC_SMALL_BYTES, &S.bar_w);
-    tc::bulk_g2s(S.X, X + row0 * NIN, TC_X_BYTES, &S.bar_w);
-  }
-  if (!tc::mbar_wait(&S.bar_w, 0, wait_limit)) S.fail = 1;
-  __syncthreads();
-  const bool start_ok = S.fail == 0;
-  // layer 0 (FP32): thread = hidden unit n over one half of the rows
-  if (start_ok) {
-    const int n = tid & (NH - 1), r0 = (tid >> 8) * (TC_ROWS / 2);
-    float w0[NIN];
-#pragma unroll
-    for (int i = 0; i < NIN; ++i) w0[i] = S.W0[n * NIN + i];
-    const float bb = S.b0[n];
-#pragma unroll 4
-    for (int r = r0; r < r0 + (int)TC_ROWS / 2; ++r) {
-      float z = bb;
-#pragma unroll
-      for (int i = 0; i < NIN; ++i) z += S.X[r * NIN + i] * w0[i];
-      *reinterpret_cast<__nv_bfloat16*>(As + tc::sw128_off(r, n, TC_ROWS)) = __float2bfloat16_rn(mlp::silu(z));
-    }
-  }
-  tc::fence_proxy_async();
-  __syncthreads();
-  const uint32_t a_addr = tc::smem_u32(As), b_addr = tc::smem_u32(Bs);
+  const uint32_t a_addr = tc::smem_u32(As), b_addr = tc::smem_u32(Bs), w4_addr = tc::smem_u32(W4s);
   // warp w: TMEM lanes (rows) 32 (w mod 4).., columns 64 (w div 4)..
   const uint32_t q = warp & 3, cq = warp >> 2;
   const int row = (int)(q * 32 + lane);
-  float part[NOUT] = {0, 0, 0, 0, 0, 0};
-  uint32_t ph = 0;
-  for (int l = 0; l < 3 && start_ok; ++l) {
+  const uint32_t t_lane = tmem + ((q * 32u) << 16);
+  // parity of the next phase of each barrier (every thread keeps the count);
+  // thread 0 also records the last phase it armed / committed and whether it
+  // has seen that phase complete
+  uint32_t pw = 0, pm = 0, w_par = 0, m_par = 0;
+  bool w_out = false, m_out = false;
+  int t = blockIdx.x;
+  if (tid == 0 && issue_first && t < ntiles) {
+    tc::mbar_expect_tx(&S.bar_w, TC_W4_BYTES + TC_SMALL_BYTES + TC_W0_BYTES + TC_X_BYTES);
+    tc::bulk_g2s(W4s, Wsw + TC_W0_BYTES + 3 * (size_t)TC_B_BYTES, TC_W4_BYTES, &S.bar_w);
+    tc::bulk_g2s(S.bh, Psmall, TC_SMALL_BYTES, &S.bar_w);
+    tc::bulk_g2s(Bs, Wsw, TC_W0_BYTES, &S.bar_w);
+    tc::bulk_g2s(S.X, X + (size_t)t * TC_ROWS * NIN, TC_X_BYTES, &S.bar_w);
+    w_out = true;
+    w_par = pw;
+  }
+  for (; t < ntiles; t += gridDim.x) {
+    // this tile's inputs and layer-0 weights (on the first tile also layer 4
+    // and the biases); one thread waits, the CTA barrier releases the rest
     if (tid == 0) {
-      if (tc::mbar_wait(&S.bar_w, ph, wait_limit)) {
-        tc::fence_after_sync();
+      if (!tc::mbar_wait(&S.bar_w, pw, wait_limit)) S.fail = 1;
+      else w_out = false;
+    }
+    pw ^= 1u;
+    __syncthreads();
+    if (S.fail) break;
+    {
+      // layer 0's A tile, K 0..31: thread = (row r, 16-byte chunk c)
+      const int r = tid >> 2, c = tid & 3;
+      uint32_t pk[4];
 #pragma unroll
-        for (int s = 0; s < NH / 16; ++s) {
-          const uint64_t ad = tc::sw128_desc(a_addr + (s >> 2) * (TC_ROWS * 128) + (s & 3) * 32);
-          const uint64_t bd = tc::sw128_desc(b_addr + (s >> 2) * (NH * 128) + (s & 3) * 32);
-          tc::mma_bf16(tmem, ad, bd, TC_IDESC, s > 0 ? 1u : 0u);
+      for (int e = 0; e < 4; ++e) {
+        __nv_bfloat16 h[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int k = c * 8 + 2 * e + u;
+          __nv_bfloat16 hi, lo;
+          split_bf16(S.X[r * NIN + (k < 18 ? k % 6 : 0)], &hi, &lo);
+          h[u] = k < 18 ? ((k >= 6 && k < 12) ? lo : hi) : __float2bfloat16_rn(k < 20 ? 1.f : 0.f);
         }
-        tc::mma_commit(&S.bar_mma);
-        mma_committed = l;
-      } else {
-        S.fail = 1;
+        pk[e] = (uint32_t)__bfloat16_as_ushort(h[0]) | ((uint32_t)__bfloat16_as_ushort(h[1]) << 16);
       }
+      *reinterpret_cast<uint4*>(As + tc::sw128_off(r, c * 8, TC_ROWS)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
     }
+    tc::fence_proxy_async();
     __syncthreads();
-    if (S.fail) break;
-    if (!tc::mbar_wait(&S.bar_mma, ph, wait_limit)) S.fail = 1;
-    ph ^= 1u;
-    __syncthreads();
-    if (S.fail) break;
-    tc::fence_after_sync();
-    if (tid == 0 && l < 2) {
-      // the MMAs are done with the weight tile: fetch the next layer's
-      tc::mbar_expect_tx(&S.bar_w, TC_B_BYTES);
+    if (tid == 0) {
+      tc::fence_after_sync();
 #pragma unroll
-      for (int c = 0; c < 4; ++c)
-        tc::bulk_g2s(Bs + c * 32768, Wsw + (size_t)(l + 1) * TC_B_BYTES + c * 32768, 32768, &S.bar_w);
-      w_armed = l + 1;
+      for (int s = 0; s < 2; ++s)
+        tc::mma_bf16(tmem, tc::sw128_desc(a_addr + s * 32), tc::sw128_desc(b_addr + s * 32), TC_IDESC,
+                     s > 0 ? 1u : 0u);
+      tc::mma_commit(&S.bar_mma);
+      m_out = true;
+      m_par = pm;
     }
+    for (int L = 0; L < 5; ++L) {
+      // layer L's MMAs are done (one thread waits, as above)
+      if (tid == 0) {
+        if (!tc::mbar_wait(&S.bar_mma, pm, wait_limit)) S.fail = 1;
+        else m_out = false;
+      }
+      pm ^= 1u;
+      __syncthreads();
+      if (S.fail) break;
+      tc::fence_after_sync();
+      if (tid == 0 && L < 4) {
+        // the weight buffer is free: the next layer's weights, or after layer
+        // 3 the next tile's layer-0 weights and inputs
+        if (L < 3) {
+          tc::mbar_expect_tx(&S.bar_w, TC_B_BYTES);
+#pragma unroll
+          for (int c = 0; c < 4; ++c)
+            tc::bulk_g2s(Bs + c * 32768, Wsw + TC_W0_BYTES + (size_t)L * TC_B_BYTES + c * 32768, 32768, &S.bar_w);
+          w_out = true;
+          w_par = pw;
+        } else if (t + (int)gridDim.x < ntiles) {
+          tc::mbar_expect_tx(&S.bar_w, TC_W0_BYTES + TC_X_BYTES);
+          tc::bulk_g2s(Bs, Wsw, TC_W0_BYTES, &S.bar_w);
+          tc::bulk_g2s(S.X, X + (size_t)(t + gridDim.x) * TC_ROWS * NIN, TC_X_BYTES, &S.bar_w);
+          w_out = true;
+          w_par = pw;
+        }
+      }
+      if (L == 4) break;
+      // epilogue of layer L: bias (layers 1-3), SiLU, bf16 into the activation tile
+      const float2 bm = L > 0 ? make_float2(1.f, 1.f) : make_float2(0.f, 0.f);
 #pragma unroll 1
-    for (int c = 0; c < 2; ++c) {
-      const int col0 = (int)cq * 64 + c * 32;
-      float v[32];
-      tc::tmem_ld32(tmem + ((q * 32u) << 16) + (uint32_t)col0, v);
-      if (l < 2) {
+      for (int c = 0; c < 2; ++c) {
+        const int col0 = (int)cq * 64 + c * 32;
+        const float2* b2 = reinterpret_cast<const float2*>(S.bh[L > 0 ? L - 1 : 0] + col0);
+        float v[32];
+        tc::tmem_ld32(t_lane + (uint32_t)col0, v);
 #pragma unroll
         for (int ch = 0; ch < 4; ++ch) {
           uint32_t pk[4];
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
-            const int k = col0 + ch * 8 + 2 * e;
-            const __nv_bfloat162 h2 = __floats2bfloat162_rn(mlp::silu(v[ch * 8 + 2 * e] + S.bh[l][k]),
-                                                            mlp::silu(v[ch * 8 + 2 * e + 1] + S.bh[l][k + 1]));
+            const int j = ch * 8 + 2 * e;
+            const float2 h = silu2(__ffma2_rn(b2[j / 2], bm, make_float2(v[j], v[j + 1])));
+            const __nv_bfloat162 h2 = __floats2bfloat162_rn(h.x, h.y);
             pk[e] = *reinterpret_cast<const uint32_t*>(&h2);
           }
           *reinterpret_cast<uint4*>(As + tc::sw128_off(row, col0 + ch * 8, TC_ROWS)) =
               make_uint4(pk[0], pk[1], pk[2], pk[3]);
         }
-      } else {
+      }
+      tc::fence_proxy_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        bool ok = true;
+        if (L < 3) {
+          // layer L + 1 from the copied weights
+          ok = tc::mbar_wait(&S.bar_w, pw, wait_limit);
+          if (ok) {
+            w_out = false;
 #pragma unroll
-        for (int e = 0; e < 32; ++e) {
-          const int k = col0 + e;
-          const float h = __bfloat162float(__float2bfloat16_rn(mlp::silu(v[e] + S.bh[2][k])));
+            for (int s = 0; s < NH / 16; ++s) {
+              const uint64_t ad = tc::sw128_desc(a_addr + (s >> 2) * (TC_ROWS * 128) + (s & 3) * 32);
+              const uint64_t bd = tc::sw128_desc(b_addr + (s >> 2) * (NH * 128) + (s & 3) * 32);
+              tc::mma_bf16(tmem, ad, bd, TC_IDESC, s > 0 ? 1u : 0u);
+            }
+          }
+        } else {
+          // layer 4 from the resident image: N = 16
 #pragma unroll
-          for (int o = 0; o < NOUT; ++o) part[o] += h * S.W4[o * NH + k];
+          for (int s = 0; s < NH / 16; ++s) {
+            const uint64_t ad = tc::sw128_desc(a_addr + (s >> 2) * (TC_ROWS * 128) + (s & 3) * 32);
+            const uint64_t bd = tc::sw128_desc(w4_addr + (s >> 2) * (TC_W4_ROWS * 128) + (s & 3) * 32);
+            tc::mma_bf16(tmem, ad, bd, TC_IDESC4, s > 0 ? 1u : 0u);
+          }
+        }
+        if (ok) {
+          tc::mma_commit(&S.bar_mma);
+          m_out = true;
+          m_par = pm;
+        } else {
+          S.fail = 1;
         }
       }
+      if (L < 3) pw ^= 1u;
+      __syncthreads();
+      if (S.fail) break;
     }
-    tc::fence_proxy_async();
+    if (S.fail) break;
+    // layer 4 epilogue: out = acc[hi] + acc[lo] + b4
+    if (warp < 4) {
+      float v[16];
+      tc::tmem_ld16(t_lane, v);
+      float* o = O + ((size_t)t * TC_ROWS + row) * NOUT;
+#pragma unroll
+      for (int k = 0; k < NOUT; ++k) o[k] = v[k] + v[k + 8] + S.b4[k];
+    }
     tc::fence_before_sync();
-    __syncthreads();
+    __syncthreads();  // the accumulator is read before the next tile's MMAs
+    if (tid == 0) tile_status[t] = 0;
   }
   const bool failed = S.fail != 0;
-  // layer-4 partial sums over each warp's 64 columns, in the weight tile
-  // (free: the last MMA has completed and no copy targets it)
-  float* Opart = reinterpret_cast<float*>(Bs);
-  if (!failed) {
-#pragma unroll
-    for (int o = 0; o < NOUT; ++o) Opart[(cq * TC_ROWS + row) * NOUT + o] = part[o];
-  } else if (tid == 0) {
-    // drain: a parity wait on the last armed / committed phase returns at
-    // once if it has completed and otherwise waits for it (each barrier has
-    // at most one phase outstanding)
-    if (w_armed >= 0) (void)tc::mbar_wait(&S.bar_w, (uint32_t)w_armed & 1u, wait_limit);
-    if (mma_committed >= 0) (void)tc::mbar_wait(&S.bar_mma, (uint32_t)mma_committed & 1u, wait_limit);
+  if (failed && tid == 0) {
+    // drain: a parity wait on the last armed / committed phase returns at once
+    // if it has completed and otherwise waits for it (each barrier has at most
+    // one phase outstanding)
+    if (w_out) (void)tc::mbar_wait(&S.bar_w, w_par, wait_limit);
+    if (m_out) (void)tc::mbar_wait(&S.bar_mma, m_par, wait_limit);
+    if (counters) atomicMax(counters + CNT_STATUS, (unsigned long long)ST_ECUDA);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -1118,18 +1234,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     tc::fence_after_sync();
     tc::tmem_dealloc(tmem, TC_TMEM_COLS);
   }
-  if (tid == 0) {
-    tile_status[blockIdx.x] = failed ? 1 : 0;
-    if (failed && counters) atomicMax(counters + CNT_STATUS, (unsigned long long)ST_ECUDA);
-  }
-  if (failed) return;
-  for (int c = tid; c < (int)(TC_ROWS * NOUT); c += TC_THREADS) {
-    const int r = c / NOUT, k = c - r * NOUT;
-    float acc = S.b4[k];
-#pragma unroll
-    for (int g = 0; g < 4; ++g) acc += Opart[(g * TC_ROWS + r) * NOUT + k];
-    O[row0 * NOUT + c] = acc;
-  }
+}
+
+// Grid of the persistent network kernel: one CTA per SM, at most one per tile.
+inline int tc_grid(int ntiles) {
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0)
+    nsm = 1;
+  return ntiles < nsm ? ntiles : nsm;
 }
 
 }  // namespace sur
@@ -1220,7 +1333,7 @@ int sync_bf16(st_surrogate* s) {
     st::tcg::transpose_bf16<<<dim3(NH / 32, NH / 32), 256, 0, s->stream>>>(s->Wb[l], s->Wt[l], NH, NH);
     SC(cudaGetLastError());
   }
-  pack_sw128<<<(3 * NH * NH + 255) / 256, 256, 0, s->stream>>>(s->P, s->Wsw);
+  pack_sw128<<<(TC_PACK_N + 255) / 256, 256, 0, s->stream>>>(s->P, s->Wsw);
   SC(cudaGetLastError());
   pack_small<<<(TC_SMALL_BYTES / 4 + 255) / 256, 256, 0, s->stream>>>(s->P, s->Psmall);
   SC(cudaGetLastError());
@@ -1418,7 +1531,7 @@ int st_surrogate_create(st_surrogate** out, int device, unsigned long long seed)
       return fail(ST_ENOMEM);
   if (cudaMalloc(&s->d_status, sizeof(int)) != cudaSuccess || cudaMemset(s->d_status, 0, sizeof(int)) != cudaSuccess)
     return fail(ST_ENOMEM);
-  if (cudaMalloc(&s->Wsw, 3 * (size_t)TC_B_BYTES) != cudaSuccess) return fail(ST_ENOMEM);
+  if (cudaMalloc(&s->Wsw, TC_WSW_BYTES) != cudaSuccess) return fail(ST_ENOMEM);
   if (cudaMalloc(&s->Psmall, TC_SMALL_BYTES) != cudaSuccess) return fail(ST_ENOMEM);
   // He-style uniform initialisation from a splitmix64 stream (host)
   std::vector<float> P(NPARAM, 0.f);
@@ -1518,9 +1631,10 @@ int st_surrogate_forward_tc(st_surrogate* s, const float* X, int n, float* out) 
   SC(cudaMemsetAsync(s->fX, 0, (size_t)B * NIN * 4, st));
   SC(cudaMemcpyAsync(s->fX, X, (size_t)n * NIN * 4, cudaMemcpyHostToDevice, st));
   SC(cudaFuncSetAttribute(sur_mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+  SC(cudaMemsetAsync(s->fStatus, 0xFF, (size_t)nb * sizeof(int), st));  // -1 until a tile finishes
   const TcWait tw = tc_wait_mode();
-  sur_mlp_tc_kernel<<<nb, TC_THREADS, TC_SMEM, st>>>(s->Psmall, s->Wsw, s->fX, s->fO, s->fStatus, nullptr, tw.limit,
-                                                     tw.issue_first);
+  sur_mlp_tc_kernel<<<tc_grid(nb), TC_THREADS, TC_SMEM, st>>>(s->Psmall, s->Wsw, s->fX, s->fO, s->fStatus, nb,
+                                                               nullptr, tw.limit, tw.issue_first);
   SC(cudaGetLastError());
   std::vector<int> status(nb);
   SC(cudaMemcpyAsync(out, s->fO, (size_t)n * NOUT * 4, cudaMemcpyDeviceToHost, st));
@@ -1642,10 +1756,10 @@ int surrogate_frame(st_surrogate* s, const TraceParams& p, const Variant& v, con
     SC(cudaGetLastError());
     SC(cudaFuncSetAttribute(sur::sur_mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)sur::TC_SMEM));
+    SC(cudaMemsetAsync(s->fStatus, 0xFF, (size_t)nb * sizeof(int), stream));  // -1 until a tile finishes
     const TcWait tw = tc_wait_mode();
-    sur::sur_mlp_tc_kernel<<<nb, sur::TC_THREADS, sur::TC_SMEM, stream>>>(s->Psmall, s->Wsw, s->fX, s->fO,
-                                                                          s->fStatus, p.counters, tw.limit,
-                                                                          tw.issue_first);
+    sur::sur_mlp_tc_kernel<<<sur::tc_grid((int)nb), sur::TC_THREADS, sur::TC_SMEM, stream>>>(
+        s->Psmall, s->Wsw, s->fX, s->fO, s->fStatus, (int)nb, p.counters, tw.limit, tw.issue_first);
     SC(cudaGetLastError());
     sur::sur_gate_kernel<<<nb, 128, 0, stream>>>(p, f, s->fO, s->fAux, s->fFl, s->fStatus, s->fMask, s->fCount);
     SC(cudaGetLastError());
