@@ -48,7 +48,12 @@ SIGMA_WIDE = 4e-4
 FLOPS_RHS_KERR = 126
 FLOPS_RHS_SCHW = 34
 FLOPS_RK4_UPDATE = 74
-FLOPS_GAS_SAMPLE = 150
+# One gas sample (march_gas + sample_volume, FP64 form): 52 for every sample
+# (position and its cylinder radius and angle, the log-radial grid index, the
+# trilinear density) plus 77 for an emitting one (blackbody temperature, the
+# emitter's redshift, the colour-table index, Planck factor, absorption,
+# compositing); 62 % of the config-1 frame's samples emit, so 52 + 0.62 * 77.
+FLOPS_GAS_SAMPLE = 100
 
 
 def flops_per_step(kerr: bool) -> int:
