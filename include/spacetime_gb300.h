@@ -397,7 +397,11 @@ int st_render_layered_ring(st_context* ctx, const st_camera* cam, const st_space
                            int ring_box, float* out_rgb, st_ray_diag* diag, st_stats* stats);
 
 /* Render `nframes` camera poses (a camera track) in one persistent launch;
- * out_rgb holds nframes frames back to back. */
+ * out_rgb holds nframes frames back to back.  With p->surrogate the frames
+ * run one after another (a surrogate pass and a trace launch each, the
+ * network's inputs in each frame's own static frame); every camera must lie
+ * in the network's domain (KS radius 4-50 M above the equatorial plane,
+ * 0 <= a <= 0.99, M = 1), else ST_EUNSUPPORTED and nothing is written. */
 int st_render_frames(st_context* ctx, int nframes, const st_camera* cams,
                      const st_spacetime* st, const st_render_params* p,
                      float* out_rgb, st_stats* stats);

@@ -679,6 +679,15 @@ long long queue_budget(long long computed) {
   return computed;
 }
 
+// The learned surrogate's domain: camera KS radius in [4, 50] M, above the
+// equatorial plane, 0 <= a <= 0.99 M, M = 1 (the training ranges).  Fills
+// the camera's static frame.
+bool surrogate_domain(const st_camera* cam, const st_spacetime* stp, st::SurFrame* sf) {
+  st::host_static_frame(cam->pos, stp->M, stp->a, sf);
+  return sf->r >= 4.0 * stp->M && sf->r <= 50.0 * stp->M && sf->th <= 1.5707963267948966 && stp->a >= 0.0 &&
+         stp->a <= 0.99 * stp->M && stp->M == 1.0;
+}
+
 int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, const st_render_params* rp,
               float* host_rgb, st_ray_diag* host_diag, const float** dev_rgba, st_stats* stats,
               const Motion* mo = nullptr, const Depth* depth = nullptr) {
@@ -698,11 +707,7 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
   cudaStream_t s = ctx->stream;
   st::SurFrame sf{};
   if (rp->surrogate) {
-    // network domain: camera r in [4, 50] M, above the plane, 0 <= a <= 0.99
-    st::host_static_frame(cam->pos, stp->M, stp->a, &sf);
-    if (!(sf.r >= 4.0 * stp->M && sf.r <= 50.0 * stp->M && sf.th <= 1.5707963267948966 && stp->a >= 0.0 &&
-          stp->a <= 0.99 * stp->M && stp->M == 1.0))
-      return ST_EUNSUPPORTED;
+    if (!surrogate_domain(cam, stp, &sf)) return ST_EUNSUPPORTED;
     sf.sigma_max = rp->surrogate_sigma > 0.0 ? rp->surrogate_sigma : 1e-4;
     if ((rc = ensure(&ctx->d_list, &ctx->list_cap, npix)) != ST_OK) return rc;
     if (!ctx->d_count && cudaMalloc(&ctx->d_count, sizeof(int)) != cudaSuccess) return ST_ENOMEM;
@@ -1484,10 +1489,56 @@ int st_render_device(st_context* ctx, const st_camera* cam, const st_spacetime* 
   return do_render(ctx, cam, st, p, nullptr, nullptr, dev_rgba, stats);
 }
 
+// A camera track with the learned surrogate: each frame's network inputs are
+// taken in that frame's own static frame, so the frames run one after
+// another through the single-frame path (a surrogate pass, then one trace
+// launch over the pixels the gate left), into consecutive slots of out_rgb.
+// Every camera is checked first, so a track with a camera outside the
+// network's domain is refused whole and nothing is written.  The first frame
+// that returns a status other than ST_OK ends the call with that status.
+int render_frames_surrogate(st_context* ctx, int nframes, const st_camera* cams, const st_spacetime* stp,
+                            const st_render_params* rp, float* out_rgb, st_stats* stats) {
+  const auto t0 = std::chrono::steady_clock::now();
+  const size_t npix = (size_t)rp->width * rp->height;
+  if (rp->width <= 0 || rp->height <= 0 || npix * (size_t)nframes > (size_t)1 << 31) return ST_EINVAL;
+  for (int f = 0; f < nframes; ++f) {
+    TraceParams q;
+    st::Variant w;
+    const int rc = fill_params(ctx, &cams[f], stp, rp, &q, &w);
+    if (rc != ST_OK) return rc;
+    st::SurFrame sf{};
+    if (!surrogate_domain(&cams[f], stp, &sf)) return ST_EUNSUPPORTED;
+  }
+  st_stats tot;
+  std::memset(&tot, 0, sizeof tot);
+  for (int f = 0; f < nframes; ++f) {
+    st_stats one;
+    std::memset(&one, 0, sizeof one);
+    one.status = -1;  // stays -1 if the call fails before its stats are written
+    const int rc = do_render(ctx, &cams[f], stp, rp, out_rgb + 3 * npix * (size_t)f, nullptr, nullptr, &one);
+    if (rc != ST_OK && one.status == -1) return rc;
+    tot.kernel_ms += one.kernel_ms;
+    tot.rays += one.rays;
+    tot.steps += one.steps;
+    tot.fp64_steps += one.fp64_steps;
+    tot.gas_samples += one.gas_samples;
+    tot.surrogate_rays += one.surrogate_rays;
+    tot.launches += one.launches;
+    tot.h2d_bytes += one.h2d_bytes;
+    tot.d2h_bytes += one.d2h_bytes;
+    tot.status = one.status;
+    if (rc != ST_OK) break;
+  }
+  tot.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (stats) *stats = tot;
+  return tot.status;
+}
+
 int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const st_spacetime* stp,
                      const st_render_params* rp, float* out_rgb, st_stats* stats) {
   if (!ctx || nframes <= 0 || !cams || !stp || !rp || !out_rgb) return ST_EINVAL;
-  if (rp->semantics != ST_SEM_DRAFT || rp->samples != 1 || rp->surrogate) return ST_EUNSUPPORTED;
+  if (rp->semantics != ST_SEM_DRAFT || rp->samples != 1) return ST_EUNSUPPORTED;
+  if (rp->surrogate) return render_frames_surrogate(ctx, nframes, cams, stp, rp, out_rgb, stats);
   if (rp->order != 0 && rp->order != 4 && rp->schedule == ST_SCHED_PERSISTENT) return ST_EUNSUPPORTED;
   const auto t0 = std::chrono::steady_clock::now();
   TraceParams p;

@@ -114,3 +114,49 @@ def test_tcgen05_frame_kernel_matches_mma_sync(built_lib, monkeypatch):
           "fraction above 1e-5", (d > 1e-5).mean())
     assert np.median(d) <= 1e-6 and np.percentile(d, 99) <= 1e-3 and d.max() <= 1e-2
     sur.close()
+
+
+def test_surrogate_on_a_camera_track(built_lib):
+    """st_render_frames with the surrogate: a short track of static cameras
+    (config 1's hole, cameras at r = 14-16 M, inclination 80 deg, stepped in
+    azimuth; no disc, no gas) runs frame by frame through the single-frame
+    path, so each frame equals st_render of its camera bit for bit, rays are
+    served, and the stats are the frames' sums.  A track with one camera
+    inside r = 4 M (outside the network's domain) is refused whole, and so is
+    a context with gas, as st_render refuses it."""
+    from spacetime_gb300.scene import Camera, kerr_position, lens_fov
+    from spacetime_gb300.surrogate import load_trained
+    w = _scene(disc=False)
+    sky = workloads.sky(512, 256)
+    sur = load_trained()
+
+    def cam(r, phi):
+        x, y, z = kerr_position(r, 80.0, 0.9)
+        c, s = np.cos(phi), np.sin(phi)
+        return Camera.look_at((c * x - s * y, s * x + c * y, z), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), lens_fov(24.0))
+
+    cams = [cam(15.0, 0.0), cam(16.0, 0.4), cam(14.0, 0.8)]
+    with Context(sky, disc=None, emitter=w.emitter) as ctx:
+        ctx.set_surrogate(sur)
+        p = ctx.params(w.semantics, width=w.width, height=w.height, precision=_abi.ST_PREC_FP32, surrogate=1,
+                       surrogate_sigma=4e-4, **w.params)
+        track = ctx.render_frames_raw(cams, w.bh, p)
+        singles = [ctx.render_raw(c, w.bh, p) for c in cams]
+        with pytest.raises(_abi.StError) as e:
+            ctx.render_frames_raw(cams[:2] + [cam(3.0, 0.0)], w.bh, p)
+        assert e.value.code == _abi.ST_EUNSUPPORTED
+    assert track.stats["status"] == _abi.ST_OK
+    for f, one in enumerate(singles):
+        np.testing.assert_array_equal(track.image[f], one.image)
+    for key in ("rays", "steps", "surrogate_rays", "launches"):
+        assert track.stats[key] == sum(one.stats[key] for one in singles), key
+    assert track.stats["surrogate_rays"] > 0.2 * len(cams) * w.width * w.height
+    wg = workloads.config1().scaled(w.width, w.height)
+    with Context(sky, disc=wg.disc, volume=wg.vol, emitter=wg.emitter) as ctx:
+        ctx.set_surrogate(sur)
+        p = ctx.params(wg.semantics, width=w.width, height=w.height, precision=_abi.ST_PREC_FP32, surrogate=1,
+                       surrogate_sigma=4e-4, **w.params)
+        with pytest.raises(_abi.StError) as e:
+            ctx.render_frames_raw(cams, wg.bh, p)
+        assert e.value.code == _abi.ST_EUNSUPPORTED
+    sur.close()
