@@ -74,6 +74,30 @@ def forward_bf16(P, X):
     return h @ w["W4"].T + w["b4"]
 
 
+def split_bf16(x):
+    """(hi, lo) bf16 pair of FP32 values: hi = bf16(x), lo = bf16(x - hi)."""
+    x = np.asarray(x, dtype=np.float32).astype(np.float64)
+    hi = bf16(x)
+    return hi, bf16((x - hi).astype(np.float32))
+
+
+def forward_split(P, X):
+    """forward_bf16 with the edge layers as the tensor-core network kernel
+    computes them (sur_mlp_tc_kernel): layer 0 as the split-bf16 product
+    x_hi.w_hi + x_lo.w_hi + x_hi.w_lo + b_hi + b_lo, layer 4 as
+    h.(w_hi + w_lo) + b4 on the bf16 activations.  Returns (outputs, z0)."""
+    w = unpack(P)
+    xh, xl = split_bf16(X)
+    wh, wl = split_bf16(w["W0"])
+    bh, bl = split_bf16(w["b0"])
+    z0 = xh @ wh.T + xl @ wh.T + xh @ wl.T + bh + bl
+    h = bf16(_silu(z0))
+    for l in (1, 2, 3):
+        h = bf16(_silu(h @ bf16(w[f"W{l}"]).T + w[f"b{l}"]))
+    w4h, w4l = split_bf16(w["W4"])
+    return h @ (w4h + w4l).T + w["b4"], z0
+
+
 def loss_grad(P, X, T):
     """(loss4, grad) with loss4 = (total, direction MSE, radius MSE, g MSE)."""
     w = unpack(P)
