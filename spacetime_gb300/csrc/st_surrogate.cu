@@ -1470,8 +1470,9 @@ int gemm_status(st_surrogate* s) {
 }
 
 // Wait bound and first-copy switch of sur_mlp_tc_kernel.  The environment
-// variable SPACETIME_GB300_TC_WAIT_OUT=1 makes every tile's first wait run out
-// (its copies are never issued, short wait bound): the failure path under test.
+// variable SPACETIME_GB300_TC_WAIT_OUT=1 makes every CTA's first wait run out
+// (its first copies are never issued, short wait bound), so all tiles fail:
+// the failure path under test.
 struct TcWait {
   uint32_t limit;
   int issue_first;

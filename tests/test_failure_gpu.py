@@ -5,9 +5,9 @@
   runs out.  The kernel records ST_EBUDGET in the status word and returns;
   the call reports it, and the same context renders correctly afterwards.
 - Every mbarrier wait of the tcgen05 network kernel is bounded.
-  SPACETIME_GB300_TC_WAIT_OUT=1 leaves each tile's first copies unissued (a
-  barrier nothing completes) with a short bound, so every tile's first wait
-  runs out with nothing in flight.  The kernel marks its tiles failed, frees
+  SPACETIME_GB300_TC_WAIT_OUT=1 leaves each CTA's first copies unissued (a
+  barrier nothing completes) with a short bound, so every CTA's first wait
+  runs out with nothing in flight.  The kernel leaves all its tiles failed, frees
   its TMEM and returns: st_surrogate_forward_tc reports ST_ECUDA, a surrogate
   frame integrates every pixel (the plain frame, exactly) and reports the
   status, and both work normally on the next call.
