@@ -18,7 +18,7 @@
  *                          render_draft_mtl(ctx, cam, st; width, height, samples, dt,
  *                          fisheye_deg, aperture_world, focus_dist, relativistic, order)
  *                          src/metal.jl:2040-2242 (semantics ST_SEM_DRAFT)
- *   st_render_frames       the per-frame loop of examples/videos/*.jl over
+ *   st_render_frames       the per-frame loop of the examples/videos scripts over
  *                          render_draft_mtl, batched into one persistent launch
  *   st_render_device       _trace_preview_gpu!, src/metal.jl:1825-1881 (result left
  *                          on the device, no download)
