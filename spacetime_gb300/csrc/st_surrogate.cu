@@ -991,30 +991,52 @@ __global__ void __launch_bounds__(128) sur_gate_kernel(const __grid_constant__ T
   }
 }
 
-// Exclusive prefix sum of the per-warp counts in one CTA of 1024 threads
-// (each thread a contiguous run), and the total into *count.
+// Exclusive prefix sum of the per-warp counts in one CTA of 1024 threads,
+// and the total into *count.  The counts go through in chunks of 1024 in
+// index order (thread t takes entry base + t); each thread first loads its
+// entries of eight chunks (coalesced, independent loads), then the chunks are
+// scanned one after another: warp scans by shuffle, the 32 warp totals by
+// one more warp, and a running carry.
 __global__ void __launch_bounds__(1024) sur_scan_kernel(const int* __restrict__ wcount, int* __restrict__ woff,
                                                          int nwarps, int* count) {
-  __shared__ int part[1024];
-  const int t = threadIdx.x;
-  const int per = (nwarps + 1023) / 1024;
-  const int b = t * per, e = min(b + per, nwarps);
-  int sum = 0;
-  for (int i = b; i < e; ++i) sum += wcount[i];
-  part[t] = sum;
-  __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {
-    const int v = t >= off ? part[t - off] : 0;
-    __syncthreads();
-    part[t] += v;
-    __syncthreads();
+  constexpr int U = 8;
+  __shared__ int wsum[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  int carry = 0;
+  for (int base = 0; base < nwarps; base += 1024 * U) {
+    int v[U];
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      const int idx = base + k * 1024 + t;
+      v[k] = idx < nwarps ? wcount[idx] : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      int x = v[k];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane == 31) wsum[w] = x;
+      __syncthreads();
+      if (w == 0) {
+        int s = wsum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, s, o);
+          if (lane >= o) s += y;
+        }
+        wsum[lane] = s;  // inclusive over warps
+      }
+      __syncthreads();
+      const int idx = base + k * 1024 + t;
+      if (idx < nwarps) woff[idx] = carry + (w > 0 ? wsum[w - 1] : 0) + x - v[k];
+      carry += wsum[31];
+      __syncthreads();  // every thread has read wsum before the next chunk writes it
+    }
   }
-  int run = part[t] - sum;  // exclusive prefix of this thread's run
-  for (int i = b; i < e; ++i) {
-    woff[i] = run;
-    run += wcount[i];
-  }
-  if (t == 1023) *count = part[1023];
+  if (t == 0) *count = carry;
 }
 
 // Pixels left to integrate, in tile raster order (warp by warp).
