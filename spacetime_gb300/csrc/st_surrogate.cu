@@ -161,28 +161,62 @@ __global__ void l4_bwd_dx(const float* __restrict__ dout, const float* __restric
   dZ3[idx] = __float2bfloat16_rn(v * mlp::dsilu(Z3[idx]));
 }
 
-// dW4[j][k] += sum_b dout[b][j] H3[b][k], db4[j] += sum_b dout[b][j]; a block
-// of 256 threads (one per k) sweeps RED_ROWS rows (32: a batch of 16384 gives
-// 512 blocks, enough to cover the GPU's SMs, for one atomic per output per block).
+// dW4[j][k] = sum_b dout[b][j] H3[b][k], db4[j] = sum_b dout[b][j], in two
+// stages: a block of 256 threads (one per k) sweeps RED_ROWS rows (32: a batch
+// of 16384 gives 512 blocks, enough to cover the GPU's SMs) and writes its
+// partial sums to its row of `part` ([block][L4_PART]: dW4 row-major, then db4),
+// then reduce_parts sums the blocks' rows in a fixed order.  (Atomic adds of
+// every block into the same 1.5-1.8 K gradient words serialise on the few L2
+// slices those words live in.)
 constexpr int RED_ROWS = 32;
-__global__ void l4_bwd_w(const float* __restrict__ dout, const __nv_bfloat16* __restrict__ H3, float* G, int B) {
+constexpr int L4_PART = NOUT * NH + NOUT;  // 1542
+constexpr int L0_PART = NH * NIN + NH;     // 1792
+__global__ void l4_bwd_w(const float* __restrict__ dout, const __nv_bfloat16* __restrict__ H3, float* part, int B) {
   const int k = threadIdx.x;
   const int b0 = blockIdx.x * RED_ROWS, b1 = min(B, b0 + RED_ROWS);
-  float acc[NOUT] = {0, 0, 0, 0, 0, 0}, db[NOUT] = {0, 0, 0, 0, 0, 0};
+  // the block's rows of dout, which every thread reads, staged once
+  __shared__ float ds[RED_ROWS * NOUT];
+  if (k < (b1 - b0) * NOUT) ds[k] = dout[(size_t)b0 * NOUT + k];
+  __syncthreads();
+  float acc[NOUT] = {0, 0, 0, 0, 0, 0};
 #pragma unroll 8
   for (int b = b0; b < b1; ++b) {
     const float h = __bfloat162float(H3[(size_t)b * NH + k]);
 #pragma unroll
-    for (int j = 0; j < NOUT; ++j) {
-      const float d = dout[(size_t)b * NOUT + j];
-      acc[j] += d * h;
-      if (k == 0) db[j] += d;
-    }
+    for (int j = 0; j < NOUT; ++j) acc[j] += ds[(b - b0) * NOUT + j] * h;
   }
+  float* row = part + (size_t)blockIdx.x * L4_PART;
 #pragma unroll
-  for (int j = 0; j < NOUT; ++j) {
-    atomicAdd(G + OW4 + j * NH + k, acc[j]);
-    if (k == 0) atomicAdd(G + OB4 + j, db[j]);
+  for (int j = 0; j < NOUT; ++j) row[j * NH + k] = acc[j];
+  if (k < NOUT) {
+    // thread j < 6: the block's db4[j]
+    float db = 0.f;
+    for (int b = 0; b < b1 - b0; ++b) db += ds[b * NOUT + k];
+    row[NOUT * NH + k] = db;
+  }
+}
+
+// G[base + c] = sum over the nparts rows of part[p][c], c < ncols, in a
+// fixed order.  Block: 32 columns (a lane each) x 32 warps, warp w taking rows
+// w, w + 32, ... (coalesced 128-byte loads, 16 per warp for 512 rows); the
+// warps' sums combine in shared memory.
+__global__ void __launch_bounds__(1024) reduce_parts(const float* __restrict__ part, int nparts, int ncols,
+                                                     float* G, size_t base) {
+  __shared__ float red[32][33];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int c = blockIdx.x * 32 + lane;
+  float acc = 0.f;
+  if (c < ncols) {
+#pragma unroll 8
+    for (int p = w; p < nparts; p += 32) acc += part[(size_t)p * ncols + c];
+  }
+  red[w][lane] = acc;
+  __syncthreads();
+  if (w == 0 && c < ncols) {
+    float t = red[0][lane];
+#pragma unroll
+    for (int k = 1; k < 32; ++k) t += red[k][lane];
+    G[base + c] = t;
   }
 }
 
@@ -196,21 +230,28 @@ __global__ void colsum_bf16(const __nv_bfloat16* __restrict__ D, float* G, size_
   atomicAdd(G + off + n, s);
 }
 
-// dW0[n][i] += sum_b dZ0[b][n] X[b][i], db0[n] += sum_b dZ0[b][n]
-__global__ void l0_bwd(const __nv_bfloat16* __restrict__ dZ0, const float* __restrict__ X, float* G, int B) {
+// dW0[n][i] = sum_b dZ0[b][n] X[b][i], db0[n] = sum_b dZ0[b][n]: the block
+// partials of the two-stage reduction above ([block][L0_PART]: dW0 row-major,
+// then db0)
+__global__ void l0_bwd(const __nv_bfloat16* __restrict__ dZ0, const float* __restrict__ X, float* part, int B) {
   const int n = threadIdx.x;
   const int b0 = blockIdx.x * RED_ROWS, b1 = min(B, b0 + RED_ROWS);
+  // the block's rows of X, which every thread reads, staged once
+  __shared__ float xs[RED_ROWS * NIN];
+  if (n < (b1 - b0) * NIN) xs[n] = X[(size_t)b0 * NIN + n];
+  __syncthreads();
   float acc[NIN] = {0, 0, 0, 0, 0, 0}, db = 0.f;
 #pragma unroll 8
   for (int b = b0; b < b1; ++b) {
     const float d = __bfloat162float(dZ0[(size_t)b * NH + n]);
     db += d;
 #pragma unroll
-    for (int i = 0; i < NIN; ++i) acc[i] += d * X[b * NIN + i];
+    for (int i = 0; i < NIN; ++i) acc[i] += d * xs[(b - b0) * NIN + i];
   }
+  float* row = part + (size_t)blockIdx.x * L0_PART;
 #pragma unroll
-  for (int i = 0; i < NIN; ++i) atomicAdd(G + OW0 + n * NIN + i, acc[i]);
-  atomicAdd(G + OB0 + n, db);
+  for (int i = 0; i < NIN; ++i) row[n * NIN + i] = acc[i];
+  row[NH * NIN + n] = db;
 }
 
 __global__ void adamw(float* P, const float* G, float* Mm, float* Vv, size_t n, float lr, float b1, float b2,
@@ -1304,6 +1345,7 @@ struct st_surrogate {
   float* Z[4] = {nullptr, nullptr, nullptr, nullptr};
   __nv_bfloat16* H[4] = {nullptr, nullptr, nullptr, nullptr};
   __nv_bfloat16 *dZa = nullptr, *dZb = nullptr;
+  float* part = nullptr;  // block partials of the layer-0 / layer-4 weight gradients
   float *out = nullptr, *dout = nullptr, *T = nullptr, *loss = nullptr;
   // training set (device)
   float *DX = nullptr, *DT = nullptr;
@@ -1328,6 +1370,8 @@ int ensure_work(st_surrogate* s, int rows) {
   cudaFree(s->dZa); cudaFree(s->dZb); cudaFree(s->out); cudaFree(s->dout); cudaFree(s->T);
   for (int l = 0; l < 3; ++l) { cudaFree(s->HT[l]); s->HT[l] = nullptr; }
   for (int l = 0; l < 2; ++l) { cudaFree(s->dZT[l]); s->dZT[l] = nullptr; }
+  cudaFree(s->part);
+  s->part = nullptr;
   s->cap = 0;
   const size_t R = rows;
   if (cudaMalloc(&s->X, R * NIN * 4) != cudaSuccess) return ST_ENOMEM;
@@ -1344,10 +1388,13 @@ int ensure_work(st_surrogate* s, int rows) {
     if (cudaMalloc(&s->HT[l], R * NH * 2) != cudaSuccess) return ST_ENOMEM;
   for (int l = 0; l < 2; ++l)
     if (cudaMalloc(&s->dZT[l], R * NH * 2) != cudaSuccess) return ST_ENOMEM;
+  if (cudaMalloc(&s->part, (R / RED_ROWS + 1) * (size_t)L0_PART * 4) != cudaSuccess) return ST_ENOMEM;
   s->cap = rows;
   return ST_OK;
 }
 
+// The training kernels' bf16 copies of the hidden weights (and W^T), after
+// every parameter update.
 int sync_bf16(st_surrogate* s) {
   for (int l = 0; l < 3; ++l) {
     to_bf16<<<(NH * NH + 255) / 256, 256, 0, s->stream>>>(s->P + OWH[l], s->Wb[l], NH * NH);
@@ -1355,6 +1402,13 @@ int sync_bf16(st_surrogate* s) {
     st::tcg::transpose_bf16<<<dim3(NH / 32, NH / 32), 256, 0, s->stream>>>(s->Wb[l], s->Wt[l], NH, NH);
     SC(cudaGetLastError());
   }
+  return ST_OK;
+}
+
+// The tensor-core network kernel's weight images and packed biases: once the
+// parameters are final (creation, st_surrogate_set_params, the end of
+// st_surrogate_train), not after every training step.
+int sync_tc_images(st_surrogate* s) {
   pack_sw128<<<(TC_PACK_N + 255) / 256, 256, 0, s->stream>>>(s->P, s->Wsw);
   SC(cudaGetLastError());
   pack_small<<<(TC_SMALL_BYTES / 4 + 255) / 256, 256, 0, s->stream>>>(s->P, s->Psmall);
@@ -1416,6 +1470,17 @@ int forward(st_surrogate* s, const float* X, int B, bool keep_z, cudaStream_t st
   return ST_OK;
 }
 
+// Layer 0's weight and bias gradients from dZ0: block partials, then their
+// ordered sum into G (dW0 and db0 are adjacent in the parameter vector).
+int l0_backward(st_surrogate* s, const __nv_bfloat16* dZ0, const float* X, int B, int nred) {
+  static_assert(OB0 == OW0 + NH * NIN, "dW0 and db0 adjacent in the parameter vector");
+  l0_bwd<<<nred, NH, 0, s->stream>>>(dZ0, X, s->part, B);
+  SC(cudaGetLastError());
+  reduce_parts<<<(L0_PART + 31) / 32, 1024, 0, s->stream>>>(s->part, nred, L0_PART, s->G, OW0);
+  SC(cudaGetLastError());
+  return ST_OK;
+}
+
 // backward from s->dout (already scaled by 1/B); accumulates into s->G
 int backward(st_surrogate* s, const float* X, int B) {
   cudaStream_t st = s->stream;
@@ -1423,7 +1488,10 @@ int backward(st_surrogate* s, const float* X, int B) {
   l4_bwd_dx<<<(B * NH + 255) / 256, 256, 0, st>>>(s->dout, s->P, s->Z[3], s->dZa, B);
   SC(cudaGetLastError());
   const int nred = (B + RED_ROWS - 1) / RED_ROWS;
-  l4_bwd_w<<<nred, NH, 0, st>>>(s->dout, s->H[3], s->G, B);
+  l4_bwd_w<<<nred, NH, 0, st>>>(s->dout, s->H[3], s->part, B);
+  SC(cudaGetLastError());
+  static_assert(OB4 == OW4 + NOUT * NH, "dW4 and db4 adjacent in the parameter vector");
+  reduce_parts<<<(L4_PART + 31) / 32, 1024, 0, st>>>(s->part, nred, L4_PART, s->G, OW4);
   SC(cudaGetLastError());
   __nv_bfloat16* dZ = s->dZa;
   __nv_bfloat16* dZn = s->dZb;
@@ -1451,9 +1519,7 @@ int backward(st_surrogate* s, const float* X, int B) {
       std::swap(dZ, dZn);
       cur ^= 1;
     }
-    l0_bwd<<<nred, NH, 0, st>>>(dZ, X, s->G, B);
-    SC(cudaGetLastError());
-    return ST_OK;
+    return l0_backward(s, dZ, X, B, nred);
   }
   for (int l = 3; l >= 1; --l) {
     // dW_l = dZ_l^T H_{l-1}
@@ -1472,9 +1538,7 @@ int backward(st_surrogate* s, const float* X, int B) {
     SC(cudaGetLastError());
     std::swap(dZ, dZn);
   }
-  l0_bwd<<<nred, NH, 0, st>>>(dZ, X, s->G, B);
-  SC(cudaGetLastError());
-  return ST_OK;
+  return l0_backward(s, dZ, X, B, nred);
 }
 
 int pad128(long long n) { return (int)((n + 127) / 128 * 128); }
@@ -1583,7 +1647,8 @@ int st_surrogate_create(st_surrogate** out, int device, unsigned long long seed)
   uint32_t v[SOBOL_DIMS][32];
   sobol_directions(v);
   if (cudaMemcpyToSymbol(c_sobol_v, v, sizeof v) != cudaSuccess) return fail(ST_ECUDA);
-  if (sync_bf16(s) != ST_OK || cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(ST_ECUDA);
+  if (sync_bf16(s) != ST_OK || sync_tc_images(s) != ST_OK || cudaStreamSynchronize(s->stream) != cudaSuccess)
+    return fail(ST_ECUDA);
   *out = s;
   return ST_OK;
 }
@@ -1597,6 +1662,7 @@ void st_surrogate_destroy(st_surrogate* s) {
   cudaFree(s->d_status);
   for (int l = 0; l < 3; ++l) cudaFree(s->HT[l]);
   for (int l = 0; l < 2; ++l) cudaFree(s->dZT[l]);
+  cudaFree(s->part);
   cudaFree(s->Wsw);
   cudaFree(s->Psmall);
   cudaFree(s->fX); cudaFree(s->fAux); cudaFree(s->fFl); cudaFree(s->fO); cudaFree(s->fStatus);
@@ -1622,7 +1688,7 @@ int st_surrogate_set_params(st_surrogate* s, const float* host) {
   if (!s || !host) return ST_EINVAL;
   if (cudaSetDevice(s->device) != cudaSuccess) return ST_ECUDA;
   SC(cudaMemcpy(s->P, host, NPARAM * 4, cudaMemcpyHostToDevice));
-  if (sync_bf16(s) != ST_OK) return ST_ECUDA;
+  if (sync_bf16(s) != ST_OK || sync_tc_images(s) != ST_OK) return ST_ECUDA;
   SC(cudaStreamSynchronize(s->stream));
   return ST_OK;
 }
@@ -1748,6 +1814,7 @@ int st_surrogate_train(st_surrogate* s, int steps, int batch, float lr, float we
     if ((rc = sync_bf16(s)) != ST_OK) return rc;
     if (loss_hist) SC(cudaMemcpyAsync(&lh[k], s->loss, 4, cudaMemcpyDeviceToHost, st));
   }
+  if ((rc = sync_tc_images(s)) != ST_OK) return rc;
   SC(cudaStreamSynchronize(st));
   if ((rc = gemm_status(s)) != ST_OK) return rc;
   if (loss_hist) std::memcpy(loss_hist, lh.data(), steps * sizeof(float));
