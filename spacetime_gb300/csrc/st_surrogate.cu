@@ -64,15 +64,30 @@ constexpr size_t OBH[3] = {OB1, OB2, OB3};
 // small FP32 layers, loss, reductions, AdamW
 // ---------------------------------------------------------------------------
 
-__global__ void l0_fwd(const float* __restrict__ X, const float* __restrict__ P, float* Z0, __nv_bfloat16* H0, int B) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= B * NH) return;
-  const int b = idx / NH, n = idx - b * NH;
-  float z = P[OB0 + n];
+// Z0 = X W0^T + b0, H0 = bf16(silu(Z0)): a block of 256 threads (one per
+// unit, its weights in registers) takes L0_ROWS rows, whose inputs it stages in
+// shared memory; each row's outputs are one coalesced store per array.
+constexpr int L0_ROWS = 16;
+__global__ void __launch_bounds__(NH) l0_fwd(const float* __restrict__ X, const float* __restrict__ P, float* Z0,
+                                             __nv_bfloat16* H0, int B) {
+  const int n = threadIdx.x;
+  const int b0 = blockIdx.x * L0_ROWS, nb = min(B - b0, L0_ROWS);
+  __shared__ float xs[L0_ROWS * NIN];
+  if (n < nb * NIN) xs[n] = X[(size_t)b0 * NIN + n];
+  float w[NIN];
 #pragma unroll
-  for (int i = 0; i < NIN; ++i) z += X[b * NIN + i] * P[OW0 + n * NIN + i];
-  if (Z0) Z0[idx] = z;
-  H0[idx] = __float2bfloat16_rn(mlp::silu(z));
+  for (int i = 0; i < NIN; ++i) w[i] = P[OW0 + n * NIN + i];
+  const float bias = P[OB0 + n];
+  __syncthreads();
+#pragma unroll 4
+  for (int r = 0; r < nb; ++r) {
+    float z = bias;
+#pragma unroll
+    for (int i = 0; i < NIN; ++i) z += xs[r * NIN + i] * w[i];
+    const size_t idx = (size_t)(b0 + r) * NH + n;
+    if (Z0) Z0[idx] = z;
+    H0[idx] = __float2bfloat16_rn(mlp::silu(z));
+  }
 }
 
 // one warp per row: out[b][j] = H3[b] . W4[j] + b4[j]
@@ -150,15 +165,28 @@ __global__ void loss_grad(const float* __restrict__ out, const float* __restrict
 }
 
 // dZ3 = silu'(Z3) * (dout . W4)
+// dZ3 = silu'(Z3) * (dout . W4); a thread takes four adjacent units of one
+// row (vector loads and stores), the row's output gradient read once.
 __global__ void l4_bwd_dx(const float* __restrict__ dout, const float* __restrict__ P, const float* __restrict__ Z3,
                           __nv_bfloat16* dZ3, int B) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= B * NH) return;
-  const int b = idx / NH, k = idx - b * NH;
-  float v = 0.f;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;  // quad index
+  if (q >= B * (NH / 4)) return;
+  const int b = q / (NH / 4), k0 = (q - b * (NH / 4)) * 4;
+  float d[NOUT];
 #pragma unroll
-  for (int j = 0; j < NOUT; ++j) v += dout[(size_t)b * NOUT + j] * P[OW4 + j * NH + k];
-  dZ3[idx] = __float2bfloat16_rn(v * mlp::dsilu(Z3[idx]));
+  for (int j = 0; j < NOUT; ++j) d[j] = dout[(size_t)b * NOUT + j];
+  const size_t idx = (size_t)b * NH + k0;
+  const float4 z = *reinterpret_cast<const float4*>(Z3 + idx);
+  float v[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int j = 0; j < NOUT; ++j) {
+    const float4 w = *reinterpret_cast<const float4*>(P + OW4 + j * NH + k0);
+    v[0] += d[j] * w.x; v[1] += d[j] * w.y; v[2] += d[j] * w.z; v[3] += d[j] * w.w;
+  }
+  const __nv_bfloat162 a = __floats2bfloat162_rn(v[0] * mlp::dsilu(z.x), v[1] * mlp::dsilu(z.y));
+  const __nv_bfloat162 c = __floats2bfloat162_rn(v[2] * mlp::dsilu(z.z), v[3] * mlp::dsilu(z.w));
+  *reinterpret_cast<uint2*>(dZ3 + idx) =
+      make_uint2(*reinterpret_cast<const uint32_t*>(&a), *reinterpret_cast<const uint32_t*>(&c));
 }
 
 // dW4[j][k] = sum_b dout[b][j] H3[b][k], db4[j] = sum_b dout[b][j], in two
@@ -1442,7 +1470,7 @@ int gemm_tc(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, in
 
 // forward of B rows (B multiple of 128) from s->X-like input pointer
 int forward(st_surrogate* s, const float* X, int B, bool keep_z, cudaStream_t st) {
-  l0_fwd<<<(B * NH + 255) / 256, 256, 0, st>>>(X, s->P, keep_z ? s->Z[0] : nullptr, s->H[0], B);
+  l0_fwd<<<(B + L0_ROWS - 1) / L0_ROWS, NH, 0, st>>>(X, s->P, keep_z ? s->Z[0] : nullptr, s->H[0], B);
   SC(cudaGetLastError());
   const bool tc5 = train_on_tcgen05();
   if (tc5 && keep_z) {
@@ -1485,7 +1513,7 @@ int l0_backward(st_surrogate* s, const __nv_bfloat16* dZ0, const float* X, int B
 int backward(st_surrogate* s, const float* X, int B) {
   cudaStream_t st = s->stream;
   SC(cudaMemsetAsync(s->G, 0, NPARAM * 4, st));
-  l4_bwd_dx<<<(B * NH + 255) / 256, 256, 0, st>>>(s->dout, s->P, s->Z[3], s->dZa, B);
+  l4_bwd_dx<<<(B * (NH / 4) + 255) / 256, 256, 0, st>>>(s->dout, s->P, s->Z[3], s->dZa, B);
   SC(cudaGetLastError());
   const int nred = (B + RED_ROWS - 1) / RED_ROWS;
   l4_bwd_w<<<nred, NH, 0, st>>>(s->dout, s->H[3], s->part, B);
