@@ -286,7 +286,7 @@ def _errors(img, diag, ref, rays, served=None):
     return out
 
 
-def headline_block(ctx_cls, device: int, flush, sigma: float, reps: int = 3) -> dict:
+def headline_block(ctx_cls, device: int, flush, sigma: float, reps: int = 5) -> dict:
     """The metric's comparison on one GB300: surrogate + FP32 against the plain
     FP64-guarded RK4 path and plain FP32 RK4, each frame 1920x1080 with config
     1's camera and hole (Kerr a=0.9, r=15 M, i=80 deg, Lens(24), kernel rules,
@@ -344,11 +344,12 @@ def headline_block(ctx_cls, device: int, flush, sigma: float, reps: int = 3) -> 
                 torch.cuda.synchronize()
                 _, st = ctx.render_device(w.cam, w.bh, p)
                 ts.append(st["kernel_ms"])
-            ms = float(np.mean(ts))
+            ms = float(np.median(ts))  # median of the frames: one slow frame does not move the ratios
             r = ctx.render_raw(w.cam, w.bh, p, diag=True)
             img, diag = _crop_stack(r.image, r.diag)
             served = (diag["flags"] & _abi.ST_RAY_SURROGATE) > 0 if kw.get("surrogate") else None
             block[name] = {"value": 1920 * 1080 / (ms * 1e-3) / 1e6, "ms_per_step": ms,
+                           "ms_range": [float(min(ts)), float(max(ts))],
                            "served_fraction": st["surrogate_rays"] / (1920 * 1080),
                            "steps_per_frame": st["steps"], "fp64_steps_per_frame": st["fp64_steps"],
                            "errors": _errors(img, diag, ref, rays, served)}
