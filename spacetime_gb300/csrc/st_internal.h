@@ -129,6 +129,9 @@ struct TraceParams {
   void* defer_state;
   unsigned int* defer_count;
   int defer_cap;
+  // pixel schedule of one full frame: block b traces tile tile_order[b]
+  // (row-major over the grid); null = raster order
+  const int* tile_order;
   // persistent schedule
   const FrameCam* frames;    // optional per-frame cameras (device)
   int n_frames;              // frames in the table (pixel schedule: grid z)

@@ -51,8 +51,14 @@ __global__ void __launch_bounds__(128, ORD == 4 ? ST_MINB : ST_MINB_ADAPTIVE) tr
     for (int k = lin; k < p.lut_size; k += nthr) st_lut_smem[k] = __ldg(p.lut + k);
     __syncthreads();
   }
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int j = blockIdx.y * blockDim.y + threadIdx.y;
+  int tbx = blockIdx.x, tby = blockIdx.y;
+  if (p.tile_order) {  // a full frame dispatched centre first
+    const int t = __ldg(p.tile_order + blockIdx.y * gridDim.x + blockIdx.x);
+    tby = t / (int)gridDim.x;
+    tbx = t - tby * (int)gridDim.x;
+  }
+  int i = tbx * blockDim.x + threadIdx.x;
+  int j = tby * blockDim.y + threadIdx.y;
   if (p.box_cols > 0) {  // a refinement pass over its box only
     if (i >= p.box_cols || j >= p.box_rows) i = p.width;  // idle
     i += p.box_col0;
