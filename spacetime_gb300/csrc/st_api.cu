@@ -1659,6 +1659,13 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
   p.nmax = nmax_max;
   v.sched = rp->schedule == ST_SCHED_PIXEL ? ST_SCHED_PIXEL : ST_SCHED_PERSISTENT;
   if ((rc = setup_defer(ctx, &p, v, npix * nframes)) != ST_OK) return rc;
+  if (v.sched == ST_SCHED_PIXEL) {
+    // every frame's slice of the grid dispatched centre first (the first
+    // camera's projection of the hole)
+    int bx = rp->block_x, by = rp->block_y;
+    if (bx <= 0 || by <= 0 || bx * by != 128) { bx = 16; by = 8; }
+    if ((rc = ensure_tile_order(ctx, &cams[0], rp->width, rp->height, bx, by, s, &p.tile_order)) != ST_OK) return rc;
+  }
   // the device work of one call: stage cameras, clear queue and counters,
   // trace all frames in one launch, pack, read the counters
   // Under stream capture a plain event record only orders streams; the
