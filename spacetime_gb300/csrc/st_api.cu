@@ -350,6 +350,7 @@ struct st_context {
   size_t order_cap = 0;
   int order_key[4] = {-1, -1, -1, -1};
   std::vector<int> h_order;
+  size_t h2d_extra = 0;  // bytes uploaded by the current call beyond its parameters
 };
 
 namespace {
@@ -721,6 +722,7 @@ int ensure_tile_order(st_context* ctx, const st_camera* cam, int width, int heig
         cudaSuccess)
       return ST_ECUDA;
     ctx->order_key[0] = gx; ctx->order_key[1] = gy; ctx->order_key[2] = cx; ctx->order_key[3] = cy;
+    ctx->h2d_extra += (size_t)n * sizeof(int);
   }
   *out = ctx->d_order;
   return ST_OK;
@@ -744,6 +746,7 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
   int rc = fill_params(ctx, cam, stp, rp, &p, &v);
   if (rc != ST_OK) return rc;
   if (cudaSetDevice(ctx->device) != cudaSuccess) return ST_ECUDA;
+  ctx->h2d_extra = 0;
   const size_t npix = (size_t)rp->width * rp->height;
   if ((rc = ensure(&ctx->d_fb, &ctx->fb_cap, npix)) != ST_OK) return rc;
   if (host_rgb && (rc = ensure(&ctx->d_rgb, &ctx->rgb_cap, 3 * npix)) != ST_OK) return rc;
@@ -906,7 +909,7 @@ int do_render(st_context* ctx, const st_camera* cam, const st_spacetime* stp, co
     if (rp->surrogate) stats->rays += stats->surrogate_rays;
     stats->launches = launches;
     stats->status = status;
-    stats->h2d_bytes = sizeof(TraceParams) * launches;
+    stats->h2d_bytes = sizeof(TraceParams) * launches + ctx->h2d_extra;
     stats->d2h_bytes = d2h + sizeof cnt;
     stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
@@ -1659,6 +1662,7 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
   p.nmax = nmax_max;
   v.sched = rp->schedule == ST_SCHED_PIXEL ? ST_SCHED_PIXEL : ST_SCHED_PERSISTENT;
   if ((rc = setup_defer(ctx, &p, v, npix * nframes)) != ST_OK) return rc;
+  ctx->h2d_extra = 0;
   if (v.sched == ST_SCHED_PIXEL) {
     // every frame's slice of the grid dispatched centre first (the first
     // camera's projection of the hole)
@@ -1721,7 +1725,7 @@ int st_render_frames(st_context* ctx, int nframes, const st_camera* cams, const 
     stats->gas_samples = cnt[st::CNT_GAS];
     stats->launches = 1;
     stats->status = status;
-    stats->h2d_bytes = nframes * sizeof(st::FrameCam) + (rp->graph ? 0 : sizeof(TraceParams));
+    stats->h2d_bytes = nframes * sizeof(st::FrameCam) + (rp->graph ? 0 : sizeof(TraceParams)) + ctx->h2d_extra;
     stats->d2h_bytes = 3 * npix * nframes * sizeof(float) + st::CNT_N * sizeof(unsigned long long);
     stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
