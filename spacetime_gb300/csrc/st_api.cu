@@ -705,6 +705,10 @@ int ensure_tile_order(st_context* ctx, const st_camera* cam, int width, int heig
     hi = 0.5 * width + (xr / (xf * cam->fov_factor)) * 0.5 * height;
     hj = 0.5 * height + (xu / (xf * cam->fov_factor)) * 0.5 * height;
   }
+  // clamp in double first: a hole almost square to the view axis projects far
+  // off the frame, beyond what an int holds
+  hi = std::min(std::max(hi, 0.0), (double)width - 1.0);
+  hj = std::min(std::max(hj, 0.0), (double)height - 1.0);
   const int cx = std::min(std::max((int)std::floor(hi / bx), 0), gx - 1);
   const int cy = std::min(std::max((int)std::floor(hj / by), 0), gy - 1);
   if (ctx->order_key[0] != gx || ctx->order_key[1] != gy || ctx->order_key[2] != cx || ctx->order_key[3] != cy) {
