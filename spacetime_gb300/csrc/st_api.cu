@@ -707,6 +707,7 @@ int ensure_tile_order(st_context* ctx, const st_camera* cam, int width, int heig
   }
   // clamp in double first: a hole almost square to the view axis projects far
   // off the frame, beyond what an int holds
+  if (!std::isfinite(hi) || !std::isfinite(hj)) { hi = 0.5 * width; hj = 0.5 * height; }
   hi = std::min(std::max(hi, 0.0), (double)width - 1.0);
   hj = std::min(std::max(hj, 0.0), (double)height - 1.0);
   const int cx = std::min(std::max((int)std::floor(hi / bx), 0), gx - 1);
