@@ -167,7 +167,8 @@ def _strided_dirs(w, FW: int, FH: int, n_rays: int):
 
 
 def cpu_baseline(seconds_target: float = 15.0, threads: int | None = None, gpu_frame=None,
-                 gpu_diag=None, workload: str = "config1", frame_size=(1920, 1080), rate_hint=None) -> dict:
+                 gpu_diag=None, workload: str = "config1", frame_size=(1920, 1080), rate_hint=None,
+                 twin: bool = True) -> dict:
     """The CPU path timed on the host cores: the oracle's restatement of the
     reference's CPU renderer loop -- DifferentialEquations-style Tsit5 at the
     reference's own tolerances (reltol = abstol = 1e-6, src/raytrace.jl:369-373)
@@ -204,23 +205,25 @@ def cpu_baseline(seconds_target: float = 15.0, threads: int | None = None, gpu_f
     out = {"value": n / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port", "rate_rays_per_s": n / dt,
            "sample": f"pixels on a stride-{stride} grid over the whole {FW}x{FH} frame ({workload}; {n} rays), "
                      f"FP64 Tsit5 reltol = abstol = 1e-6 (the reference renderer's), {dt:.1f} s on {threads} threads"}
-    # the same CPU restatement with the GPU path's own integrator: the oracle's
-    # FP64 RK4 twin of the kernel (its step rule and stopping rules), on a
-    # strided sample sized for about half the Tsit5 time
-    tw = O.scene_for(w, sky, O.INT_RK4)
+    if twin:
+        # the same CPU restatement with the GPU path's own integrator: the
+        # oracle's FP64 RK4 twin of the kernel (its step rule and stopping
+        # rules), on a strided sample sized for about half the Tsit5 time
+        tw = O.scene_for(w, sky, O.INT_RK4)
 
-    def run_twin(m):
-        dirs, st = _strided_dirs(w, FW, FH, m)
-        t1 = time.perf_counter()
-        tw.trace_dirs(dirs, nthreads=threads)
-        return dirs.shape[0], st, time.perf_counter() - t1
+        def run_twin(m):
+            dirs, st = _strided_dirs(w, FW, FH, m)
+            t1 = time.perf_counter()
+            tw.trace_dirs(dirs, nthreads=threads)
+            return dirs.shape[0], st, time.perf_counter() - t1
 
-    m0, _, s0 = run_twin(2000)
-    mt, st_t, dtt = run_twin(int(min(max(m0 / max(s0, 1e-6) * seconds_target / 2, 2000), 400000)))
-    out["fp64_rk4_twin"] = {
-        "value": mt / dtt / 1e6, "unit": UNIT, "cores": threads,
-        "sample": f"pixels on a stride-{st_t} grid over the whole {FW}x{FH} frame ({mt} rays), the oracle's FP64 "
-                  f"RK4 twin of the kernel (the GPU path's step and stopping rules), {dtt:.1f} s on {threads} threads"}
+        m0, _, s0 = run_twin(2000)
+        mt, st_t, dtt = run_twin(int(min(max(m0 / max(s0, 1e-6) * seconds_target / 2, 2000), 400000)))
+        out["fp64_rk4_twin"] = {
+            "value": mt / dtt / 1e6, "unit": UNIT, "cores": threads,
+            "sample": f"pixels on a stride-{st_t} grid over the whole {FW}x{FH} frame ({mt} rays), the oracle's "
+                      f"FP64 RK4 twin of the kernel (the GPU path's step and stopping rules), {dtt:.1f} s on "
+                      f"{threads} threads"}
     if gpu_frame is not None:
         import numpy as np
         cw, ch = 596, 335
@@ -530,7 +533,7 @@ def run_reference(args):
     secs = max(1.0, min(args.ref_seconds, 120.0 / max(args.warmup + args.steps, 1)))
     rate = None
     for k in range(args.warmup + args.steps):
-        b = cpu_baseline(seconds_target=secs, threads=threads, rate_hint=rate)
+        b = cpu_baseline(seconds_target=secs, threads=threads, rate_hint=rate, twin=False)
         rate = b["rate_rays_per_s"]
         if k >= args.warmup:
             per_step.append(b["value"])
